@@ -1,0 +1,125 @@
+// Shared definitions of the sm_103a ring-arithmetic backend: tensor views as kernels see them,
+// exact 64/128-bit modular arithmetic, and launch helpers.
+//
+// The arithmetic reproduces the reference's integer formulas exactly (same inputs -> same
+// representatives), because downstream base-conversion corrections depend on the
+// representative, not only on the residue:
+//   Barrett multiplication by a constant   cyclosubfield-dbfv/src/hal/ntt.rs:126-158
+//   Montgomery reductions (R = 2^64)       cyclosubfield-dbfv/src/hal/mont.rs:36-76
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/halcuda.h"
+
+typedef __int128 i128;
+typedef unsigned __int128 u128;
+
+#define HC_MAX_MODS 96     // RNS rows per call whose moduli travel as kernel parameters
+#define HC_MAX_TERMS 64    // inner-product terms per call
+#define HC_MAX_STAGES 40   // NTT stages per plan (2^40-point transforms)
+
+// ------------------------------------------------------------------------------------------
+// Views
+// ------------------------------------------------------------------------------------------
+
+/// A kernel-side 4-D view: shape plus element strides; `s3` is implicitly 1. Broadcast
+/// sources carry stride 0 in the broadcast dimensions (`b3` marks a broadcast dimension 3).
+struct KView {
+    char* p;
+    int64_t n0, n1, n2, n3;
+    int64_t s0, s1, s2;
+    int32_t b3;
+};
+
+template <typename T>
+__device__ __forceinline__ T* kat(const KView& v, int64_t i, int64_t j, int64_t k, int64_t l) {
+    return reinterpret_cast<T*>(v.p) + i * v.s0 + j * v.s1 + k * v.s2 + (v.b3 ? 0 : l);
+}
+
+/// Montgomery moduli of one call, by value in the kernel's parameter space.
+struct KMods {
+    int64_t n[HC_MAX_MODS];
+    int64_t ninv[HC_MAX_MODS];
+    int64_t r2[HC_MAX_MODS];
+    int64_t r3[HC_MAX_MODS];
+};
+
+// ------------------------------------------------------------------------------------------
+// Exact arithmetic
+// ------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ int64_t wadd(int64_t a, int64_t b) { return (int64_t)((uint64_t)a + (uint64_t)b); }
+__device__ __forceinline__ int64_t wsub(int64_t a, int64_t b) { return (int64_t)((uint64_t)a - (uint64_t)b); }
+
+/// Barrett multiplication by the constant (z, u): q = floor((u x + 2^63) / 2^64), result
+/// z x + q n in wrapping 64-bit arithmetic (|result| <= 3n/4 for |x| <= 2^63).
+__device__ __forceinline__ int64_t bmul(int64_t z, int64_t u, int64_t x, int64_t n) {
+    int64_t hi = __mul64hi(u, x);
+    uint64_t lo = (uint64_t)u * (uint64_t)x;
+    int64_t q = hi + (int64_t)(lo >> 63);
+    return (int64_t)((uint64_t)z * (uint64_t)x + (uint64_t)q * (uint64_t)n);
+}
+
+/// Montgomery reduction of the 128-bit value hi:lo: ((x + m n) >> 64) with m = lo * (-n^-1).
+/// The low words of x and m n cancel, so the carry out of the low word is (lo != 0).
+__device__ __forceinline__ int64_t red128(uint64_t lo, int64_t hi, int64_t n, int64_t ninv) {
+    int64_t m = (int64_t)(lo * (uint64_t)ninv);
+    int64_t thi = __mul64hi(m, n);
+    return (int64_t)((uint64_t)hi + (uint64_t)thi + (uint64_t)(lo != 0));
+}
+__device__ __forceinline__ int64_t red128(i128 x, int64_t n, int64_t ninv) {
+    return red128((uint64_t)x, (int64_t)(x >> 64), n, ninv);
+}
+
+/// Montgomery product of two i64 values (the i128 product must stay within 2^63 n).
+__device__ __forceinline__ int64_t mul_mont(int64_t a, int64_t b, int64_t n, int64_t ninv) {
+    uint64_t lo = (uint64_t)a * (uint64_t)b;
+    int64_t hi = __mul64hi(a, b);
+    return red128(lo, hi, n, ninv);
+}
+
+/// Double Montgomery reduction of any i128 (x 2^-128 mod n, in [-n, n]).
+__device__ __forceinline__ int64_t double_red128(i128 x, int64_t n, int64_t ninv) {
+    uint64_t lo = (uint64_t)x;
+    int64_t m = (int64_t)(lo * (uint64_t)ninv);
+    i128 t = (i128)m * (i128)n;
+    i128 carry = (i128)(((u128)lo + (u128)(uint64_t)t) >> 64);
+    i128 r1 = (x >> 64) + (t >> 64) + carry;
+    return red128(r1, n, ninv);
+}
+
+__device__ __forceinline__ int64_t to_mont64(int64_t x, int64_t n, int64_t ninv, int64_t r2) {
+    return mul_mont(x, r2, n, ninv);
+}
+__device__ __forceinline__ int64_t to_mont128(i128 x, int64_t n, int64_t ninv, int64_t r3) {
+    return mul_mont(red128(x, n, ninv), r3, n, ninv);
+}
+
+__device__ __forceinline__ i128 ld128(const void* p) {
+    longlong2 v = *reinterpret_cast<const longlong2*>(p);
+    return (i128)(((u128)(uint64_t)v.y << 64) | (uint64_t)v.x);
+}
+__device__ __forceinline__ void st128(void* p, i128 x) {
+    longlong2 v;
+    v.x = (long long)(uint64_t)x;
+    v.y = (long long)(x >> 64);
+    *reinterpret_cast<longlong2*>(p) = v;
+}
+
+// ------------------------------------------------------------------------------------------
+// Host-side helpers shared by the translation units
+// ------------------------------------------------------------------------------------------
+namespace hc {
+
+void set_error(const std::string& msg);
+hc_status fail(hc_status st, const std::string& msg);
+hc_status cuda_check(cudaError_t e, const char* what);
+cudaStream_t stream_of(hc_context ctx);
+void count_launch(hc_context ctx, uint64_t n = 1);
+int num_sms(hc_context ctx);
+size_t max_smem_optin(hc_context ctx);
+
+}  // namespace hc

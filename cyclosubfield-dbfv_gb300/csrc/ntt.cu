@@ -1,0 +1,493 @@
+// Lazy radix-2/3 group NTTs along dimension 2 or 3 of a ring-element tensor.
+//
+// The reference applies, per cyclic factor and per stage, Cooley-Tukey butterflies whose twiddle
+// products are Barrett multiplications and whose sums stay unreduced; full reduction passes are
+// inserted only where a data-independent worst-case bound says the next stage could overflow
+// (cyclosubfield-dbfv/src/hal/ntt.rs:301-537, plan level :581-657). Because that schedule does
+// not depend on the data, the host simulates it once per plan and stores a *stage program*
+// (radix, geometry, reduce-before, twiddle-1 skip permission, fused final reduction/scaling)
+// next to the twiddle constants in device memory. The kernel executes the program over a tile
+// held in shared memory: a dimension-3 line (one CTA per line), or a block of dimension-2
+// columns (one CTA per column block). Each butterfly performs exactly the reference's integer
+// formula, so outputs are bit-identical; stages are not algebraically merged.
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+
+namespace {
+
+struct DevStage {
+    int32_t radix;      // 2 or 3
+    int32_t stride;     // element stride of the factor's digit within the axis (suffix product)
+    int32_t flen;       // factor length
+    int32_t stage_len;  // length of one block in this stage
+    int32_t tw_off;     // twiddle offset (pairs z,u): fwd r2: 1/block, fwd r3: 6/block, inv r2: 1, inv r3: 2
+    int32_t zeta_off;   // inverse radix-3: offset of (zeta, zeta2)
+    int32_t reduce_before;
+    int32_t skip_ok;    // forward only
+    int32_t last;       // last stage of the last factor (fwd: fusable reduction, inv: fused len^-1)
+    int32_t pad;
+};
+
+struct DevPlanHeader {
+    int64_t n;
+    int32_t len;
+    int32_t nfwd;
+    int32_t ninv;
+    int32_t ntw;
+    int64_t one_z, one_u, invlen_z, invlen_u;
+    DevStage fwd[HC_MAX_STAGES];
+    DevStage inv[HC_MAX_STAGES];
+    // followed by the twiddle table: ntw pairs (z, u)
+};
+
+// ---------------------------------------------------------------- host-side constants
+int64_t h_mul_mod(int64_t a, int64_t b, int64_t q) { return (int64_t)(((i128)a * (i128)b) % (i128)q); }
+int64_t h_pow_mod(int64_t b, uint64_t e, int64_t q) {
+    int64_t r = 1;
+    b %= q;
+    while (e) {
+        if (e & 1) r = h_mul_mod(r, b, q);
+        b = h_mul_mod(b, b, q);
+        e >>= 1;
+    }
+    return r;
+}
+bool is_pow2(uint64_t x) { return x && !(x & (x - 1)); }
+int64_t h_find_root(int64_t q, uint64_t n) {
+    uint64_t p = is_pow2(n) ? 2 : 3;
+    for (int64_t c = 2;; c++) {
+        int64_t root = h_pow_mod(c, (uint64_t)((q - 1) / (int64_t)n), q);
+        if (h_pow_mod(root, n / p, q) != 1) return root;
+    }
+}
+/// BarrettMul::new (src/hal/ntt.rs:134-144): centred z, u = round(-z 2^64 / n).
+void h_barrett(int64_t value, int64_t n, int64_t* z_out, int64_t* u_out) {
+    int64_t z = value % n;
+    if (2 * (i128)z > n) z -= n;
+    else if (2 * (i128)z < -n) z += n;
+    i128 a = -((i128)z << 64), b = n;
+    i128 u = a >= 0 ? (a + b / 2) / b : -((-a + b / 2) / b);
+    *z_out = z;
+    *u_out = (int64_t)u;
+}
+
+struct HostPlan {
+    DevPlanHeader h;
+    std::vector<int64_t> tw;  // pairs
+    void push(int64_t value) {
+        int64_t z, u;
+        h_barrett(value, h.n, &z, &u);
+        tw.push_back(z);
+        tw.push_back(u);
+    }
+    int32_t next_tw() const { return (int32_t)(tw.size() / 2); }
+};
+
+const u128 I64MAX = (u128)INT64_MAX;
+
+}  // namespace
+
+struct hc_ntt_plan_s {
+    void* dev;        // DevPlanHeader + twiddles
+    int64_t n;
+    int32_t len;
+    size_t bytes;
+};
+
+// ---------------------------------------------------------------- device kernel
+namespace {
+
+/// One stage of the forward transform over a tile of `len` x V elements in shared memory
+/// (element e, vector v at s[e * V + v]).
+__device__ __forceinline__ void fwd_stage(int64_t* s, int len, int V, const DevStage& st, const int64_t* tw,
+                                          int64_t n, int64_t one_z, int64_t one_u, bool reduce_output) {
+    const int radix = st.radix, S = st.stride, sub = st.stage_len / radix;
+    const int nblocks = st.flen / st.stage_len;
+    const bool fuse = st.last && reduce_output;
+    const int nbf = (len / radix) * V;
+    for (int b = threadIdx.x; b < nbf; b += blockDim.x) {
+        int v = b % V, bb = b / V;
+        int suffix = bb % S, rest = bb / S;
+        int jj = rest % sub, rest2 = rest / sub;
+        int block = rest2 % nblocks, prefix = rest2 / nblocks;
+        int e = (prefix * st.flen + block * st.stage_len + jj) * S + suffix;
+        int64_t* x = s + (int64_t)e * V + v;
+        int64_t* y = x + (int64_t)sub * S * V;
+        if (radix == 2) {
+            int64_t z = tw[2 * (st.tw_off + block)], u = tw[2 * (st.tw_off + block) + 1];
+            bool skip = st.skip_ok && z == 1;
+            int64_t a = *x, t = skip ? *y : bmul(z, u, *y, n);
+            int64_t o0 = wadd(a, t), o1 = wsub(a, t);
+            if (fuse) {
+                o0 = bmul(one_z, one_u, o0, n);
+                o1 = bmul(one_z, one_u, o1, n);
+            }
+            *x = o0;
+            *y = o1;
+        } else {
+            int64_t* zp = y + (int64_t)sub * S * V;
+            const int64_t* w = tw + 2 * (st.tw_off + 6 * block);
+            bool skip = st.skip_ok && w[0] == 1;
+            int64_t a = *x, bv = *y, c = *zp;
+            int64_t t_b = skip ? bv : bmul(w[0], w[1], bv, n);
+            int64_t t_bz = bmul(w[2], w[3], bv, n);
+            int64_t t_bzz = bmul(w[4], w[5], bv, n);
+            int64_t t_c = skip ? c : bmul(w[6], w[7], c, n);
+            int64_t t_cz = bmul(w[8], w[9], c, n);
+            int64_t t_czz = bmul(w[10], w[11], c, n);
+            int64_t o0 = wadd(wadd(a, t_b), t_c), o1 = wadd(wadd(a, t_bz), t_czz), o2 = wadd(wadd(a, t_bzz), t_cz);
+            if (fuse) {
+                o0 = bmul(one_z, one_u, o0, n);
+                o1 = bmul(one_z, one_u, o1, n);
+                o2 = bmul(one_z, one_u, o2, n);
+            }
+            *x = o0;
+            *y = o1;
+            *zp = o2;
+        }
+    }
+}
+
+__device__ __forceinline__ void inv_stage(int64_t* s, int len, int V, const DevStage& st, const int64_t* tw,
+                                          int64_t n, int64_t il_z, int64_t il_u) {
+    const int radix = st.radix, S = st.stride, sub = st.stage_len / radix;
+    const int nblocks = st.flen / st.stage_len;
+    const bool fused = st.last;
+    const int nbf = (len / radix) * V;
+    for (int b = threadIdx.x; b < nbf; b += blockDim.x) {
+        int v = b % V, bb = b / V;
+        int suffix = bb % S, rest = bb / S;
+        int jj = rest % sub, rest2 = rest / sub;
+        int block = rest2 % nblocks, prefix = rest2 / nblocks;
+        int e = (prefix * st.flen + block * st.stage_len + jj) * S + suffix;
+        int64_t* x = s + (int64_t)e * V + v;
+        int64_t* y = x + (int64_t)sub * S * V;
+        if (radix == 2) {
+            int64_t yz, yu;
+            if (fused) {
+                yz = il_z;
+                yu = il_u;
+            } else {
+                yz = tw[2 * (st.tw_off + block)];
+                yu = tw[2 * (st.tw_off + block) + 1];
+            }
+            bool skip = !fused && yz == 1;
+            int64_t y0 = *x, y1 = *y;
+            int64_t sum = wadd(y0, y1), dif = wsub(y0, y1);
+            *x = fused ? bmul(yz, yu, sum, n) : sum;
+            *y = skip ? dif : bmul(yz, yu, dif, n);
+        } else {
+            int64_t* zp = y + (int64_t)sub * S * V;
+            int64_t yz, yu, zz, zu;
+            if (fused) {
+                yz = zz = il_z;
+                yu = zu = il_u;
+            } else {
+                const int64_t* w = tw + 2 * (st.tw_off + 2 * block);
+                yz = w[0], yu = w[1], zz = w[2], zu = w[3];
+            }
+            bool skip = !fused && yz == 1;
+            const int64_t* zt = tw + 2 * st.zeta_off;
+            int64_t y0 = *x, y1 = *y, y2 = *zp;
+            int64_t y1z = bmul(zt[0], zt[1], y1, n), y1zz = bmul(zt[2], zt[3], y1, n);
+            int64_t y2z = bmul(zt[0], zt[1], y2, n), y2zz = bmul(zt[2], zt[3], y2, n);
+            int64_t s0 = wadd(wadd(y0, y1), y2);
+            int64_t sy = wadd(wadd(y0, y1zz), y2z), sz = wadd(wadd(y0, y1z), y2zz);
+            *x = fused ? bmul(yz, yu, s0, n) : s0;
+            *y = skip ? sy : bmul(yz, yu, sy, n);
+            *zp = skip ? sz : bmul(zz, zu, sz, n);
+        }
+    }
+}
+
+struct PlanPtrs {
+    const DevPlanHeader* p[HC_MAX_MODS];
+};
+
+/// mode 0: forward (reduced), 1: inverse, 2: forward unreduced + Montgomery multiplication by `mul`.
+/// dim 3: tile = line (i, j, k), element e at l = e.  dim 2: tile = (i, j, column block),
+/// element (e, v) at k = e, l = cb * V + v.
+__global__ void __launch_bounds__(256) ntt_tile_kernel(KView t, PlanPtrs plans, int dim, int mode, KView mul,
+                                                       KMods mods, int V, int ntile2, int use_smem) {
+    extern __shared__ int64_t smem[];
+    const int len = dim == 3 ? (int)t.n3 : (int)t.n2;
+    int64_t tile = blockIdx.x;
+    int64_t i, j, k = 0, cb = 0;
+    if (dim == 3) {
+        k = tile % t.n2;
+        int64_t r = tile / t.n2;
+        j = r % t.n1;
+        i = r / t.n1;
+    } else {
+        cb = tile % ntile2;
+        int64_t r = tile / ntile2;
+        j = r % t.n1;
+        i = r / t.n1;
+    }
+    const DevPlanHeader* P = plans.p[j];
+    const int64_t n = P->n;
+    const int64_t* tw = reinterpret_cast<const int64_t*>(P + 1);
+    int64_t* g = reinterpret_cast<int64_t*>(t.p) + i * t.s0 + j * t.s1 + (dim == 3 ? k * t.s2 : cb * V);
+    const int64_t ge = dim == 3 ? 1 : t.s2;  // global stride of element e
+    const int64_t ncol = dim == 3 ? 1 : t.n3 - cb * V;
+    const int total = len * V;
+    int64_t* s = smem;
+    if (use_smem) {
+        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+            int e = idx / V, v = idx % V;
+            s[idx] = v < ncol ? g[e * ge + v] : 0;
+        }
+        __syncthreads();
+    }
+    // without shared memory (lines too long for it) the tile is worked on in place in global
+    // memory; this is only valid for dim 3 (V == 1, unit element stride)
+    if (!use_smem) s = g;
+    const bool inverse = mode == 1;
+    const int nst = inverse ? P->ninv : P->nfwd;
+    for (int si = 0; si < nst; si++) {
+        const DevStage& st = inverse ? P->inv[si] : P->fwd[si];
+        if (st.reduce_before) {
+            for (int idx = threadIdx.x; idx < total; idx += blockDim.x) s[idx] = bmul(P->one_z, P->one_u, s[idx], n);
+            __syncthreads();
+        }
+        if (inverse) inv_stage(s, len, V, st, tw, n, P->invlen_z, P->invlen_u);
+        else fwd_stage(s, len, V, st, tw, n, P->one_z, P->one_u, mode == 0);
+        __syncthreads();
+    }
+    // plans without factors (length 1): the inverse scales by 1^-1, the reduced forward
+    // reduces; an unreduced forward leaves the data unchanged
+    if (nst == 0 && (mode == 0 || mode == 1)) {
+        int64_t fz = inverse ? P->invlen_z : P->one_z, fu = inverse ? P->invlen_u : P->one_u;
+        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) s[idx] = bmul(fz, fu, s[idx], n);
+        __syncthreads();
+    }
+    if (mode == 2) {
+        const int64_t mn = mods.n[j], mi = mods.ninv[j];
+        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+            int e = idx / V, v = idx % V;
+            if (v >= ncol) continue;
+            int64_t kk = dim == 3 ? k : e, ll = dim == 3 ? e : cb * V + v;
+            int64_t m = *kat<int64_t>(mul, i, j, kk, ll);
+            s[idx] = mul_mont(s[idx], m, mn, mi);
+        }
+        __syncthreads();
+    }
+    if (use_smem) {
+        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+            int e = idx / V, v = idx % V;
+            if (v < ncol) g[e * ge + v] = s[idx];
+        }
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- plan construction
+namespace hc {
+
+/// Builds the stage programs and twiddle tables of CpuNTTPlan::new (src/hal/ntt.rs:561-566,
+/// LazyFactorNTT::new :216-281) and simulates the bound tracking of `apply` (:581-657) and of
+/// the factor transforms (:301-537).
+hc_status build_plan(hc_context ctx, const hc_modulus* m, const size_t* shape, size_t k, hc_ntt_plan* out) {
+    const int64_t n = m->n;
+    if (n <= 1 || n % 2 == 0 || n >= ((int64_t)1 << 62)) return fail(HC_ERR_ARG, "NTT modulus must be odd and < 2^62");
+    HostPlan hp;
+    std::memset(&hp.h, 0, sizeof(hp.h));
+    hp.h.n = n;
+    std::vector<size_t> factors;
+    size_t len = 1;
+    for (size_t i = 0; i < k; i++) {
+        len *= shape[i];
+        if (shape[i] > 1) factors.push_back(shape[i]);
+    }
+    if (len > ((size_t)1 << 30)) return fail(HC_ERR_UNSUPPORTED, "NTT length too large");
+    hp.h.len = (int32_t)len;
+    int64_t z, u;
+    h_barrett(1, n, &z, &u);
+    hp.h.one_z = z, hp.h.one_u = u;
+    int64_t inv_len = h_pow_mod((int64_t)(len % (size_t)n), (uint64_t)(n - 2), n);
+    h_barrett(inv_len, n, &z, &u);
+    hp.h.invlen_z = z, hp.h.invlen_u = u;
+
+    u128 fbound = 2 * (u128)n, ibound = 2 * (u128)n;
+    size_t suffix = 1;
+    for (size_t f : factors) suffix *= f;
+    for (size_t fi = 0; fi < factors.size(); fi++) {
+        const size_t flen = factors[fi];
+        suffix /= flen;
+        const bool last_factor = fi + 1 == factors.size();
+        const bool r2 = is_pow2(flen);
+        if (!r2) {
+            size_t l = flen;
+            while (l > 1) {
+                if (l % 3) return fail(HC_ERR_ARG, "NTT length must be a power of 2 or a power of 3");
+                l /= 3;
+            }
+        }
+        if ((n - 1) % (int64_t)flen) return fail(HC_ERR_ARG, "modulus doesn't support roots of unity of this order");
+        if (r2 && 2 * (u128)n > I64MAX) return fail(HC_ERR_ARG, "modulus too large for lazy radix-2 butterflies");
+        if (!r2 && 3 * (u128)n > I64MAX) return fail(HC_ERR_ARG, "modulus too large for lazy radix-3 butterflies");
+        const int radix = r2 ? 2 : 3;
+        int64_t root = h_find_root(n, flen);
+        int64_t inv_root = h_pow_mod(root, flen - 1, n);
+        // twiddles per stage, in the residue-tree order of src/hal/ntt.rs:226-232 / :250-270
+        std::vector<std::vector<int64_t>> fw, iv;
+        std::vector<size_t> exps{0};
+        int64_t zeta = 0, zeta2 = 0;
+        if (!r2) {
+            zeta = h_pow_mod(root, flen / 3, n);
+            zeta2 = h_mul_mod(zeta, zeta, n);
+        }
+        while (exps.size() < flen) {
+            std::vector<int64_t> f1, i1;
+            for (size_t e : exps) {
+                if (r2) {
+                    f1.push_back(h_pow_mod(root, e / 2, n));
+                    i1.push_back(h_pow_mod(inv_root, e / 2, n));
+                } else {
+                    int64_t v = h_pow_mod(root, e / 3, n), v2 = h_mul_mod(v, v, n);
+                    f1.push_back(v);
+                    f1.push_back(h_mul_mod(zeta, v, n));
+                    f1.push_back(h_mul_mod(zeta2, v, n));
+                    f1.push_back(v2);
+                    f1.push_back(h_mul_mod(zeta, v2, n));
+                    f1.push_back(h_mul_mod(zeta2, v2, n));
+                    int64_t vi = h_pow_mod(inv_root, e / 3, n);
+                    i1.push_back(vi);
+                    i1.push_back(h_mul_mod(vi, vi, n));
+                }
+            }
+            fw.push_back(f1);
+            iv.push_back(i1);
+            std::vector<size_t> next;
+            for (size_t e : exps)
+                for (int c = 0; c < radix; c++) next.push_back(e / radix + c * (flen / radix));
+            exps.swap(next);
+        }
+        const size_t nst = fw.size();
+        int32_t zeta_off = 0;
+        if (!r2) {
+            zeta_off = hp.next_tw();
+            hp.push(zeta);
+            hp.push(zeta2);
+        }
+        // forward program (src/hal/ntt.rs:312-353, :355-411)
+        size_t stage_len = flen;
+        for (size_t s = 0; s < nst; s++) {
+            if (hp.h.nfwd >= HC_MAX_STAGES) return fail(HC_ERR_UNSUPPORTED, "too many NTT stages");
+            DevStage& st = hp.h.fwd[hp.h.nfwd++];
+            st.radix = radix;
+            st.stride = (int32_t)suffix;
+            st.flen = (int32_t)flen;
+            st.stage_len = (int32_t)stage_len;
+            st.tw_off = hp.next_tw();
+            for (int64_t v : fw[s]) hp.push(v);
+            st.last = last_factor && s + 1 == nst;
+            const u128 grow = r2 ? (u128)n : 2 * (u128)n;
+            if (fbound + grow > I64MAX) {
+                st.reduce_before = 1;
+                fbound = (u128)n;
+            }
+            st.skip_ok = (u128)radix * fbound <= I64MAX;
+            // the unreduced bound is tracked; a fused final reduction only affects the returned
+            // bound of the very last stage, which nothing reads
+            fbound = st.skip_ok ? (u128)radix * fbound : fbound + grow;
+            stage_len /= radix;
+        }
+        // inverse program (src/hal/ntt.rs:438-478, :480-533): stages in reverse order
+        for (size_t si = nst; si-- > 0;) {
+            if (hp.h.ninv >= HC_MAX_STAGES) return fail(HC_ERR_UNSUPPORTED, "too many NTT stages");
+            DevStage& st = hp.h.inv[hp.h.ninv++];
+            st.radix = radix;
+            st.stride = (int32_t)suffix;
+            st.flen = (int32_t)flen;
+            size_t sl = flen;
+            for (size_t q = 0; q < si; q++) sl /= radix;
+            st.stage_len = (int32_t)sl;
+            st.tw_off = hp.next_tw();
+            for (int64_t v : iv[si]) hp.push(v);
+            st.zeta_off = zeta_off;
+            st.last = last_factor && si == 0;
+            if ((u128)radix * ibound > I64MAX) {
+                st.reduce_before = 1;
+                ibound = (u128)n;
+            }
+            ibound = st.last ? (u128)n : (u128)radix * ibound;
+        }
+    }
+    hp.h.ntw = hp.next_tw();
+    size_t bytes = sizeof(DevPlanHeader) + hp.tw.size() * sizeof(int64_t);
+    std::vector<char> blob(bytes);
+    std::memcpy(blob.data(), &hp.h, sizeof(DevPlanHeader));
+    if (!hp.tw.empty()) std::memcpy(blob.data() + sizeof(DevPlanHeader), hp.tw.data(), hp.tw.size() * sizeof(int64_t));
+    void* dev = nullptr;
+    if (cudaMalloc(&dev, bytes) != cudaSuccess) return fail(HC_ERR_OOM, "cannot allocate NTT plan");
+    hc_status st = cuda_check(cudaMemcpy(dev, blob.data(), bytes, cudaMemcpyHostToDevice), "plan upload");
+    if (st != HC_OK) {
+        cudaFree(dev);
+        return st;
+    }
+    auto* plan = new hc_ntt_plan_s();
+    plan->dev = dev;
+    plan->n = n;
+    plan->len = (int32_t)len;
+    plan->bytes = bytes;
+    *out = plan;
+    return HC_OK;
+}
+
+hc_status destroy_plan(hc_ntt_plan p) {
+    if (!p) return HC_OK;
+    cudaFree(p->dev);
+    delete p;
+    return HC_OK;
+}
+
+int64_t plan_modulus(hc_ntt_plan p) { return p->n; }
+int32_t plan_len(hc_ntt_plan p) { return p->len; }
+const void* plan_device(hc_ntt_plan p) { return p->dev; }
+
+/// Launches the tile kernel for one HAL NTT call (mode 0 ntt, 1 intt, 2 ntt_mul).
+hc_status launch_ntt(hc_context ctx, const KView& t, const hc_ntt_plan* plans, size_t nplans, int dim, int mode,
+                     const KView& mul, const KMods& mods) {
+    if ((int64_t)nplans != t.n1) return fail(HC_ERR_SHAPE, "one NTT plan per RNS row required");
+    if (nplans > HC_MAX_MODS) return fail(HC_ERR_UNSUPPORTED, "too many RNS rows in one call");
+    const int64_t len = dim == 3 ? t.n3 : t.n2;
+    PlanPtrs pp;
+    for (size_t j = 0; j < nplans; j++) {
+        if (!plans[j]) return fail(HC_ERR_ARG, "null NTT plan");
+        if (plans[j]->len != len) return fail(HC_ERR_SHAPE, "NTT plan length does not match the transformed dimension");
+        pp.p[j] = reinterpret_cast<const DevPlanHeader*>(plans[j]->dev);
+    }
+    if (t.n0 == 0 || t.n1 == 0 || t.n2 == 0 || t.n3 == 0) return HC_OK;
+    int V = 1;
+    int64_t ntile2 = 1;
+    if (dim == 2) {
+        // as many dimension-3 columns per tile as fit into 48 KB of shared memory (<= 64)
+        V = 64;
+        while (V > 1 && (len * V * 8 > 49152 || V / 2 >= t.n3)) V /= 2;
+        ntile2 = (t.n3 + V - 1) / V;
+    }
+    size_t smem = (size_t)len * V * 8;
+    int use_smem = 1;
+    size_t maxs = max_smem_optin(ctx);
+    if (smem > maxs) {
+        if (dim == 2) return fail(HC_ERR_UNSUPPORTED, "dimension-2 NTT length too large");
+        use_smem = 0;
+        smem = 0;
+    }
+    if (smem > 49152) {
+        cudaError_t e = cudaFuncSetAttribute(ntt_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return cuda_check(e, "ntt smem attribute");
+    }
+    int64_t tiles = dim == 3 ? t.n0 * t.n1 * t.n2 : t.n0 * t.n1 * ntile2;
+    if (tiles > 0x7fffffff) return fail(HC_ERR_UNSUPPORTED, "too many NTT tiles in one call");
+    ntt_tile_kernel<<<(unsigned)tiles, 256, smem, stream_of(ctx)>>>(t, pp, dim, mode, mul, mods, V, (int)ntile2,
+                                                                    use_smem);
+    count_launch(ctx);
+    return cuda_check(cudaGetLastError(), "ntt kernel launch");
+}
+
+}  // namespace hc

@@ -62,11 +62,13 @@ def view(a, i128=False):
         assert a.ndim == 4
         strides = [s // 8 for s in a.strides]
         shape = a.shape
+    if a.size == 0:  # numpy reports arbitrary strides for empty arrays
+        strides = [shape[1] * shape[2] * shape[3], shape[2] * shape[3], shape[3], 1]
     v = OrView()
     v.ptr = a.ctypes.data
     for d in range(4):
         v.shape[d] = shape[d]
-        v.strides[d] = strides[d] if shape[d] > 1 else (strides[d] if strides[d] else 0)
+        v.strides[d] = strides[d]
     return v
 
 

@@ -4,8 +4,10 @@ import sys
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-if ROOT not in sys.path:
-    sys.path.insert(0, ROOT)
+PKG = os.path.join(ROOT, "cyclosubfield-dbfv_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
 
 
 def pytest_configure(config):
@@ -19,3 +21,12 @@ def po():
 
     pyoracle.lib()
     return pyoracle
+
+
+@pytest.fixture(scope="session")
+def be():
+    import halcuda
+
+    backend = halcuda.CudaBackend(0)
+    yield backend
+    backend.close()
