@@ -1,0 +1,1443 @@
+// Ring and BFV layers on the GPU (include/ringcuda.h).
+//
+// Host-side state mirrors the reference's RingContext (cyclosubfield-dbfv/src/ring.rs:594-652):
+// the field's group data, the RNS factors with their Montgomery moduli and NTT plans, the
+// NTT-domain CRT kernels, and caches for base conversions, gadget conversions and Galois
+// permutations. All constants are computed on the host without big integers (products of primes
+// are evaluated modulo each prime). The per-element work runs as sm_103a kernels: the HAL kernels
+// for transforms and pointwise steps, and the fused kernels of ring_kernels.cu for base
+// conversion, key switching, Galois automorphisms and tensor products.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <memory>
+#include <set>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/ringcuda.h"
+#include "common.cuh"
+
+namespace hc {
+hc_status launch_bconv_fused(hc_context ctx, const KView& src, const KView& dst, const int64_t* qinv,
+                             const int64_t* mat, const int64_t* qmodp, const int32_t* ucol, int r, int rd, int nb,
+                             int shift, int chunk, const KMods& sm, const KMods& dm, int64_t ns);
+hc_status launch_galois(hc_context ctx, const KView& d, const KView& s, const uint32_t* p2, const uint32_t* p3);
+hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys, int nterms, const KView* add0,
+                           const KView* add1, int full0, int full1, const KView& dst, const KMods& m,
+                           const int64_t* one_dev, const uint32_t* p2, const uint32_t* p3);
+hc_status launch_tensor(hc_context ctx, const KView& d, const KView& lhs, const KView& rhs, const KMods& m, int f0,
+                        int f1, int f2);
+}  // namespace hc
+
+using namespace hc;
+
+namespace {
+
+const i128 I128MAX = (i128)(~(u128)0 >> 1);
+
+struct Fail {
+    hc_status st;
+};
+#define CK(expr)                                \
+    do {                                        \
+        hc_status _st = (expr);                 \
+        if (_st != HC_OK) throw Fail{_st};      \
+    } while (0)
+#define REQUIRE(cond, st, msg)                  \
+    do {                                        \
+        if (!(cond)) throw Fail{fail(st, msg)}; \
+    } while (0)
+
+template <typename F>
+hc_status guard(F f) {
+    try {
+        f();
+        return HC_OK;
+    } catch (const Fail& e) {
+        return e.st;
+    } catch (const std::exception& e) {
+        return fail(HC_ERR_ARG, e.what());
+    }
+}
+
+// ------------------------------------------------------------------------- integer helpers
+int64_t mulm(int64_t a, int64_t b, int64_t p) { return (int64_t)(((i128)a * b) % p); }
+int64_t emod(int64_t a, int64_t p) {
+    int64_t r = a % p;
+    return r < 0 ? r + p : r;
+}
+int64_t powm(int64_t b, uint64_t e, int64_t p) {
+    int64_t r = 1;
+    b = emod(b, p);
+    while (e) {
+        if (e & 1) r = mulm(r, b, p);
+        b = mulm(b, b, p);
+        e >>= 1;
+    }
+    return r;
+}
+int64_t invm(int64_t a, int64_t p) { return powm(emod(a, p), (uint64_t)(p - 2), p); }
+/// x * 2^64 mod p with the sign of x (Rust's truncating `%`, src/ring.rs:109)
+int64_t mont_repr(int64_t x, int64_t p) { return (int64_t)(((i128)x << 64) % (i128)p); }
+/// representative in [-(p-1)/2, (p-1)/2] (feanor-math smallest_lift)
+int64_t centred(int64_t x, int64_t p) {
+    x = emod(x, p);
+    return x > (p - 1) / 2 ? x - p : x;
+}
+int64_t from_mont(int64_t x, int64_t p) { return mulm(emod(x, p), invm(mont_repr(1, p), p), p); }
+uint64_t umulm(uint64_t a, uint64_t b, uint64_t m) { return (uint64_t)((u128)a * b % m); }
+
+bool is_prime64(uint64_t n) {
+    if (n < 2) return false;
+    static const uint64_t bases[] = {2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37};
+    for (uint64_t p : bases)
+        if (n % p == 0) return n == p;
+    uint64_t d = n - 1;
+    int s = 0;
+    while (!(d & 1)) d >>= 1, s++;
+    for (uint64_t a : bases) {
+        uint64_t x = 1, b = a % n, e = d;
+        while (e) {
+            if (e & 1) x = umulm(x, b, n);
+            b = umulm(b, b, n);
+            e >>= 1;
+        }
+        if (x == 1 || x == n - 1) continue;
+        bool comp = true;
+        for (int i = 1; i < s && comp; i++) {
+            x = umulm(x, x, n);
+            if (x == n - 1) comp = false;
+        }
+        if (comp) return false;
+    }
+    return true;
+}
+
+size_t bitlen_u128(u128 v) {
+    size_t b = 0;
+    while (v) b++, v >>= 1;
+    return b;
+}
+
+/// Exact bit length of a product of primes.
+size_t product_bits(const std::vector<int64_t>& ps) {
+    std::vector<uint64_t> limbs{1};
+    for (int64_t p : ps) {
+        u128 carry = 0;
+        for (auto& w : limbs) {
+            u128 t = (u128)w * (uint64_t)p + carry;
+            w = (uint64_t)t;
+            carry = t >> 64;
+        }
+        if (carry) limbs.push_back((uint64_t)carry);
+    }
+    return 64 * (limbs.size() - 1) + bitlen_u128(limbs.back());
+}
+
+// ------------------------------------------------------------------------- fields
+/// Hard-coded field data (cyclosubfield-dbfv/src/field.rs:529-769): conductor m, the prime m',
+/// generators of Gal(M'|L') and Gal(M_K|K) in (Z/mZ)*, and the cyclic decompositions
+/// (generator, order) of Gal(L'|Q) and Gal(K|Q), L'-factors first.
+struct FieldSpec {
+    const char* name;
+    uint64_t m, m_prime;
+    std::vector<uint64_t> gens_lp, gens_k;
+    std::vector<std::pair<uint64_t, size_t>> cyc_lp, cyc_k;
+};
+
+const std::vector<FieldSpec>& field_specs() {
+    static const std::vector<FieldSpec> specs = {
+        {"field_36864", 8536255, 13, {}, {3283177}, {{3939811, 4}, {7879621, 3}},
+         {{7316791, 2}, {1169351, 3}, {4560466, 8}, {8071246, 64}}},
+        {"field_49152", 35297665, 13, {29867256}, {2715207}, {{32582461, 4}},
+         {{1291681, 3}, {20965738, 64}, {30783429, 64}}},
+        {"field_192", 90627, 3, {}, {30211}, {{60419, 2}}, {{45427, 2}, {4183, 3}, {47533, 16}}},
+        {"field_18", 1729, 19, {274}, {457}, {{1548, 3}}, {{1483, 2}, {932, 3}}},
+        {"field_16", 257, 1, {}, {2}, {}, {{155, 16}}},
+        {"field_2", 7, 1, {}, {2}, {}, {{6, 2}}},
+        {"field_32", 255, 17, {}, {137}, {{241, 16}}, {{52, 2}}},
+    };
+    return specs;
+}
+
+struct Field {
+    FieldSpec spec;
+    std::vector<uint64_t> m_factors;
+    std::vector<std::pair<uint64_t, size_t>> cyc;  // L' factors then K factors
+    size_t nlp;                                    // number of L' factors
+    size_t deg_l, deg_lp, deg_k;
+    std::vector<uint64_t> gal_ml, gal_lp, gal_k;   // Gal(M|L), Gal(M'|L'), Gal(M_K|K)
+    std::unordered_map<uint64_t, size_t> tindex;   // transversal element -> flat index
+
+    uint64_t m() const { return spec.m; }
+    uint64_t m_k() const { return spec.m / spec.m_prime; }
+
+    static std::vector<uint64_t> subgroup(const std::vector<uint64_t>& gens, uint64_t m) {
+        std::set<uint64_t> el{1};
+        std::vector<uint64_t> todo{1};
+        while (!todo.empty()) {
+            uint64_t x = todo.back();
+            todo.pop_back();
+            for (uint64_t g : gens) {
+                uint64_t y = umulm(x, g, m);
+                if (el.insert(y).second) todo.push_back(y);
+            }
+        }
+        return std::vector<uint64_t>(el.begin(), el.end());
+    }
+    /// elements g_1^e_1 ... g_k^e_k in row-major order of (e_1, ..., e_k)
+    std::vector<uint64_t> transversal(size_t from, size_t to) const {
+        std::vector<uint64_t> out{1};
+        for (size_t f = from; f < to; f++) {
+            std::vector<uint64_t> next;
+            next.reserve(out.size() * cyc[f].second);
+            for (uint64_t x : out) {
+                uint64_t pw = 1;
+                for (size_t e = 0; e < cyc[f].second; e++) {
+                    next.push_back(umulm(x, pw, spec.m));
+                    pw = umulm(pw, cyc[f].first, spec.m);
+                }
+            }
+            out.swap(next);
+        }
+        return out;
+    }
+    std::vector<size_t> orders(size_t from, size_t to) const {
+        std::vector<size_t> o;
+        for (size_t f = from; f < to; f++) o.push_back(cyc[f].second);
+        return o;
+    }
+    uint64_t rou_order() const {
+        uint64_t l = 1;
+        for (auto& c : cyc) {
+            uint64_t a = l, b = c.second;
+            while (b) std::swap(a, b), b %= a;
+            l = l / a * c.second;
+        }
+        return spec.m * l;
+    }
+    /// exponents of g in the cyclic decomposition of Gal(L|Q) (src/field.rs:338-352)
+    std::vector<size_t> gal_to_shift(uint64_t g) const {
+        uint64_t gm = g % spec.m;
+        size_t idx = (size_t)-1;
+        for (uint64_t h : gal_ml) {
+            auto it = tindex.find(umulm(gm, h, spec.m));
+            if (it != tindex.end()) {
+                idx = it->second;
+                break;
+            }
+        }
+        REQUIRE(idx != (size_t)-1, HC_ERR_ARG, "not an element of (Z/mZ)* / inconsistent field data");
+        std::vector<size_t> s(cyc.size());
+        for (size_t f = cyc.size(); f-- > 0;) {
+            s[f] = idx % cyc[f].second;
+            idx /= cyc[f].second;
+        }
+        return s;
+    }
+
+    static Field make(const std::string& name) {
+        const FieldSpec* sp = nullptr;
+        for (auto& s : field_specs())
+            if (name == s.name) sp = &s;
+        REQUIRE(sp, HC_ERR_ARG, "unknown field " + name);
+        Field f;
+        f.spec = *sp;
+        if (sp->m_prime != 1) f.m_factors.push_back(sp->m_prime);
+        uint64_t rest = sp->m / sp->m_prime;
+        for (uint64_t p = 3; rest > 1; p += 2)
+            if (rest % p == 0) rest /= p, f.m_factors.push_back(p);
+        f.cyc = sp->cyc_lp;
+        f.cyc.insert(f.cyc.end(), sp->cyc_k.begin(), sp->cyc_k.end());
+        f.nlp = sp->cyc_lp.size();
+        f.deg_l = f.deg_lp = 1;
+        for (size_t i = 0; i < f.cyc.size(); i++) {
+            f.deg_l *= f.cyc[i].second;
+            if (i < f.nlp) f.deg_lp *= f.cyc[i].second;
+        }
+        f.deg_k = f.deg_l / f.deg_lp;
+        f.gal_lp = subgroup(sp->gens_lp, sp->m);
+        f.gal_k = subgroup(sp->gens_k, sp->m);
+        std::vector<uint64_t> all = sp->gens_lp;
+        all.insert(all.end(), sp->gens_k.begin(), sp->gens_k.end());
+        f.gal_ml = subgroup(all, sp->m);
+        std::vector<uint64_t> tr = f.transversal(0, f.cyc.size());
+        for (size_t i = 0; i < tr.size(); i++) f.tindex[tr[i]] = i;
+        return f;
+    }
+};
+
+uint64_t inv_mod_u(uint64_t a, uint64_t n) {
+    i128 r0 = (i128)(a % n), r1 = n, s0 = 1, s1 = 0;
+    while (r1) {
+        i128 q = r0 / r1, t = r0 - q * r1;
+        r0 = r1, r1 = t;
+        t = s0 - q * s1;
+        s0 = s1, s1 = t;
+    }
+    i128 v = (s0 * r0) % (i128)n;
+    return (uint64_t)(v < 0 ? v + n : v);
+}
+uint64_t crt2(uint64_t a1, uint64_t m1, uint64_t a2, uint64_t m2) {
+    if (m1 == 1) return a2 % m2;
+    if (m2 == 1) return a1 % m1;
+    uint64_t k = umulm((a2 + m2 - a1 % m2) % m2, inv_mod_u(m1 % m2, m2), m2);
+    return (uint64_t)(((u128)a1 + (u128)m1 * k) % ((u128)m1 * m2));
+}
+
+// ------------------------------------------------------------------------- prime sampling
+/// Largest prime <= bound that is 1 mod m, stepping down (src/ring.rs:136-146).
+int64_t prime_below(int64_t bound, int64_t m) {
+    int64_t c = bound - (bound - 1) % m;
+    while (!is_prime64((uint64_t)c)) {
+        c -= m;
+        REQUIRE(c > 0, HC_ERR_ARG, "no suitable prime");
+    }
+    return c;
+}
+/// Adds primes of at most `each` bits until the product has `min_bits` (src/ring.rs:150-183).
+std::vector<int64_t> sample_primes(std::vector<int64_t> have, size_t min_bits, size_t max_bits, size_t each,
+                                   int64_t m) {
+    const std::vector<int64_t> start = have;
+    double bits = 0;
+    for (int64_t p : have) bits += std::log2((double)p);
+    int64_t ub = (int64_t)1 << each;
+    while (bits < (double)min_bits) {
+        double remaining = (double)min_bits - bits, allowed;
+        if (remaining < (double)each) allowed = std::fmin((double)max_bits - bits, (double)each);
+        else allowed = std::fmin(((double)max_bits - bits) / std::ceil(remaining / (double)each), (double)each);
+        ub = std::min(ub, (int64_t)1 << (size_t)std::floor(allowed));
+        int64_t p = prime_below(ub, m);
+        ub = p - 1;
+        while (std::find(start.begin(), start.end(), p) != start.end()) {
+            p = prime_below(ub, m);
+            ub = p - 1;
+        }
+        bits += std::log2((double)p);
+        have.push_back(p);
+    }
+    return have;
+}
+
+// ------------------------------------------------------------------------- device buffers
+struct DBuf {
+    hc_context ctx = nullptr;
+    void* p = nullptr;
+    DBuf() {}
+    DBuf(hc_context c, size_t bytes) : ctx(c) {
+        CK(cuda_check(cudaMallocAsync(&p, bytes ? bytes : 16, stream_of(c)), "ring buffer allocation"));
+    }
+    DBuf(hc_context c, const void* host, size_t bytes) : DBuf(c, bytes) {
+        CK(cuda_check(cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, stream_of(c)), "ring table upload"));
+        CK(cuda_check(cudaStreamSynchronize(stream_of(c)), "ring table upload"));
+    }
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : ctx(o.ctx), p(o.p) { o.p = nullptr; }
+    DBuf& operator=(DBuf&& o) noexcept {
+        std::swap(ctx, o.ctx);
+        std::swap(p, o.p);
+        return *this;
+    }
+    ~DBuf() {
+        if (p) cudaFreeAsync(p, stream_of(ctx));
+    }
+    template <typename T>
+    T* as() const {
+        return (T*)p;
+    }
+};
+
+/// An owned contiguous device tensor [n0, n1, n2, n3] of i64 or i128 entries.
+struct Tensor {
+    DBuf buf;
+    int64_t shape[4] = {0, 0, 0, 0};
+    bool wide = false;
+    Tensor() {}
+    Tensor(hc_context c, int64_t a, int64_t b, int64_t cc, int64_t d, bool w = false) : wide(w) {
+        shape[0] = a, shape[1] = b, shape[2] = cc, shape[3] = d;
+        CK(w ? hc_allocate_i128(c, shape, &buf.p) : hc_allocate_i64(c, shape, &buf.p));
+        buf.ctx = c;
+    }
+    hc_view view() const {
+        hc_view v;
+        v.ptr = buf.p;
+        for (int d = 0; d < 4; d++) v.shape[d] = shape[d];
+        v.strides[3] = 1, v.strides[2] = shape[3], v.strides[1] = shape[2] * shape[3];
+        v.strides[0] = shape[1] * shape[2] * shape[3];
+        return v;
+    }
+};
+
+size_t esize_of(bool wide) { return wide ? 16 : 8; }
+/// rows [s, e) of dimension 0
+hc_view vrows(hc_view v, int64_t s, int64_t e, bool wide = false) {
+    v.ptr = (char*)v.ptr + s * v.strides[0] * (int64_t)esize_of(wide);
+    v.shape[0] = e - s;
+    return v;
+}
+/// RNS rows [s, e) of dimension 1
+hc_view vbase(hc_view v, int64_t s, int64_t e, bool wide = false) {
+    v.ptr = (char*)v.ptr + s * v.strides[1] * (int64_t)esize_of(wide);
+    v.shape[1] = e - s;
+    return v;
+}
+KView kv(const hc_view& v) {
+    KView k;
+    k.p = (char*)v.ptr;
+    k.n0 = v.shape[0], k.n1 = v.shape[1], k.n2 = v.shape[2], k.n3 = v.shape[3];
+    k.s0 = v.strides[0], k.s1 = v.strides[1], k.s2 = v.strides[2];
+    k.b3 = 0;
+    return k;
+}
+void check_view(const hc_view& v, int64_t n0, int64_t n1, int64_t n2, int64_t n3, const char* what) {
+    REQUIRE(v.shape[0] == n0 && v.shape[1] == n1 && v.shape[2] == n2 && v.shape[3] == n3, HC_ERR_SHAPE,
+            std::string(what) + ": unexpected shape");
+    REQUIRE(n3 <= 1 || v.strides[3] == 1, HC_ERR_SHAPE, std::string(what) + ": dimension 3 must be contiguous");
+    REQUIRE(v.ptr || n0 * n1 * n2 * n3 == 0, HC_ERR_ARG, std::string(what) + ": null data");
+}
+
+typedef std::vector<size_t> Base;
+typedef std::vector<std::pair<size_t, size_t>> Digits;
+
+enum class Basis { PB, CRT };
+
+// ------------------------------------------------------------------------- caches
+struct Factor {
+    int64_t p;
+    hc_modulus mod;
+    bool transform;
+    hc_ntt_plan plan_lp = nullptr, plan_k = nullptr;
+    std::vector<int64_t> kl, kk, ikl, ikk;  // NTT-domain CRT kernels (Montgomery form)
+    bool have_kernels = false;
+};
+
+struct TransformCache {
+    Base base;
+    std::vector<hc_modulus> mods;
+    std::vector<hc_ntt_plan> plp, pk;
+    Tensor kl, kk, ikl, ikk;
+};
+
+struct BconvCache {
+    Base src, dst;
+    int shift;
+    int chunk;
+    DBuf qinv, mat, qmodp, ucol;
+};
+
+struct GadgetCache {
+    Base base;
+    Digits digits;
+    int shift;
+    int chunk;
+    DBuf dinv, mat, dmodp, ucol;
+};
+
+struct PermCache {
+    DBuf p2, p3;
+};
+
+}  // namespace
+
+struct hc_ring_s {
+    hc_context ctx;
+    Field field;
+    std::vector<Factor> factors;
+    size_t initial_len = 0;
+    size_t t_bits = 0;
+    std::vector<std::unique_ptr<TransformCache>> tcache;
+    std::vector<std::unique_ptr<BconvCache>> bcache;
+    std::vector<std::unique_ptr<GadgetCache>> gcache;
+    std::map<std::vector<size_t>, std::unique_ptr<PermCache>> pcache;
+    std::map<Base, std::unique_ptr<DBuf>> one_cache;
+    std::map<std::pair<Base, i128>, std::unique_ptr<Tensor>> scalar_cache;
+
+    ~hc_ring_s() {
+        cudaStreamSynchronize(stream_of(ctx));
+        for (auto& f : factors) {
+            if (f.plan_lp) hc_destroy_ntt_plan(ctx, f.plan_lp);
+            if (f.plan_k) hc_destroy_ntt_plan(ctx, f.plan_k);
+        }
+    }
+
+    size_t n() const { return field.deg_l; }
+    int64_t dl() const { return (int64_t)field.deg_lp; }
+    int64_t dk() const { return (int64_t)field.deg_k; }
+    int64_t prime(size_t i) const { return factors[i].p; }
+    std::vector<hc_modulus> mods(const Base& b) const {
+        std::vector<hc_modulus> m;
+        for (size_t i : b) m.push_back(factors[i].mod);
+        return m;
+    }
+    KMods kmods(const Base& b) const {
+        REQUIRE(b.size() <= HC_MAX_MODS, HC_ERR_UNSUPPORTED, "too many RNS factors in one base");
+        KMods k;
+        for (size_t j = 0; j < b.size(); j++) {
+            const hc_modulus& m = factors[b[j]].mod;
+            k.n[j] = m.n, k.ninv[j] = m.neg_inv_n, k.r2[j] = m.r2_mod_n, k.r3[j] = m.r3_mod_n;
+        }
+        return k;
+    }
+    int64_t max_p(const Base& b) const {
+        int64_t m = 1;
+        for (size_t i : b) m = std::max(m, factors[i].p);
+        return m;
+    }
+    int64_t min_p(const Base& b) const {
+        int64_t m = INT64_MAX;
+        for (size_t i : b) m = std::min(m, factors[i].p);
+        return b.empty() ? 1 : m;
+    }
+    void check_base(const Base& b) const {
+        for (size_t i : b) REQUIRE(i < factors.size(), HC_ERR_ARG, "RNS factor index out of range");
+    }
+    /// Q(base) mod p
+    int64_t q_mod(const Base& b, int64_t p) const {
+        int64_t r = 1 % p;
+        for (size_t i : b) r = mulm(r, factors[i].p % p, p);
+        return emod(r, p);
+    }
+    double log2_q(const Base& b) const {
+        double s = 0;
+        for (size_t i : b) s += std::log2((double)factors[i].p);
+        return s;
+    }
+
+    // ---------------------------------------------------------------- construction
+    void add_factor(int64_t p, bool transform) {
+        REQUIRE(p >= ((int64_t)1 << 40) && p <= ((int64_t)1 << 57) - 1, HC_ERR_ARG, "RNS factor size");
+        Factor f;
+        f.p = p;
+        f.transform = transform;
+        CK(hc_create_modulus(p, &f.mod));
+        if (transform) {
+            REQUIRE((p - 1) % (int64_t)field.rou_order() == 0, HC_ERR_ARG, "RNS factor incompatible with the field");
+            std::vector<size_t> olp = field.orders(0, field.nlp), ok = field.orders(field.nlp, field.cyc.size());
+            CK(hc_create_ntt_plan(ctx, &f.mod, olp.data(), olp.size(), &f.plan_lp));
+            CK(hc_create_ntt_plan(ctx, &f.mod, ok.data(), ok.size(), &f.plan_k));
+        }
+        factors.push_back(std::move(f));
+    }
+
+    /// NTT-domain CRT kernels of one factor: Gaussian periods mod the prime, transformed by the
+    /// group NTT on the GPU, inverted pointwise (src/ring.rs:1338-1415).
+    void ensure_kernels(Factor& f) {
+        if (f.have_kernels) return;
+        const int64_t p = f.p, m = (int64_t)field.m();
+        int64_t zeta = 0;
+        for (int64_t c = 2;; c++) {
+            zeta = powm(c, (uint64_t)((p - 1) / m), p);
+            bool ok = true;
+            for (uint64_t q : field.m_factors) ok = ok && powm(zeta, (uint64_t)(m / (int64_t)q), p) != 1;
+            if (ok) break;
+        }
+        int64_t z_lp = powm(zeta, crt2(1, field.spec.m_prime, 0, field.m_k()), p);
+        int64_t z_k = powm(zeta, crt2(0, field.spec.m_prime, 1, field.m_k()), p);
+        auto periods = [&](int64_t zp, uint64_t order, const std::vector<uint64_t>& sub,
+                           const std::vector<uint64_t>& tr) {
+            std::vector<int64_t> pw(order);
+            int64_t cur = 1;
+            for (uint64_t i = 0; i < order; i++) pw[i] = cur, cur = mulm(cur, zp, p);
+            std::vector<int64_t> out;
+            for (uint64_t g : tr) {
+                uint64_t gi = inv_mod_u(g, field.m());
+                int64_t s = 0;
+                for (uint64_t x : sub) s = (s + pw[umulm(x, gi, field.m()) % order]) % p;
+                out.push_back(s);
+            }
+            return out;
+        };
+        std::vector<int64_t> k_lp =
+            periods(z_lp, field.spec.m_prime, field.gal_lp, field.transversal(0, field.nlp));
+        std::vector<int64_t> k_k = periods(z_k, field.m_k(), field.gal_k, field.transversal(field.nlp, field.cyc.size()));
+        auto to_ntt = [&](const std::vector<int64_t>& ker, hc_ntt_plan plan, bool dim2) {
+            std::vector<int64_t> h;
+            for (int64_t x : ker) h.push_back(mont_repr(x, p));
+            int64_t len = (int64_t)h.size();
+            Tensor t(ctx, 1, 1, dim2 ? len : 1, dim2 ? 1 : len);
+            CK(hc_import(ctx, t.view(), h.data(), h.size()));
+            CK(hc_ntt_mont64_dim(ctx, t.view(), &plan, 1, dim2 ? HC_DIM2 : HC_DIM3));
+            CK(hc_export(ctx, t.view(), h.data(), h.size()));
+            for (auto& x : h) x = emod(x, p);
+            return h;
+        };
+        f.kl = to_ntt(k_lp, f.plan_lp, true);
+        f.kk = to_ntt(k_k, f.plan_k, false);
+        auto invert = [&](const std::vector<int64_t>& v) {
+            std::vector<int64_t> o;
+            for (int64_t x : v) {
+                int64_t plain = from_mont(x, p);
+                REQUIRE(plain != 0, HC_ERR_ARG, "CRT kernel is not invertible");
+                o.push_back(mont_repr(invm(plain, p), p));
+            }
+            return o;
+        };
+        f.ikl = invert(f.kl);
+        f.ikk = invert(f.kk);
+        f.have_kernels = true;
+    }
+
+    TransformCache& transform_cache(const Base& b) {
+        for (auto& c : tcache)
+            if (c->base == b) return *c;
+        check_base(b);
+        auto c = std::make_unique<TransformCache>();
+        c->base = b;
+        c->mods = mods(b);
+        std::vector<int64_t> kl, kk, ikl, ikk;
+        for (size_t i : b) {
+            Factor& f = factors[i];
+            REQUIRE(f.transform, HC_ERR_ARG, "RNS factor doesn't support the basis transforms");
+            ensure_kernels(f);
+            c->plp.push_back(f.plan_lp);
+            c->pk.push_back(f.plan_k);
+            kl.insert(kl.end(), f.kl.begin(), f.kl.end());
+            kk.insert(kk.end(), f.kk.begin(), f.kk.end());
+            ikl.insert(ikl.end(), f.ikl.begin(), f.ikl.end());
+            ikk.insert(ikk.end(), f.ikk.begin(), f.ikk.end());
+        }
+        int64_t r = (int64_t)b.size();
+        auto up = [&](Tensor& t, const std::vector<int64_t>& v, bool lp) {
+            t = Tensor(ctx, 1, r, lp ? dl() : 1, lp ? 1 : dk());
+            CK(hc_import(ctx, t.view(), v.data(), v.size()));
+        };
+        up(c->kl, kl, true);
+        up(c->kk, kk, false);
+        up(c->ikl, ikl, true);
+        up(c->ikk, ikk, false);
+        tcache.push_back(std::move(c));
+        return *tcache.back();
+    }
+
+    // ---------------------------------------------------------------- transforms
+    void transform(const hc_view& v, const Base& b, bool inverse) {
+        REQUIRE(v.shape[1] == (int64_t)b.size() && v.shape[2] == dl() && v.shape[3] == dk(), HC_ERR_SHAPE,
+                "transform: tensor shape does not match the ring and base");
+        TransformCache& c = transform_cache(b);
+        const size_t r = b.size();
+        CK(hc_ntt_mul_mont64_dim(ctx, v, c.plp.data(), r, HC_DIM2, inverse ? c.ikl.view() : c.kl.view(),
+                                 c.mods.data(), r));
+        CK(hc_ntt_mul_mont64_dim(ctx, v, c.pk.data(), r, HC_DIM3, inverse ? c.ikk.view() : c.kk.view(),
+                                 c.mods.data(), r));
+        CK(hc_intt_mont64_dim(ctx, v, c.plp.data(), r, HC_DIM2));
+        CK(hc_intt_mont64_dim(ctx, v, c.pk.data(), r, HC_DIM3));
+    }
+
+    // ---------------------------------------------------------------- base conversion
+    BconvCache& bconv_cache(const Base& src, const Base& dst) {
+        for (auto& c : bcache)
+            if (c->src == src && c->dst == dst) return *c;
+        check_base(src);
+        check_base(dst);
+        REQUIRE(!src.empty(), HC_ERR_ARG, "empty source base");
+        auto c = std::make_unique<BconvCache>();
+        c->src = src, c->dst = dst;
+        const size_t r = src.size(), rd = dst.size();
+        int64_t mx = std::max(max_p(src), max_p(dst)), mn = min_p(src);
+        c->shift = (int)std::max<size_t>(64, bitlen_u128((u128)(4 * (i128)r * mx + 1)));
+        REQUIRE(c->shift <= 126, HC_ERR_UNSUPPORTED, "base conversion precision");
+        const i128 qt = (i128)1 << c->shift;
+        REQUIRE((qt - 1) / mn + 1 <= INT64_MAX, HC_ERR_ARG, "correction vector coefficients don't fit into an i64");
+        c->chunk = (int)std::min<i128>(I128MAX / ((i128)mx * mx), 1 << 30);
+        std::vector<int64_t> qinv(r), mat((rd + 1) * r), qm(rd);
+        for (size_t u = 0; u < r; u++) {
+            int64_t pu = prime(src[u]), qo = 1;
+            for (size_t l = 0; l < r; l++)
+                if (l != u) qo = mulm(qo, prime(src[l]) % pu, pu);
+            qinv[u] = centred(invm(qo, pu), pu);
+        }
+        for (size_t j = 0; j < rd; j++) {
+            int64_t pj = prime(dst[j]);
+            int64_t r1 = mont_repr(1, pj), r2 = mulm(r1, r1, pj);
+            for (size_t u = 0; u < r; u++) {
+                int64_t v = 1;
+                for (size_t l = 0; l < r; l++)
+                    if (l != u) v = mulm(v, prime(src[l]) % pj, pj);
+                mat[j * r + u] = centred(mulm(emod(v, pj), emod(r2, pj), pj), pj);
+            }
+            qm[j] = centred(mulm(q_mod(src, pj), emod(-r1, pj), pj), pj);
+        }
+        for (size_t u = 0; u < r; u++) {
+            i128 a = qt, bp = prime(src[u]);
+            mat[rd * r + u] = (int64_t)((a + bp / 2) / bp);
+        }
+        int32_t uc[2] = {0, (int32_t)r};
+        c->qinv = DBuf(ctx, qinv.data(), qinv.size() * 8);
+        c->mat = DBuf(ctx, mat.data(), mat.size() * 8);
+        c->qmodp = DBuf(ctx, qm.data(), qm.size() * 8);
+        c->ucol = DBuf(ctx, uc, sizeof(uc));
+        bcache.push_back(std::move(c));
+        return *bcache.back();
+    }
+
+    void bconv(const hc_view& dst, const Base& db, const hc_view& src, const Base& sb) {
+        check_view(src, src.shape[0], (int64_t)sb.size(), src.shape[2], src.shape[3], "bconv src");
+        check_view(dst, src.shape[0], (int64_t)db.size(), src.shape[2], src.shape[3], "bconv dst");
+        BconvCache& c = bconv_cache(sb, db);
+        CK(launch_bconv_fused(ctx, kv(src), kv(dst), c.qinv.as<int64_t>(), c.mat.as<int64_t>(),
+                              c.qmodp.as<int64_t>(), c.ucol.as<int32_t>(), (int)sb.size(), (int)db.size(), 1,
+                              c.shift, c.chunk, kmods(sb), kmods(db), src.shape[0]));
+    }
+
+    GadgetCache& gadget_cache(const Base& b, const Digits& digits) {
+        for (auto& c : gcache)
+            if (c->base == b && c->digits == digits) return *c;
+        check_base(b);
+        const size_t r = b.size(), d = digits.size();
+        REQUIRE(d > 0, HC_ERR_ARG, "at least one gadget digit required");
+        for (size_t i = 0; i < d; i++) {
+            REQUIRE(digits[i].first < digits[i].second && digits[i].second <= r, HC_ERR_ARG, "gadget digit range");
+            REQUIRE(i == 0 || digits[i - 1].second <= digits[i].first, HC_ERR_ARG,
+                    "digits must be sorted and disjoint");
+        }
+        auto c = std::make_unique<GadgetCache>();
+        c->base = b, c->digits = digits;
+        int64_t mx = max_p(b), mn = min_p(b);
+        size_t maxlen = 0;
+        for (auto& dg : digits) maxlen = std::max(maxlen, dg.second - dg.first);
+        c->shift = (int)std::max<size_t>(64, bitlen_u128((u128)(4 * (i128)maxlen * mx + 1)));
+        const i128 qt = (i128)1 << c->shift;
+        REQUIRE((qt - 1) / mn + 1 <= INT64_MAX, HC_ERR_ARG, "correction vector coefficients don't fit into an i64");
+        c->chunk = (int)std::min<i128>(I128MAX / ((i128)mx * mx), 1 << 30);
+        auto dover = [&](size_t di, size_t u, int64_t q) {
+            int64_t v = 1;
+            for (size_t l = digits[di].first; l < digits[di].second; l++)
+                if (l != u) v = mulm(v, prime(b[l]) % q, q);
+            return emod(v, q);
+        };
+        std::vector<int64_t> dinv(r, 0), mat(d * (r + 1) * r, 0), dm;
+        std::vector<int32_t> uc;
+        for (size_t di = 0; di < d; di++) {
+            uc.push_back((int32_t)digits[di].first);
+            uc.push_back((int32_t)digits[di].second);
+            for (size_t u = digits[di].first; u < digits[di].second; u++) {
+                int64_t pu = prime(b[u]);
+                dinv[u] = centred(invm(dover(di, u, pu), pu), pu);
+            }
+            for (size_t j = 0; j < r; j++) {
+                int64_t pj = prime(b[j]);
+                int64_t r1 = mont_repr(1, pj), r2 = emod(mulm(r1, r1, pj), pj);
+                for (size_t u = digits[di].first; u < digits[di].second; u++)
+                    mat[(di * (r + 1) + j) * r + u] = centred(mulm(dover(di, u, pj), r2, pj), pj);
+                int64_t dmod = 1;
+                for (size_t l = digits[di].first; l < digits[di].second; l++) dmod = mulm(dmod, prime(b[l]) % pj, pj);
+                dm.push_back(centred(mulm(emod(dmod, pj), emod(-r1, pj), pj), pj));
+            }
+            for (size_t u = digits[di].first; u < digits[di].second; u++) {
+                i128 bp = prime(b[u]);
+                mat[(di * (r + 1) + r) * r + u] = (int64_t)((qt + bp / 2) / bp);
+            }
+        }
+        c->dinv = DBuf(ctx, dinv.data(), dinv.size() * 8);
+        c->mat = DBuf(ctx, mat.data(), mat.size() * 8);
+        c->dmodp = DBuf(ctx, dm.data(), dm.size() * 8);
+        c->ucol = DBuf(ctx, uc.data(), uc.size() * 4);
+        gcache.push_back(std::move(c));
+        return *gcache.back();
+    }
+
+    void bconv_gadget(const hc_view& dst, const hc_view& src, const Base& b, const Digits& digits) {
+        check_view(src, 1, (int64_t)b.size(), src.shape[2], src.shape[3], "gadget src");
+        check_view(dst, (int64_t)digits.size(), (int64_t)b.size(), src.shape[2], src.shape[3], "gadget dst");
+        GadgetCache& c = gadget_cache(b, digits);
+        KMods km = kmods(b);
+        CK(launch_bconv_fused(ctx, kv(src), kv(dst), c.dinv.as<int64_t>(), c.mat.as<int64_t>(), c.dmodp.as<int64_t>(),
+                              c.ucol.as<int32_t>(), (int)b.size(), (int)b.size(), (int)digits.size(), c.shift, c.chunk,
+                              km, km, 1));
+    }
+
+    // ---------------------------------------------------------------- Galois
+    PermCache& perms(uint64_t g) {
+        std::vector<size_t> s = field.gal_to_shift(g);
+        auto it = pcache.find(s);
+        if (it != pcache.end()) return *it->second;
+        auto make = [&](size_t from, size_t to) {
+            std::vector<size_t> sh(s.begin() + from, s.begin() + to), ord = field.orders(from, to);
+            size_t n = 1;
+            for (size_t o : ord) n *= o;
+            std::vector<uint32_t> perm(n);
+            std::vector<size_t> idx(ord.size(), 0);
+            for (size_t e = 0; e < n; e++) {
+                size_t src = 0;
+                for (size_t t = 0; t < ord.size(); t++) src = src * ord[t] + (idx[t] + ord[t] - sh[t] % ord[t]) % ord[t];
+                perm[e] = (uint32_t)src;
+                for (size_t t = ord.size(); t-- > 0;) {
+                    if (++idx[t] < ord[t]) break;
+                    idx[t] = 0;
+                }
+            }
+            return perm;
+        };
+        auto c = std::make_unique<PermCache>();
+        std::vector<uint32_t> a = make(0, field.nlp), bb = make(field.nlp, field.cyc.size());
+        c->p2 = DBuf(ctx, a.data(), a.size() * 4);
+        c->p3 = DBuf(ctx, bb.data(), bb.size() * 4);
+        auto& ref = *c;
+        pcache[s] = std::move(c);
+        return ref;
+    }
+    void apply_galois(const hc_view& dst, const hc_view& src, uint64_t g) {
+        check_view(dst, src.shape[0], src.shape[1], dl(), dk(), "galois dst");
+        check_view(src, dst.shape[0], dst.shape[1], dl(), dk(), "galois src");
+        PermCache& pc = perms(g);
+        CK(launch_galois(ctx, kv(dst), kv(src), pc.p2.as<uint32_t>(), pc.p3.as<uint32_t>()));
+    }
+
+    // ---------------------------------------------------------------- scalars
+    const int64_t* one_dev(const Base& b) {
+        auto it = one_cache.find(b);
+        if (it != one_cache.end()) return it->second->as<int64_t>();
+        std::vector<int64_t> v;
+        for (size_t i : b) v.push_back(mont_repr(1, prime(i)));
+        auto buf = std::make_unique<DBuf>(ctx, v.data(), v.size() * 8);
+        const int64_t* p = buf->as<int64_t>();
+        one_cache[b] = std::move(buf);
+        return p;
+    }
+    /// [1, r, 1, 1] tensor of mont(scalar mod p) (src/ring.rs:876-887)
+    const Tensor& scalar_tensor(const Base& b, i128 s) {
+        auto key = std::make_pair(b, s);
+        auto it = scalar_cache.find(key);
+        if (it != scalar_cache.end()) return *it->second;
+        std::vector<int64_t> v;
+        for (size_t i : b) v.push_back(mont_repr((int64_t)(s % (i128)prime(i)), prime(i)));
+        auto t = std::make_unique<Tensor>(ctx, 1, (int64_t)b.size(), 1, 1);
+        CK(hc_import(ctx, t->view(), v.data(), v.size()));
+        auto& ref = *t;
+        scalar_cache[key] = std::move(t);
+        return ref;
+    }
+    /// [1, r, 1, 1] tensor holding mont(smallest_lift(residue(p))) (src/ring.rs:890-902)
+    Tensor scalar_tensor_big(const Base& b, const std::function<int64_t(int64_t)>& residue) {
+        std::vector<int64_t> v;
+        for (size_t i : b) v.push_back(mont_repr(centred(residue(prime(i)), prime(i)), prime(i)));
+        Tensor t(ctx, 1, (int64_t)b.size(), 1, 1);
+        CK(hc_import(ctx, t.view(), v.data(), v.size()));
+        return t;
+    }
+};
+
+namespace {
+
+// ------------------------------------------------------------------------- wide accumulation
+/// Delayed-reduction i128 accumulator (WideRingEls, src/ring.rs:330-532): the per-row
+/// worst-case bound decides between single and double reduction when finishing, and a row's
+/// first accumulation overwrites it. Used for key generation and encryption (set-up work).
+struct Wide {
+    hc_ring R;
+    Base base;
+    Tensor data;
+    std::vector<u128> bound;
+    int64_t maxp, minp;
+    Wide(hc_ring r, int64_t count, const Base& b) : R(r), base(b), bound((size_t)count, 0) {
+        data = Tensor(R->ctx, count, (int64_t)b.size(), R->dl(), R->dk(), true);
+        maxp = R->max_p(b), minp = R->min_p(b);
+    }
+    void step(size_t rs, size_t re, u128 s) {
+        for (size_t i = rs; i < re; i++) {
+            u128 nb = bound[i] + s;
+            REQUIRE(nb >= bound[i] && nb <= (u128)I128MAX, HC_ERR_ARG, "wide ring element overflow");
+            bound[i] = nb;
+        }
+    }
+    void accumulate(size_t rs, size_t re, const hc_view& lhs, const hc_view& rhs) {
+        auto op = [&](const hc_view& t, size_t s, size_t e) { return t.shape[0] == 1 ? t : vrows(t, s - rs, e - rs); };
+        size_t s = rs;
+        while (s < re) {
+            bool fresh = bound[s] == 0;
+            size_t e = s + 1;
+            while (e < re && (bound[e] == 0) == fresh) e++;
+            hc_view d = vrows(data.view(), (int64_t)s, (int64_t)e, true);
+            if (fresh) CK(hc_mul_i64(R->ctx, d, op(lhs, s, e), op(rhs, s, e)));
+            else CK(hc_fma_i64(R->ctx, d, op(lhs, s, e), op(rhs, s, e)));
+            s = e;
+        }
+    }
+    u128 mp2() const { return (u128)maxp * (u128)maxp; }
+    void fma(size_t rs, size_t re, const hc_view& l, u128 lb, const hc_view& r, u128 rb) {
+        accumulate(rs, re, l, r);
+        step(rs, re, lb * rb * mp2());
+    }
+    void add(size_t rs, size_t re, const hc_view& src, u128 sb) {
+        accumulate(rs, re, src, R->scalar_tensor(base, 1).view());
+        step(rs, re, sb * mp2());
+    }
+    bool full(size_t row) const { return bound[row] > ((u128)minp << 63); }
+    void reduce_into(const hc_view& dst) {
+        std::vector<hc_modulus> m = R->mods(base);
+        size_t s = 0;
+        while (s < bound.size()) {
+            bool f = full(s);
+            size_t e = s + 1;
+            while (e < bound.size() && full(e) == f) e++;
+            hc_view d = vrows(dst, (int64_t)s, (int64_t)e);
+            hc_view w = vrows(data.view(), (int64_t)s, (int64_t)e, true);
+            if (f) {
+                CK(hc_red_mont64_double(R->ctx, d, w, m.data(), m.size()));
+                CK(hc_i64_to_mont64(R->ctx, d, m.data(), m.size()));
+            } else {
+                CK(hc_red_mont64(R->ctx, d, w, m.data(), m.size()));
+            }
+            s = e;
+        }
+    }
+};
+
+uint64_t splitmix(uint64_t* s) {
+    *s += 0x9E3779B97F4A7C15ull;
+    uint64_t z = *s;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+Base base_of(const size_t* b, size_t r) {
+    REQUIRE(r == 0 || b, HC_ERR_ARG, "null base");
+    return Base(b, b + r);
+}
+Base prefix(size_t r) {
+    Base b;
+    for (size_t i = 0; i < r; i++) b.push_back(i);
+    return b;
+}
+Digits digits_of(const size_t* d, size_t n) {
+    REQUIRE(n == 0 || d, HC_ERR_ARG, "null digits");
+    Digits r;
+    for (size_t i = 0; i < n; i++) r.push_back({d[2 * i], d[2 * i + 1]});
+    return r;
+}
+Digits clip(const Digits& d, size_t len) {
+    Digits r;
+    for (auto& x : d)
+        if (x.first < len) r.push_back({x.first, std::min(x.second, len)});
+    return r;
+}
+i128 words(const int64_t t[2]) { return (i128)(((u128)(uint64_t)t[1] << 64) | (uint64_t)t[0]); }
+
+/// Tensor of element rows built on the host: mont(c mod p) for i128 coefficients c (src/ring.rs:1449-1461)
+Tensor element_from_coeffs(hc_ring R, const Base& b, const std::vector<i128>& coeffs) {
+    std::vector<int64_t> v;
+    v.reserve(b.size() * coeffs.size());
+    for (size_t i : b) {
+        int64_t p = R->prime(i);
+        for (i128 c : coeffs) v.push_back(mont_repr((int64_t)(c % (i128)p), p));
+    }
+    Tensor t(R->ctx, 1, (int64_t)b.size(), R->dl(), R->dk());
+    CK(hc_import(R->ctx, t.view(), v.data(), v.size()));
+    return t;
+}
+
+// ------------------------------------------------------------------------- BFV
+const double MIN_SIGMA = 3.2;
+
+double sigma_for(hc_ring R, const Base& b, double log2_alpha) {
+    return std::fmax(MIN_SIGMA, std::exp2(R->log2_q(b) - log2_alpha));
+}
+
+i128 gaussian(uint64_t* st, double sigma) {
+    double u1 = ((double)(splitmix(st) >> 11) + 0.5) / (double)(1ull << 53);
+    double u2 = (double)(splitmix(st) >> 11) / (double)(1ull << 53);
+    double g = std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * M_PI * u2);
+    return (i128)std::round(g * sigma);
+}
+
+/// b <- b + e for a fresh Gaussian e (src/bfv.rs:195-204), b in period basis
+void add_error(hc_ring R, const hc_view& b, const Base& base, uint64_t* st, double sigma) {
+    std::vector<i128> e(R->n());
+    for (auto& x : e) x = gaussian(st, sigma);
+    Tensor err = element_from_coeffs(R, base, e);
+    Wide acc(R, 1, base);
+    acc.add(0, 1, b, 1);
+    acc.add(0, 1, err.view(), 1);
+    acc.reduce_into(b);
+}
+
+/// (b + a s, -a) for uniform a (src/bfv.rs:310-326)
+void finish_enc(hc_ring R, const Base& base, const hc_view& sk, const hc_view& b, uint64_t* st, const hc_view& ct) {
+    std::vector<int64_t> vals;
+    for (size_t i : base) {
+        int64_t p = R->prime(i);
+        for (size_t c = 0; c < R->n(); c++) vals.push_back((int64_t)(splitmix(st) % (uint64_t)p));
+    }
+    Tensor a(R->ctx, 1, (int64_t)base.size(), R->dl(), R->dk());
+    CK(hc_import(R->ctx, a.view(), vals.data(), vals.size()));
+    Wide acc(R, 1, base);
+    acc.fma(0, 1, a.view(), 1, vbase(sk, 0, (int64_t)base.size()), 1);
+    acc.add(0, 1, b, 1);
+    acc.reduce_into(vrows(ct, 0, 1));
+    std::vector<hc_modulus> m = R->mods(base);
+    CK(hc_mul_mont64(R->ctx, a.view(), R->scalar_tensor(base, -1).view(), m.data(), m.size()));
+    CK(hc_assign(R->ctx, vrows(ct, 1, 2), a.view()));
+}
+
+void enc_zero(hc_ring R, const Base& base, const hc_view& sk, uint64_t* st, double log2_alpha, const hc_view& ct) {
+    Tensor b(R->ctx, 1, (int64_t)base.size(), R->dl(), R->dk());
+    add_error(R, b.view(), base, st, sigma_for(R, base, log2_alpha));
+    R->transform(b.view(), base, false);
+    finish_enc(R, base, sk, b.view(), st, ct);
+}
+
+/// Delta = round(Q/t) modulo p (src/bfv.rs:237-247), Q = 0 mod p; ties round away from zero
+std::function<int64_t(int64_t)> delta_residue(hc_ring R, const Base& base, u128 t) {
+    u128 qt = 1 % t;
+    for (size_t i : base) qt = (qt % t) * ((u128)R->prime(i) % t) % t;
+    u128 extra = (qt + t / 2) / t;
+    return [qt, t, extra](int64_t p) {
+        int64_t c = (int64_t)(qt % (u128)p);
+        return emod(mulm(emod(-c, p), invm((int64_t)(t % (u128)p), p), p) + (int64_t)extra, p);
+    };
+}
+
+i128 cmod_t(i128 a, i128 t) {
+    i128 h = t / 2, r = a % t;
+    i128 ar = r < 0 ? -r : r;
+    if (ar >= h) {
+        if (r < 0) r += t;
+        else if (r > h) r -= t;
+    }
+    return r;
+}
+
+void gen_ksk(hc_ring R, const Base& base, const hc_view& old_sk, const hc_view& new_sk, const Digits& digits,
+             uint64_t* st, double log2_alpha, const hc_view& keys) {
+    const int64_t r = (int64_t)base.size();
+    check_view(keys, 2 * (int64_t)digits.size(), r, R->dl(), R->dk(), "key tensor");
+    for (size_t di = 0; di < digits.size(); di++) {
+        hc_view ct = vrows(keys, 2 * (int64_t)di, 2 * (int64_t)di + 2);
+        enc_zero(R, base, new_sk, st, log2_alpha, ct);
+        std::map<int64_t, int64_t> res;
+        for (size_t j = 0; j < base.size(); j++)
+            res[R->prime(base[j])] = (j >= digits[di].first && j < digits[di].second) ? 1 : 0;
+        Tensor factor = R->scalar_tensor_big(base, [&res](int64_t p) { return res.at(p); });
+        Wide acc(R, 1, base);
+        acc.fma(0, 1, vbase(old_sk, 0, r), 1, factor.view(), 1);
+        acc.add(0, 1, vrows(ct, 0, 1), 1);
+        acc.reduce_into(vrows(ct, 0, 1));
+    }
+}
+
+/// rows needing the full double reduction after accumulating `step_bound` (src/ring.rs:365)
+bool needs_full(u128 bound, int64_t minp) { return bound > ((u128)minp << 63); }
+
+/// gadget_decompose (src/bfv.rs:408-426): digits of a period-basis element, in CRT basis
+Tensor gadget_decompose(hc_ring R, const hc_view& c_pb, const Base& base, const Digits& digits) {
+    Tensor parts(R->ctx, (int64_t)digits.size(), (int64_t)base.size(), R->dl(), R->dk());
+    R->bconv_gadget(parts.view(), c_pb, base, digits);
+    R->transform(parts.view(), base, false);
+    return parts;
+}
+
+/// acc[0..2] = sum_t parts[t] * key_t (+ summands through mont(1)), reduced (fused)
+void keyswitch(hc_ring R, const hc_view& parts, const hc_view& keys, const Base& base, size_t nd,
+               const hc_view* add0, const hc_view* add1, const hc_view& out, const uint32_t* p2 = nullptr,
+               const uint32_t* p3 = nullptr) {
+    const int64_t r = (int64_t)base.size();
+    REQUIRE(keys.shape[1] >= r && keys.shape[0] >= 2 * (int64_t)nd, HC_ERR_SHAPE, "key tensor too small");
+    std::vector<KView> pv, kvv;
+    u128 mp = (u128)R->max_p(base), step = 0;
+    for (size_t t = 0; t < nd; t++) {
+        pv.push_back(kv(vrows(parts, (int64_t)t, (int64_t)t + 1)));
+        kvv.push_back(kv(vbase(vrows(keys, 2 * (int64_t)t, 2 * (int64_t)t + 2), 0, r)));
+        step += mp * mp;
+    }
+    u128 b0 = step + (add0 ? mp * mp : 0), b1 = step + (add1 ? mp * mp : 0);
+    KView a0 = add0 ? kv(*add0) : KView(), a1 = add1 ? kv(*add1) : KView();
+    int64_t minp = R->min_p(base);
+    CK(launch_keyswitch(R->ctx, pv.data(), kvv.data(), (int)nd, add0 ? &a0 : nullptr, add1 ? &a1 : nullptr,
+                        needs_full(b0, minp), needs_full(b1, minp), kv(out), R->kmods(base), R->one_dev(base), p2, p3));
+}
+
+Tensor lift_to_extended(hc_ring R, const hc_view& pb, const hc_view* crt, const Base& base) {
+    const int64_t count = pb.shape[0], r = (int64_t)base.size();
+    Base ext;
+    {
+        double need = (double)(product_bits([&] {
+                                   std::vector<int64_t> ps;
+                                   for (size_t i : base) ps.push_back(R->prime(i));
+                                   return ps;
+                               }()) +
+                               R->t_bits + 60);
+        double bits = 0;
+        for (size_t i = R->initial_len; i < R->factors.size() && bits < need; i++) {
+            ext.push_back(i);
+            bits += std::log2((double)R->prime(i));
+        }
+        REQUIRE(bits >= need, HC_ERR_ARG, "extension pool too small for lifted multiplication over this base");
+    }
+    Base lifted = base;
+    lifted.insert(lifted.end(), ext.begin(), ext.end());
+    Tensor res(R->ctx, count, (int64_t)lifted.size(), R->dl(), R->dk());
+    hc_view hi = vbase(res.view(), r, (int64_t)lifted.size());
+    R->bconv(hi, ext, pb, base);
+    if (crt) {
+        R->transform(hi, ext, false);
+        CK(hc_assign(R->ctx, vbase(res.view(), 0, r), *crt));
+    } else {
+        CK(hc_assign(R->ctx, vbase(res.view(), 0, r), pb));
+        R->transform(res.view(), lifted, false);
+    }
+    return res;
+}
+
+Tensor rescale_to_base(hc_ring R, const hc_view& x, const Base& lifted, size_t base_len, i128 t) {
+    const int64_t count = x.shape[0];
+    Base base(lifted.begin(), lifted.begin() + base_len), ext(lifted.begin() + base_len, lifted.end());
+    std::vector<hc_modulus> ml = R->mods(lifted), me = R->mods(ext);
+    CK(hc_mul_mont64(R->ctx, x, R->scalar_tensor(lifted, t).view(), ml.data(), ml.size()));
+    Tensor tmp(R->ctx, count, (int64_t)ext.size(), R->dl(), R->dk());
+    hc_view xlo = vbase(x, 0, (int64_t)base_len), xhi = vbase(x, (int64_t)base_len, (int64_t)lifted.size());
+    R->bconv(tmp.view(), ext, xlo, base);
+    CK(hc_sub_i64(R->ctx, xhi, tmp.view()));
+    Tensor qinv = R->scalar_tensor_big(ext, [&](int64_t p) { return invm(R->q_mod(base, p), p); });
+    CK(hc_mul_mont64(R->ctx, xhi, qinv.view(), me.data(), me.size()));
+    Tensor out(R->ctx, count, (int64_t)base_len, R->dl(), R->dk());
+    R->bconv(out.view(), base, xhi, ext);
+    return out;
+}
+
+}  // namespace
+
+extern "C" {
+
+hc_status hc_ring_create(hc_context ctx, const char* field, size_t lo, size_t hi, size_t t_bits, hc_ring* out) {
+    return guard([&] {
+        REQUIRE(ctx && field && out, HC_ERR_ARG, "null argument");
+        REQUIRE(hi > lo, HC_ERR_ARG, "log2 q range");
+        auto R = std::make_unique<hc_ring_s>();
+        R->ctx = ctx;
+        R->field = Field::make(field);
+        int64_t rou = (int64_t)R->field.rou_order();
+        std::vector<int64_t> base = sample_primes({}, lo, hi, 57, rou);
+        std::vector<int64_t> all = sample_primes(base, 2 * hi + 60 + t_bits, 2 * hi + 60 + t_bits + 30, 57, rou);
+        R->initial_len = base.size();
+        R->t_bits = t_bits;
+        for (int64_t p : all) R->add_factor(p, true);
+        *out = R.release();
+    });
+}
+
+hc_status hc_ring_create_raw(hc_context ctx, const char* field, const int64_t* primes, size_t n, hc_ring* out) {
+    return guard([&] {
+        REQUIRE(ctx && field && out && (n == 0 || primes), HC_ERR_ARG, "null argument");
+        auto R = std::make_unique<hc_ring_s>();
+        R->ctx = ctx;
+        R->field = Field::make(field);
+        R->initial_len = n;
+        for (size_t i = 0; i < n; i++) {
+            for (auto& f : R->factors) REQUIRE(f.p != primes[i], HC_ERR_ARG, "duplicate RNS factor");
+            R->add_factor(primes[i], false);
+        }
+        *out = R.release();
+    });
+}
+
+hc_status hc_ring_destroy(hc_ring ring) {
+    delete ring;
+    return HC_OK;
+}
+size_t hc_ring_num_factors(hc_ring ring) { return ring ? ring->factors.size() : 0; }
+int64_t hc_ring_prime(hc_ring ring, size_t idx) { return ring && idx < ring->factors.size() ? ring->factors[idx].p : 0; }
+size_t hc_ring_initial_len(hc_ring ring) { return ring ? ring->initial_len : 0; }
+hc_status hc_ring_dims(hc_ring ring, size_t out[3]) {
+    if (!ring || !out) return fail(HC_ERR_ARG, "null argument");
+    out[0] = ring->field.deg_l, out[1] = ring->field.deg_lp, out[2] = ring->field.deg_k;
+    return HC_OK;
+}
+hc_status hc_ring_modulus(hc_ring ring, size_t idx, hc_modulus* out) {
+    if (!ring || !out || idx >= ring->factors.size()) return fail(HC_ERR_ARG, "bad argument");
+    *out = ring->factors[idx].mod;
+    return HC_OK;
+}
+hc_status hc_ring_extension_base(hc_ring ring, const size_t* base, size_t r, size_t* out, size_t* out_len) {
+    return guard([&] {
+        REQUIRE(ring && out && out_len, HC_ERR_ARG, "null argument");
+        Base b = base_of(base, r);
+        for (size_t i : b) REQUIRE(i < ring->initial_len, HC_ERR_ARG, "extension of a non-initial base");
+        std::vector<int64_t> ps;
+        for (size_t i : b) ps.push_back(ring->prime(i));
+        double need = (double)(product_bits(ps) + ring->t_bits + 60), bits = 0;
+        size_t n = 0;
+        for (size_t i = ring->initial_len; i < ring->factors.size() && bits < need; i++) {
+            out[n++] = i;
+            bits += std::log2((double)ring->prime(i));
+        }
+        REQUIRE(bits >= need, HC_ERR_ARG, "extension pool too small for lifted multiplication over this base");
+        *out_len = n;
+    });
+}
+hc_status hc_ring_crt_kernels(hc_ring ring, size_t idx, int64_t* out) {
+    return guard([&] {
+        REQUIRE(ring && out && idx < ring->factors.size(), HC_ERR_ARG, "bad argument");
+        Factor& f = ring->factors[idx];
+        REQUIRE(f.transform, HC_ERR_ARG, "RNS factor doesn't support the basis transforms");
+        ring->ensure_kernels(f);
+        size_t dl = f.kl.size(), dk = f.kk.size();
+        std::memcpy(out, f.kl.data(), dl * 8);
+        std::memcpy(out + dl, f.kk.data(), dk * 8);
+        std::memcpy(out + dl + dk, f.ikl.data(), dl * 8);
+        std::memcpy(out + 2 * dl + dk, f.ikk.data(), dk * 8);
+    });
+}
+
+hc_status hc_ring_pb_to_crt(hc_ring ring, hc_view data, const size_t* base, size_t r) {
+    return guard([&] {
+        REQUIRE(ring, HC_ERR_ARG, "null ring");
+        ring->transform(data, base_of(base, r), false);
+    });
+}
+hc_status hc_ring_crt_to_pb(hc_ring ring, hc_view data, const size_t* base, size_t r) {
+    return guard([&] {
+        REQUIRE(ring, HC_ERR_ARG, "null ring");
+        ring->transform(data, base_of(base, r), true);
+    });
+}
+hc_status hc_ring_bconv(hc_ring ring, hc_view dst, const size_t* db, size_t rd, hc_view src, const size_t* sb,
+                        size_t rs) {
+    return guard([&] {
+        REQUIRE(ring, HC_ERR_ARG, "null ring");
+        ring->bconv(dst, base_of(db, rd), src, base_of(sb, rs));
+    });
+}
+hc_status hc_ring_bconv_gadget(hc_ring ring, hc_view dst, hc_view src, const size_t* base, size_t r,
+                               const size_t* digits, size_t d) {
+    return guard([&] {
+        REQUIRE(ring, HC_ERR_ARG, "null ring");
+        ring->bconv_gadget(dst, src, base_of(base, r), digits_of(digits, d));
+    });
+}
+hc_status hc_ring_apply_galois(hc_ring ring, hc_view dst, hc_view src, const size_t* base, size_t r, uint64_t g) {
+    return guard([&] {
+        REQUIRE(ring, HC_ERR_ARG, "null ring");
+        REQUIRE((int64_t)r == src.shape[1], HC_ERR_SHAPE, "base length does not match the tensor");
+        ring->apply_galois(dst, src, g);
+    });
+}
+
+hc_status hc_bfv_gen_sk(hc_ring R, uint64_t* st, hc_view sk) {
+    return guard([&] {
+        REQUIRE(R && st, HC_ERR_ARG, "null argument");
+        Base b = prefix(R->initial_len);
+        check_view(sk, 1, (int64_t)b.size(), R->dl(), R->dk(), "sk");
+        std::vector<i128> c(R->n(), 0);
+        for (int i = 0; i < 128; i++) {  // SK_HWT (src/bfv.rs:41)
+            size_t j = (size_t)(splitmix(st) % (uint64_t)R->n());
+            c[j] = (i128)(splitmix(st) % 2) * 2 - 1;
+        }
+        Tensor t = element_from_coeffs(R, b, c);
+        R->transform(t.view(), b, false);
+        CK(hc_assign(R->ctx, sk, t.view()));
+        CK(hc_synchronize(R->ctx));
+    });
+}
+
+double hc_bfv_log2_alpha_for_sigma(hc_ring R, const size_t* base, size_t r, double sigma) {
+    return R->log2_q(Base(base, base + r)) - std::log2(sigma);
+}
+
+hc_status hc_bfv_enc(hc_ring R, uint64_t* st, const size_t* base, size_t r, const int64_t t[2], const int64_t* ptxt,
+                     hc_view sk, double log2_alpha, hc_view ct) {
+    return guard([&] {
+        REQUIRE(R && st && t && ptxt, HC_ERR_ARG, "null argument");
+        Base b = base_of(base, r);
+        R->check_base(b);
+        check_view(ct, 2, (int64_t)r, R->dl(), R->dk(), "ciphertext");
+        const i128 tt = words(t);
+        REQUIRE(tt >= 2, HC_ERR_ARG, "plaintext modulus");
+        std::vector<i128> c(R->n());
+        for (size_t i = 0; i < R->n(); i++)
+            c[i] = cmod_t((i128)(((u128)(uint64_t)ptxt[2 * i + 1] << 64) | (uint64_t)ptxt[2 * i]), tt);
+        Tensor bt = element_from_coeffs(R, b, c);
+        std::vector<hc_modulus> m = R->mods(b);
+        Tensor delta = R->scalar_tensor_big(b, delta_residue(R, b, (u128)tt));
+        CK(hc_mul_mont64(R->ctx, bt.view(), delta.view(), m.data(), m.size()));
+        add_error(R, bt.view(), b, st, sigma_for(R, b, log2_alpha));
+        R->transform(bt.view(), b, false);
+        finish_enc(R, b, sk, bt.view(), st, ct);
+        CK(hc_synchronize(R->ctx));
+    });
+}
+
+hc_status hc_bfv_gen_ksk(hc_ring R, uint64_t* st, const size_t* base, size_t r, hc_view old_sk, hc_view new_sk,
+                         const size_t* digits, size_t d, double log2_alpha, hc_view keys) {
+    return guard([&] {
+        REQUIRE(R && st, HC_ERR_ARG, "null argument");
+        Base b = base_of(base, r);
+        R->check_base(b);
+        gen_ksk(R, b, old_sk, new_sk, digits_of(digits, d), st, log2_alpha, keys);
+        CK(hc_synchronize(R->ctx));
+    });
+}
+
+hc_status hc_bfv_gen_rk(hc_ring R, uint64_t* st, hc_view sk, const size_t* digits, size_t d, double log2_alpha,
+                        hc_view keys) {
+    return guard([&] {
+        REQUIRE(R && st, HC_ERR_ARG, "null argument");
+        Base b = prefix(R->initial_len);
+        Wide acc(R, 1, b);
+        acc.fma(0, 1, sk, 1, sk, 1);
+        Tensor sq(R->ctx, 1, (int64_t)b.size(), R->dl(), R->dk());
+        acc.reduce_into(sq.view());
+        gen_ksk(R, b, sq.view(), sk, digits_of(digits, d), st, log2_alpha, keys);
+        CK(hc_synchronize(R->ctx));
+    });
+}
+
+hc_status hc_bfv_gen_gk(hc_ring R, uint64_t* st, hc_view sk, uint64_t g, const size_t* digits, size_t d,
+                        double log2_alpha, hc_view keys) {
+    return guard([&] {
+        REQUIRE(R && st, HC_ERR_ARG, "null argument");
+        Base b = prefix(R->initial_len);
+        Tensor gs(R->ctx, 1, (int64_t)b.size(), R->dl(), R->dk());
+        R->apply_galois(gs.view(), sk, g);
+        gen_ksk(R, b, gs.view(), sk, digits_of(digits, d), st, log2_alpha, keys);
+        CK(hc_synchronize(R->ctx));
+    });
+}
+
+hc_status hc_bfv_noisy_plaintext(hc_ring R, hc_view ct, const size_t* base, size_t r, hc_view sk, hc_view out) {
+    return guard([&] {
+        REQUIRE(R, HC_ERR_ARG, "null ring");
+        Base b = base_of(base, r);
+        check_view(ct, 2, (int64_t)r, R->dl(), R->dk(), "ciphertext");
+        Wide acc(R, 1, b);
+        acc.fma(0, 1, vrows(ct, 1, 2), 1, vbase(sk, 0, (int64_t)r), 1);
+        acc.add(0, 1, vrows(ct, 0, 1), 1);
+        acc.reduce_into(out);
+        R->transform(out, b, true);
+    });
+}
+
+hc_status hc_bfv_key_switch(hc_ring R, hc_view c0, hc_view c1_pb, const size_t* base, size_t r, hc_view keys,
+                            const size_t* digits, size_t d, hc_view out) {
+    return guard([&] {
+        REQUIRE(R, HC_ERR_ARG, "null ring");
+        Base b = base_of(base, r);
+        check_view(out, 2, (int64_t)r, R->dl(), R->dk(), "key switch output");
+        Digits dg = clip(digits_of(digits, d), r);
+        Tensor parts = gadget_decompose(R, c1_pb, b, dg);
+        keyswitch(R, parts.view(), keys, b, dg.size(), &c0, nullptr, out);
+    });
+}
+
+hc_status hc_bfv_lift_to_extended(hc_ring R, hc_view pb, hc_view crt, const size_t* base, size_t r, hc_view out) {
+    return guard([&] {
+        REQUIRE(R, HC_ERR_ARG, "null ring");
+        Base b = base_of(base, r);
+        Tensor t = lift_to_extended(R, pb, crt.ptr ? &crt : nullptr, b);
+        check_view(out, t.shape[0], t.shape[1], t.shape[2], t.shape[3], "lift output");
+        CK(hc_assign(R->ctx, out, t.view()));
+    });
+}
+
+hc_status hc_bfv_rescale_to_base(hc_ring R, hc_view x, const size_t* base, size_t r, size_t base_len,
+                                 const int64_t t[2], hc_view out) {
+    return guard([&] {
+        REQUIRE(R && t, HC_ERR_ARG, "null argument");
+        Tensor o = rescale_to_base(R, x, base_of(base, r), base_len, words(t));
+        check_view(out, o.shape[0], o.shape[1], o.shape[2], o.shape[3], "rescale output");
+        CK(hc_assign(R->ctx, out, o.view()));
+    });
+}
+
+hc_status hc_bfv_mod_switch_down(hc_ring R, hc_view x, const size_t* base, size_t r, size_t new_len, hc_view out) {
+    return guard([&] {
+        REQUIRE(R, HC_ERR_ARG, "null ring");
+        Base b = base_of(base, r);
+        REQUIRE(new_len <= r, HC_ERR_ARG, "new length exceeds the base");
+        check_view(out, x.shape[0], (int64_t)new_len, R->dl(), R->dk(), "mod switch output");
+        if (new_len == r) {
+            CK(hc_assign(R->ctx, out, x));
+            return;
+        }
+        Base kept(b.begin(), b.begin() + new_len), dropped(b.begin() + new_len, b.end());
+        Tensor tmp(R->ctx, x.shape[0], (int64_t)new_len, R->dl(), R->dk());
+        R->bconv(tmp.view(), kept, vbase(x, (int64_t)new_len, (int64_t)r), dropped);
+        CK(hc_assign(R->ctx, out, vbase(x, 0, (int64_t)new_len)));
+        CK(hc_sub_i64(R->ctx, out, tmp.view()));
+        Tensor inv = R->scalar_tensor_big(kept, [&](int64_t p) { return invm(R->q_mod(dropped, p), p); });
+        std::vector<hc_modulus> m = R->mods(kept);
+        CK(hc_mul_mont64(R->ctx, out, inv.view(), m.data(), m.size()));
+    });
+}
+
+hc_status hc_bfv_hom_mul(hc_ring R, const int64_t t[2], hc_view ct1, hc_view ct2, const size_t* base, size_t r,
+                         hc_view rk, const size_t* digits, size_t d, int period_output, hc_view out) {
+    return guard([&] {
+        REQUIRE(R && t, HC_ERR_ARG, "null argument");
+        Base b = base_of(base, r);
+        const int64_t rr = (int64_t)r;
+        REQUIRE(ct1.shape[0] == 2 && ct2.shape[0] == 2, HC_ERR_SHAPE, "ciphertexts must have 2 rows");
+        check_view(ct1, 2, rr, R->dl(), R->dk(), "ct1");
+        check_view(ct2, 2, rr, R->dl(), R->dk(), "ct2");
+        check_view(out, 2, rr, R->dl(), R->dk(), "output");
+        // lift both operands (src/bfv.rs:762-768)
+        auto lift = [&](const hc_view& ct) {
+            Tensor pb(R->ctx, 2, rr, R->dl(), R->dk());
+            CK(hc_assign(R->ctx, pb.view(), ct));
+            R->transform(pb.view(), b, true);
+            return lift_to_extended(R, pb.view(), &ct, b);
+        };
+        Tensor l = lift(ct1), rt = lift(ct2);
+        Base ext;
+        for (int64_t i = rr; i < l.shape[1]; i++) ext.push_back(R->initial_len + (size_t)(i - rr));
+        Base lifted = b;
+        lifted.insert(lifted.end(), ext.begin(), ext.end());
+        // tensor product + reduce_wide (src/bfv.rs:667-683, :769-771)
+        Tensor prod(R->ctx, 3, (int64_t)lifted.size(), R->dl(), R->dk());
+        {
+            u128 mp = (u128)R->max_p(lifted), s1 = mp * mp;
+            int64_t mn = R->min_p(lifted);
+            CK(launch_tensor(R->ctx, kv(prod.view()), kv(l.view()), kv(rt.view()), R->kmods(lifted), needs_full(s1, mn),
+                             needs_full(2 * s1, mn), needs_full(s1, mn)));
+        }
+        R->transform(prod.view(), lifted, true);
+        Tensor resc = rescale_to_base(R, prod.view(), lifted, r, words(t));
+        // relinearisation (src/bfv.rs:699-741)
+        Digits dg = clip(digits_of(digits, d), r);
+        REQUIRE(rk.shape[0] >= 2 * (int64_t)dg.size() && rk.shape[1] >= rr, HC_ERR_SHAPE, "relinearisation key shape");
+        Tensor parts = gadget_decompose(R, vrows(resc.view(), 2, 3), b, dg);
+        if (!period_output) {
+            hc_view c01 = vrows(resc.view(), 0, 2);
+            R->transform(c01, b, false);
+            hc_view a0 = vrows(c01, 0, 1), a1 = vrows(c01, 1, 2);
+            keyswitch(R, parts.view(), rk, b, dg.size(), &a0, &a1, out);
+        } else {
+            keyswitch(R, parts.view(), rk, b, dg.size(), nullptr, nullptr, out);
+            R->transform(out, b, true);
+            CK(hc_add_i64(R->ctx, out, vrows(resc.view(), 0, 2)));
+        }
+    });
+}
+
+hc_status hc_bfv_hom_gal(hc_ring R, hc_view ct, const size_t* base, size_t r, const uint64_t* gs, size_t ngs,
+                         hc_view gks, const size_t* digits, size_t d, hc_view out) {
+    return guard([&] {
+        REQUIRE(R, HC_ERR_ARG, "null ring");
+        if (ngs == 0) return;
+        REQUIRE(gs, HC_ERR_ARG, "null automorphism list");
+        Base b = base_of(base, r);
+        const int64_t rr = (int64_t)r;
+        check_view(ct, 2, rr, R->dl(), R->dk(), "ciphertext");
+        check_view(out, 2 * (int64_t)ngs, rr, R->dl(), R->dk(), "output");
+        Digits dg = clip(digits_of(digits, d), r);
+        const int64_t per = 2 * (int64_t)d;
+        REQUIRE(gks.shape[0] == per * (int64_t)ngs && gks.shape[1] >= rr, HC_ERR_SHAPE, "galois key tensor shape");
+        Tensor c1(R->ctx, 1, rr, R->dl(), R->dk());
+        CK(hc_assign(R->ctx, c1.view(), vrows(ct, 1, 2)));
+        R->transform(c1.view(), b, true);
+        Tensor parts = gadget_decompose(R, c1.view(), b, dg);
+        hc_view c0 = vrows(ct, 0, 1);
+        for (size_t gi = 0; gi < ngs; gi++) {
+            PermCache& pc = R->perms(gs[gi]);
+            keyswitch(R, parts.view(), vrows(gks, per * (int64_t)gi, per * (int64_t)(gi + 1)), b, dg.size(), &c0,
+                      nullptr, vrows(out, 2 * (int64_t)gi, 2 * (int64_t)gi + 2), pc.p2.as<uint32_t>(),
+                      pc.p3.as<uint32_t>());
+        }
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,236 @@
+// Fused ring-level kernels. Each replaces a sequence of Backend calls of the reference's ring /
+// BFV layer with one pass over the data, computing exactly the same integers:
+//  - bconv_fused_kernel: BEHZ base conversion, plain (BConvCache::bconv,
+//    cyclosubfield-dbfv/src/ring.rs:1663-1701) and gadget-batched (GadgetBConvCache::bconv,
+//    src/ring.rs:1809-1851): mul_mont64 by (q/p)^-1, the small-K i128 matmul, the double reduction,
+//    the q~-scaled correction and the conversion to Montgomery form, without the i128 `tmp` /
+//    `correction` tensors ever reaching HBM.
+//  - galois_kernel: both permutation passes of apply_galois (src/ring.rs:1212-1222) as one gather.
+//  - keyswitch_kernel: the key-switch inner product, the addition of c0 / c1 through mont(1)
+//    and reduce_wide (src/bfv.rs:498-556, src/ring.rs:460-485, :503-509, :846-865).
+//  - tensor_kernel: hom_mul_raw_acc + reduce_wide (src/bfv.rs:667-683).
+#include "common.cuh"
+
+namespace {
+
+constexpr int BCONV_THREADS = 128;
+
+struct BconvArgs {
+    KView src;  // [ns, r, dl, dk]
+    KView dst;  // [ns * nb, rd, dl, dk]
+    const int64_t* qinv;   // [r] plain lifts of (Q_b / p_u)^-1 mod p_u
+    const int64_t* mat;    // [nb][rd + 1][r]
+    const int64_t* qmodp;  // [nb][rd]
+    const int32_t* ucol;   // [nb][2] source column range of output block b
+    int r, rd, nb;
+    int shift;
+    int chunk;  // acc_before_reduce of the reference
+    int64_t npos;
+};
+
+__global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a, KMods sm, KMods dm) {
+    extern __shared__ int64_t xs[];  // [r][BCONV_THREADS]
+    const int64_t i = blockIdx.y;
+    const int64_t pos = (int64_t)blockIdx.x * BCONV_THREADS + threadIdx.x;
+    const bool live = pos < a.npos;
+    int64_t k = 0, l = 0;
+    if (live) {
+        k = pos / a.src.n3;
+        l = pos - k * a.src.n3;
+    }
+    // the source is multiplied by (Q/p)^-1 in Montgomery form, giving plain lifts in (-p, p)
+    for (int u = 0; u < a.r; u++) {
+        int64_t x = live ? *kat<int64_t>(a.src, i, u, k, l) : 0;
+        xs[u * BCONV_THREADS + threadIdx.x] = live ? mul_mont(x, a.qinv[u], sm.n[u], sm.ninv[u]) : 0;
+    }
+    if (!live) return;
+    const i128 half = (i128)1 << (a.shift - 1);
+    for (int b = 0; b < a.nb; b++) {
+        const int u0 = a.ucol[2 * b], u1 = a.ucol[2 * b + 1];
+        const int64_t* mb = a.mat + (int64_t)b * (a.rd + 1) * a.r;
+        i128 corr = 0;
+        for (int u = u0; u < u1; u++)
+            corr = (i128)((u128)corr + (u128)((i128)mb[(int64_t)a.rd * a.r + u] * (i128)xs[u * BCONV_THREADS + threadIdx.x]));
+        const int64_t q = (int64_t)((i128)((u128)corr + (u128)half) >> a.shift);
+        for (int j = 0; j < a.rd; j++) {
+            const int64_t* mj = mb + (int64_t)j * a.r;
+            int64_t val = 0;
+            bool first = true;
+            // chunks of the reference's matmul (src/ring.rs:1678-1691), restricted to the
+            // columns the matrix does not zero
+            for (int c0 = 0; c0 < a.r; c0 += a.chunk) {
+                int c1 = min(c0 + a.chunk, a.r);
+                int lo = max(c0, u0), hi = min(c1, u1);
+                i128 acc = 0;
+                for (int u = lo; u < hi; u++)
+                    acc = (i128)((u128)acc + (u128)((i128)mj[u] * (i128)xs[u * BCONV_THREADS + threadIdx.x]));
+                int64_t red = double_red128(acc, dm.n[j], dm.ninv[j]);
+                val = first ? red : wadd(val, red);
+                first = false;
+            }
+            val = wadd(val, mul_mont(q, a.qmodp[(int64_t)b * a.rd + j], dm.n[j], dm.ninv[j]));
+            *kat<int64_t>(a.dst, i * a.nb + b, j, k, l) = to_mont64(val, dm.n[j], dm.ninv[j], dm.r2[j]);
+        }
+    }
+}
+
+/// dst[i,j,k,l] = src[i,j,p2[k],p3[l]]
+__global__ void __launch_bounds__(256) galois_kernel(KView d, KView s, const uint32_t* p2, const uint32_t* p3,
+                                                     int64_t lines, int chunks) {
+    const int64_t tiles = lines * chunks;
+    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        int64_t line = tile / chunks;
+        int64_t l = (tile - line * chunks) * blockDim.x + threadIdx.x;
+        if (l >= d.n3) continue;
+        int64_t k = line % d.n2, r = line / d.n2;
+        int64_t j = r % d.n1, i = r / d.n1;
+        *kat<int64_t>(d, i, j, k, l) = *kat<int64_t>(s, i, j, p2[k], p3[l]);
+    }
+}
+
+struct KsArgs {
+    KView parts[HC_MAX_TERMS];  // [1, r, dl, dk] digit t (dimension 0 broadcast)
+    KView keys[HC_MAX_TERMS];   // [2, r, dl, dk] key t restricted to the ciphertext base
+    int nterms;
+    KView add0, add1;  // optional (has_add*) CRT-basis summands of rows 0 / 1, multiplied by mont(1)
+    int has_add0, has_add1;
+    int full0, full1;  // rows needing the full double reduction
+    KView dst;         // [2, r, dl, dk]
+    // optional Galois permutation applied to parts and summands (apply_galois fused into the
+    // read, src/bfv.rs:819-820); null means identity
+    const uint32_t* p2;
+    const uint32_t* p3;
+};
+
+__device__ __forceinline__ int64_t finish_wide(i128 acc, bool full, const KMods& m, int j) {
+    return full ? to_mont64(double_red128(acc, m.n[j], m.ninv[j]), m.n[j], m.ninv[j], m.r2[j])
+                : red128(acc, m.n[j], m.ninv[j]);
+}
+
+__global__ void __launch_bounds__(256) keyswitch_kernel(KsArgs a, KMods m, const int64_t* one, int64_t lines,
+                                                        int chunks) {
+    const int64_t tiles = lines * chunks;
+    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        int64_t line = tile / chunks;  // (j, k)
+        int64_t l = (tile - line * chunks) * blockDim.x + threadIdx.x;
+        if (l >= a.dst.n3) continue;
+        int64_t k = line % a.dst.n2, j = line / a.dst.n2;
+        const int64_t sk = a.p2 ? (int64_t)a.p2[k] : k, sl = a.p3 ? (int64_t)a.p3[l] : l;
+        i128 acc0 = 0, acc1 = 0;
+        for (int t = 0; t < a.nterms; t++) {
+            int64_t x = *kat<int64_t>(a.parts[t], 0, j, sk, sl);
+            int64_t k0 = *kat<int64_t>(a.keys[t], 0, j, k, l);
+            int64_t k1 = *kat<int64_t>(a.keys[t], 1, j, k, l);
+            acc0 = (i128)((u128)acc0 + (u128)((i128)x * (i128)k0));
+            acc1 = (i128)((u128)acc1 + (u128)((i128)x * (i128)k1));
+        }
+        const int64_t o = one[j];
+        if (a.has_add0) acc0 = (i128)((u128)acc0 + (u128)((i128)*kat<int64_t>(a.add0, 0, j, sk, sl) * (i128)o));
+        if (a.has_add1) acc1 = (i128)((u128)acc1 + (u128)((i128)*kat<int64_t>(a.add1, 0, j, sk, sl) * (i128)o));
+        *kat<int64_t>(a.dst, 0, j, k, l) = finish_wide(acc0, a.full0, m, (int)j);
+        *kat<int64_t>(a.dst, 1, j, k, l) = finish_wide(acc1, a.full1, m, (int)j);
+    }
+}
+
+/// (l0 r0, l0 r1 + l1 r0, l1 r1) of two 2-row ciphertext tensors, reduced per row.
+__global__ void __launch_bounds__(256) tensor_kernel(KView d, KView lhs, KView rhs, KMods m, int full0, int full1,
+                                                     int full2, int64_t lines, int chunks) {
+    const int64_t tiles = lines * chunks;
+    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        int64_t line = tile / chunks;  // (j, k)
+        int64_t l = (tile - line * chunks) * blockDim.x + threadIdx.x;
+        if (l >= d.n3) continue;
+        int64_t k = line % d.n2, j = line / d.n2;
+        int64_t l0 = *kat<int64_t>(lhs, 0, j, k, l), l1 = *kat<int64_t>(lhs, 1, j, k, l);
+        int64_t r0 = *kat<int64_t>(rhs, 0, j, k, l), r1 = *kat<int64_t>(rhs, 1, j, k, l);
+        i128 a0 = (i128)l0 * (i128)r0;
+        i128 a1 = (i128)((u128)((i128)l0 * (i128)r1) + (u128)((i128)l1 * (i128)r0));
+        i128 a2 = (i128)l1 * (i128)r1;
+        *kat<int64_t>(d, 0, j, k, l) = finish_wide(a0, full0, m, (int)j);
+        *kat<int64_t>(d, 1, j, k, l) = finish_wide(a1, full1, m, (int)j);
+        *kat<int64_t>(d, 2, j, k, l) = finish_wide(a2, full2, m, (int)j);
+    }
+}
+
+void grid_lines(hc_context ctx, int64_t n3, int64_t lines, int* chunks, unsigned* blocks) {
+    *chunks = (int)((n3 + 255) / 256);
+    int64_t tiles = lines * *chunks;
+    int64_t cap = (int64_t)hc::num_sms(ctx) * 32;
+    *blocks = (unsigned)(tiles < cap ? (tiles > 0 ? tiles : 1) : cap);
+}
+
+}  // namespace
+
+namespace hc {
+
+hc_status launch_bconv_fused(hc_context ctx, const KView& src, const KView& dst, const int64_t* qinv,
+                             const int64_t* mat, const int64_t* qmodp, const int32_t* ucol, int r, int rd, int nb,
+                             int shift, int chunk, const KMods& sm, const KMods& dm, int64_t ns) {
+    BconvArgs a;
+    a.src = src;
+    a.dst = dst;
+    a.qinv = qinv, a.mat = mat, a.qmodp = qmodp, a.ucol = ucol;
+    a.r = r, a.rd = rd, a.nb = nb, a.shift = shift, a.chunk = chunk;
+    a.npos = src.n2 * src.n3;
+    if (a.npos == 0 || ns == 0 || rd == 0) return HC_OK;
+    size_t smem = (size_t)r * BCONV_THREADS * 8;
+    if (smem > 49152) {
+        if (smem > max_smem_optin(ctx)) return fail(HC_ERR_UNSUPPORTED, "base conversion: too many source rows");
+        cudaError_t e = cudaFuncSetAttribute(bconv_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return cuda_check(e, "bconv smem attribute");
+    }
+    if (ns > 65535) return fail(HC_ERR_UNSUPPORTED, "base conversion: batch too large");
+    dim3 grid((unsigned)((a.npos + BCONV_THREADS - 1) / BCONV_THREADS), (unsigned)ns);
+    bconv_fused_kernel<<<grid, BCONV_THREADS, smem, stream_of(ctx)>>>(a, sm, dm);
+    count_launch(ctx);
+    return cuda_check(cudaGetLastError(), "bconv kernel launch");
+}
+
+hc_status launch_galois(hc_context ctx, const KView& d, const KView& s, const uint32_t* p2, const uint32_t* p3) {
+    int64_t lines = d.n0 * d.n1 * d.n2;
+    if (lines == 0 || d.n3 == 0) return HC_OK;
+    int chunks;
+    unsigned blocks;
+    grid_lines(ctx, d.n3, lines, &chunks, &blocks);
+    galois_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(d, s, p2, p3, lines, chunks);
+    count_launch(ctx);
+    return cuda_check(cudaGetLastError(), "galois kernel launch");
+}
+
+hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys, int nterms, const KView* add0,
+                           const KView* add1, int full0, int full1, const KView& dst, const KMods& m,
+                           const int64_t* one_dev, const uint32_t* p2, const uint32_t* p3) {
+    if (nterms > HC_MAX_TERMS) return fail(HC_ERR_UNSUPPORTED, "too many gadget digits");
+    KsArgs a;
+    for (int t = 0; t < nterms; t++) a.parts[t] = parts[t], a.keys[t] = keys[t];
+    a.nterms = nterms;
+    a.has_add0 = add0 != nullptr;
+    a.has_add1 = add1 != nullptr;
+    if (add0) a.add0 = *add0;
+    if (add1) a.add1 = *add1;
+    a.full0 = full0, a.full1 = full1;
+    a.dst = dst;
+    a.p2 = p2, a.p3 = p3;
+    int64_t lines = dst.n1 * dst.n2;
+    if (lines == 0 || dst.n3 == 0) return HC_OK;
+    int chunks;
+    unsigned blocks;
+    grid_lines(ctx, dst.n3, lines, &chunks, &blocks);
+    keyswitch_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(a, m, one_dev, lines, chunks);
+    count_launch(ctx);
+    return cuda_check(cudaGetLastError(), "keyswitch kernel launch");
+}
+
+hc_status launch_tensor(hc_context ctx, const KView& d, const KView& lhs, const KView& rhs, const KMods& m, int f0,
+                        int f1, int f2) {
+    int64_t lines = d.n1 * d.n2;
+    if (lines == 0 || d.n3 == 0) return HC_OK;
+    int chunks;
+    unsigned blocks;
+    grid_lines(ctx, d.n3, lines, &chunks, &blocks);
+    tensor_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(d, lhs, rhs, m, f0, f1, f2, lines, chunks);
+    count_launch(ctx);
+    return cuda_check(cudaGetLastError(), "tensor kernel launch");
+}
+
+}  // namespace hc

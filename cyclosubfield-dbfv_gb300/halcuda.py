@@ -130,7 +130,8 @@ class _Alloc:
 
     def __del__(self):
         try:
-            lib().hc_free(self.ctx.h, ctypes.c_void_p(self.ptr))
+            if self.ctx.h:  # a closed context already released its memory pool
+                lib().hc_free(self.ctx.h, ctypes.c_void_p(self.ptr))
         except Exception:
             pass
 
@@ -150,7 +151,8 @@ class NttPlan:
 
     def __del__(self):
         try:
-            lib().hc_destroy_ntt_plan(self.ctx.h, self.h)
+            if self.ctx.h:
+                lib().hc_destroy_ntt_plan(self.ctx.h, self.h)
         except Exception:
             pass
 
@@ -161,7 +163,8 @@ class PermPlan:
 
     def __del__(self):
         try:
-            lib().hc_destroy_permutation(self.ctx.h, self.h)
+            if self.ctx.h:
+                lib().hc_destroy_permutation(self.ctx.h, self.h)
         except Exception:
             pass
 
@@ -173,9 +176,20 @@ class CudaBackend:
         h = ctypes.c_void_p()
         check(lib().hc_context_create(ctypes.c_int(device), ctypes.byref(h)))
         self.h = h
+        self._dependents = []  # weak references to objects that must be released first
+
+    def add_dependent(self, obj):
+        import weakref
+
+        self._dependents.append(weakref.ref(obj))
 
     def close(self):
+        """Releases dependents (ring contexts), then the context; later frees are no-ops."""
         if self.h:
+            for ref in self._dependents:
+                obj = ref()
+                if obj is not None:
+                    obj.close()
             lib().hc_context_destroy(self.h)
             self.h = None
 

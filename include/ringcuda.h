@@ -1,0 +1,106 @@
+/*
+ * ringcuda.h — ring-level and BFV-level entry points of the GB300 backend.
+ *
+ * The reference runs its ring (cyclosubfield-dbfv/src/ring.rs) and BFV (src/bfv.rs) layers on top
+ * of the HAL trait. These entry points are the same operations with the HAL call sequences fused
+ * into few sm_103a kernels (base conversion, Galois permutation, key-switch inner product,
+ * tensor product); results are bit-identical to the reference's call sequences over
+ * `hal::cpu` on the same inputs. A Rust `hal::cuda` binding only needs include/halcuda.h; these
+ * exist for callers that want the fused hot path, and for the batched/served forms.
+ *
+ * Layout: a batch of ring elements over an RNS base of r factors is a 4-D device tensor
+ * [count, r, deg_L', deg_K] of Montgomery-form residues (src/ring.rs:3-13). RNS bases are lists
+ * of factor indices into the context's prime list (`RNSBaseIndices`, src/ring.rs:132-134).
+ * Key-switching keys with d digits over r_key factors are 4-D tensors [2 d, r_key, deg_L', deg_K]
+ * (rows 2t, 2t+1 hold the two components of digit t; src/bfv.rs:56-64). Gadget digits are
+ * passed as d (start, end) pairs of base positions. Plaintext moduli t are i128 values given as
+ * (low, high) int64 words. Random numbers come from the reference's splitmix64 generator
+ * (src/bfv.rs:880-886) whose 64-bit state the caller owns and which the call advances.
+ */
+#ifndef RINGCUDA_H
+#define RINGCUDA_H
+
+#include "halcuda.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct hc_ring_s* hc_ring;
+
+/* RingContext::new (src/ring.rs:622-652): samples the initial base of log2_q_lo..log2_q_hi bits
+ * and the extension pool, with NTT plans and CRT kernels per factor. Fields: "field_2",
+ * "field_16", "field_18", "field_32", "field_192", "field_36864", "field_49152". */
+hc_status hc_ring_create(hc_context ctx, const char* field, size_t log2_q_lo, size_t log2_q_hi, size_t t_bits,
+                         hc_ring* out);
+/* RingContext::new_raw (src/ring.rs:657-677): given primes, base conversions only. */
+hc_status hc_ring_create_raw(hc_context ctx, const char* field, const int64_t* primes, size_t n, hc_ring* out);
+hc_status hc_ring_destroy(hc_ring ring);
+size_t hc_ring_num_factors(hc_ring ring);
+int64_t hc_ring_prime(hc_ring ring, size_t idx);
+size_t hc_ring_initial_len(hc_ring ring);
+/* out[0] = n = deg_L, out[1] = deg_L', out[2] = deg_K */
+hc_status hc_ring_dims(hc_ring ring, size_t out[3]);
+hc_status hc_ring_modulus(hc_ring ring, size_t idx, hc_modulus* out);
+/* RingContext::extension_rns_base_for (src/ring.rs:716-731) */
+hc_status hc_ring_extension_base(hc_ring ring, const size_t* base, size_t r, size_t* out, size_t* out_len);
+/* NTT-domain CRT kernels of one factor (src/ring.rs:1338-1415): kernel_L' | kernel_K |
+ * inverse kernel_L' | inverse kernel_K, host output of 2 (deg_L' + deg_K) values. */
+hc_status hc_ring_crt_kernels(hc_ring ring, size_t idx, int64_t* out);
+
+/* pb_to_crt_tensor / crt_to_pb_tensor (src/ring.rs:1118-1161), in place; inputs bounded by 2p. */
+hc_status hc_ring_pb_to_crt(hc_ring ring, hc_view data, const size_t* base, size_t r);
+hc_status hc_ring_crt_to_pb(hc_ring ring, hc_view data, const size_t* base, size_t r);
+/* bconv_tensors (src/ring.rs:1527-1535): src [count, rs, ...] -> dst [count, rd, ...]. Unlike the
+ * reference, `src` is left unchanged. */
+hc_status hc_ring_bconv(hc_ring ring, hc_view dst, const size_t* dst_base, size_t rd, hc_view src,
+                        const size_t* src_base, size_t rs);
+/* bconv_gadget_tensors (src/ring.rs:1566-1574): src [1, r, ...] -> dst [d, r, ...]; src unchanged. */
+hc_status hc_ring_bconv_gadget(hc_ring ring, hc_view dst, hc_view src, const size_t* base, size_t r,
+                               const size_t* digits, size_t d);
+/* apply_galois (src/ring.rs:1183-1222), one gather pass. */
+hc_status hc_ring_apply_galois(hc_ring ring, hc_view dst, hc_view src, const size_t* base, size_t r, uint64_t g);
+
+/* ---------------------------------------------------------------- BFV (src/bfv.rs) */
+/* gen_sk (:180-190): sk [1, r0, ...] over the initial base, CRT basis */
+hc_status hc_bfv_gen_sk(hc_ring ring, uint64_t* rng_state, hc_view sk);
+/* bfv_enc (:294-307): ptxt holds n i128 coefficients (2 words each); ct [2, r, ...] */
+hc_status hc_bfv_enc(hc_ring ring, uint64_t* rng_state, const size_t* base, size_t r, const int64_t t[2],
+                     const int64_t* ptxt, hc_view sk, double log2_alpha, hc_view ct);
+/* gen_ksk (:433-458), gen_rk (:462-474), gen_gk (:479-491); keys [2 d, r, ...] */
+hc_status hc_bfv_gen_ksk(hc_ring ring, uint64_t* rng_state, const size_t* base, size_t r, hc_view old_sk,
+                         hc_view new_sk, const size_t* digits, size_t d, double log2_alpha, hc_view keys);
+hc_status hc_bfv_gen_rk(hc_ring ring, uint64_t* rng_state, hc_view sk, const size_t* digits, size_t d,
+                        double log2_alpha, hc_view keys);
+hc_status hc_bfv_gen_gk(hc_ring ring, uint64_t* rng_state, hc_view sk, uint64_t g, const size_t* digits, size_t d,
+                        double log2_alpha, hc_view keys);
+/* log2_alpha_for_sigma (:165-167) */
+double hc_bfv_log2_alpha_for_sigma(hc_ring ring, const size_t* base, size_t r, double sigma);
+/* noisy_plaintext (:330-343): c0 + c1 s in period basis, out [1, r, ...] (decoding is host work) */
+hc_status hc_bfv_noisy_plaintext(hc_ring ring, hc_view ct, const size_t* base, size_t r, hc_view sk, hc_view out);
+/* key_switch (:533-556): c0 [1, r] CRT basis, c1 [1, r] period basis, keys over r_key >= r rows
+ * (restricted on the fly) -> out [2, r] CRT basis */
+hc_status hc_bfv_key_switch(hc_ring ring, hc_view c0_crt, hc_view c1_pb, const size_t* base, size_t r, hc_view keys,
+                            const size_t* digits, size_t d, hc_view out);
+/* lift_to_extended (:564-595): pb [count, r] (bound <= 2), crt optional (ptr NULL = absent)
+ * -> out [count, r + ext] CRT basis */
+hc_status hc_bfv_lift_to_extended(hc_ring ring, hc_view pb, hc_view crt, const size_t* base, size_t r, hc_view out);
+/* rescale_to_base (:601-622): x [count, r + ext] period basis (modified) -> out [count, base_len] */
+hc_status hc_bfv_rescale_to_base(hc_ring ring, hc_view x, const size_t* base, size_t r, size_t base_len,
+                                 const int64_t t[2], hc_view out);
+/* mod_switch_down (:628-662): x [count, r] period basis -> out [count, new_len] */
+hc_status hc_bfv_mod_switch_down(hc_ring ring, hc_view x, const size_t* base, size_t r, size_t new_len, hc_view out);
+/* bfv_hom_mul (:747-775): ct1, ct2 [2, r] CRT basis -> out [2, r] (CRT basis, or period basis
+ * with bound 2 when period_output != 0). */
+hc_status hc_bfv_hom_mul(hc_ring ring, const int64_t t[2], hc_view ct1, hc_view ct2, const size_t* base, size_t r,
+                         hc_view rk, const size_t* digits, size_t d, int period_output, hc_view out);
+/* bfv_hom_gal (:783-841): one Galois key per automorphism, gks [ngs * 2 d, r_key, ...]
+ * -> out [ngs * 2, r, ...] CRT basis */
+hc_status hc_bfv_hom_gal(hc_ring ring, hc_view ct, const size_t* base, size_t r, const uint64_t* gs, size_t ngs,
+                         hc_view gks, const size_t* digits, size_t d, hc_view out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RINGCUDA_H */
