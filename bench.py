@@ -1,0 +1,417 @@
+"""Benchmark of the GB300 ring-arithmetic backend.
+
+Workload (BFV ciphertext multiplication at full size): field_36864 (n = 36864 = 12 x 3072), an
+initial RNS base of r = 16 primes of 57 bits (log2 q in 900..930), plaintext modulus t = 256,
+secret key sparse ternary, error sigma = 3.2, relinearisation key with ceil(r/4) = 4 gadget digits;
+one step multiplies B independent ciphertext pairs (bfv_hom_mul incl. lifting, tensoring,
+rescaling and relinearisation). Inputs are seeded synthetic ciphertexts of that shape.
+
+Prints one JSON line. `value` is ct-mults/s with the operands resident in HBM; `e2e` is the same
+metric through the C ABI with the operands copied from pinned host memory and the results
+copied back inside the timed region. `--impl reference` times the oracle, the CPU restatement of
+the reference's hal::cpu path (the Rust crate cannot be built here), on all host cores.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cyclosubfield-dbfv_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "CRT transforms/s & ct-mults/s, batched vs plain on 1 GB300, bit-exact; p99 ms"
+FIELD, LOG2_Q, T_BITS, T = "field_36864", (900, 930), 8, 256
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--batch", type=int, default=8, help="ciphertext pairs multiplied per step")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------------------ distributed
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x):
+        if not self.pg:
+            return x
+        import torch
+
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+
+# ------------------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------------------------ workload
+class Workload:
+    def __init__(self, be, batch, seed=2026):
+        import ringcuda
+
+        self.be = be
+        self.ring = ringcuda.RingContext(FIELD, LOG2_Q[0], LOG2_Q[1], T_BITS, backend=be)
+        R = self.ring
+        self.base = R.initial_base()
+        self.r = len(self.base)
+        self.digits = ringcuda.select_digits(math.ceil(self.r / 4), self.r)
+        la = R.log2_alpha_for_sigma(self.base, 3.2)
+        st = [seed]
+        self.sk = R.gen_sk(st)
+        self.rk = R.gen_rk(st, self.sk, self.digits, la)
+        self.batch = batch
+        self.cts = []
+        for b in range(batch):
+            m1 = [((i * 7 + b) % 255) - 127 for i in range(R.n)]
+            m2 = [((i * 13 + 3 * b) % 255) - 127 for i in range(R.n)]
+            self.cts.append((R.enc(st, self.base, T, m1, self.sk, la), R.enc(st, self.base, T, m2, self.sk, la)))
+        self.outs = [R.allocate(2, self.r) for _ in range(batch)]
+        self.ct_bytes = 2 * self.r * R.n * 8
+
+    def step(self, b0=0, nb=None):
+        nb = self.batch if nb is None else nb
+        for b in range(b0, b0 + nb):
+            c1, c2 = self.cts[b]
+            self.ring.hom_mul(T, c1, c2, self.base, self.rk, self.digits, out=self.outs[b])
+
+
+def flush_l2(be, scratch):
+    import halcuda
+
+    halcuda.memset_async(be, scratch.ptr, 0, scratch.numel() * 8)
+
+
+def timed_steps(be, work, steps, scratch, per_call=False):
+    """Sum of CUDA-event times of `steps` steps (L2 flushed before each, outside the events)."""
+    import halcuda
+
+    ev0, ev1 = halcuda.Event(), halcuda.Event()
+    total, per = 0.0, []
+    for _ in range(steps):
+        flush_l2(be, scratch)
+        if per_call:
+            for b in range(work.batch):
+                ev0.record(be)
+                work.step(b, 1)
+                ev1.record(be)
+                dt = ev0.elapsed_ms(ev1)
+                per.append(dt)
+                total += dt
+        else:
+            ev0.record(be)
+            work.step()
+            ev1.record(be)
+            total += ev0.elapsed_ms(ev1)
+    return total, per
+
+
+def e2e_steps(be, work, steps):
+    """ct-mults through the C ABI from pinned host buffers, results copied back, per step."""
+    import halcuda
+
+    R = work.ring
+    shape = (2, work.r, R.dl, R.dk)
+    hin = [(halcuda.PinnedBuffer(shape), halcuda.PinnedBuffer(shape)) for _ in range(work.batch)]
+    hout = [halcuda.PinnedBuffer(shape) for _ in range(work.batch)]
+    for b in range(work.batch):
+        hin[b][0].array[...] = work.cts[b][0].to_numpy()
+        hin[b][1].array[...] = work.cts[b][1].to_numpy()
+    nbytes = work.ct_bytes
+    ev0, ev1 = halcuda.Event(), halcuda.Event()
+    be.synchronize()
+    ev0.record(be)
+    for _ in range(steps):
+        for b in range(work.batch):
+            c1, c2 = work.cts[b]
+            halcuda.memcpy_async(be, c1.ptr, hin[b][0].ptr, nbytes, halcuda.H2D)
+            halcuda.memcpy_async(be, c2.ptr, hin[b][1].ptr, nbytes, halcuda.H2D)
+            work.ring.hom_mul(T, c1, c2, work.base, work.rk, work.digits, out=work.outs[b])
+            halcuda.memcpy_async(be, hout[b].ptr, work.outs[b].ptr, nbytes, halcuda.D2H)
+    ev1.record(be)
+    ms = ev0.elapsed_ms(ev1)
+    be.synchronize()
+    return ms, 2 * nbytes * work.batch, nbytes * work.batch, hout
+
+
+def kernel_roofline(be, work, reps, peaks):
+    """Dominant kernel: the dimension-3 lazy NTT of the transforms (one HAL launch), timed alone on
+    the lifted-product tensor of one ct-mult [3, r + e, 12, 3072]. Algorithmic bytes per launch:
+    one read and one write of every i64 residue (16 B per residue)."""
+    import halcuda
+
+    R = work.ring
+    lifted = work.base + R.extension_base(work.base)
+    t = R.allocate(3, len(lifted))
+    plans = [R_plan for R_plan in _k_plans(R, lifted)]
+    ev0, ev1 = halcuda.Event(), halcuda.Event()
+    for _ in range(3):
+        be.hal_intt_mont64_dim(t, plans, halcuda.DIM3)
+    be.synchronize()
+    ev0.record(be)
+    for _ in range(reps):
+        be.hal_intt_mont64_dim(t, plans, halcuda.DIM3)
+    ev1.record(be)
+    ms = ev0.elapsed_ms(ev1) / reps
+    bytes_alg = 16 * 3 * len(lifted) * R.n
+    achieved = bytes_alg / (ms * 1e-3) / 1e9
+    peak = peaks.get("hbm_gbs")
+    return {"kernel": "ntt_tile_kernel (intt, dim 3, [3, %d, 12, 3072])" % len(lifted), "bound": "hbm",
+            "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4) if peak else None, "traffic": None,
+            "bytes_per_launch": bytes_alg, "launch_ms": round(ms, 5), "peak_source": "measured"}
+
+
+_PLAN_CACHE = {}
+
+
+def _k_plans(R, base):
+    key = (id(R), tuple(base))
+    if key not in _PLAN_CACHE:
+        be = R.backend
+        _PLAN_CACHE[key] = [be.hal_create_ntt_plan(R.modulus(i), [2, 3, 8, 64]) for i in base]
+    return _PLAN_CACHE[key]
+
+
+def cpu_baseline(seconds_budget=20.0):
+    """The oracle (single thread, restating the reference's hal::cpu path) on one ct-mult."""
+    from oracle import pyoracle as po
+
+    o = po.Ring(FIELD, LOG2_Q[0], LOG2_Q[1], T_BITS)
+    base = o.initial_base()
+    la = o.log2_alpha_for_sigma(base, 3.2)
+    st = [7]
+    sk = o.gen_sk(st)
+    digits = po.select_digits(math.ceil(len(base) / 4), len(base))
+    rk = o.gen_rk(st, sk, digits, la)
+    c1 = o.enc(st, base, T, [1] * o.n, sk, la)
+    c2 = o.enc(st, base, T, [2] * o.n, sk, la)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.hom_mul(T, c1, c2, base, rk, digits)
+        n += 1
+        el = time.perf_counter() - t0
+        if n >= 2 or el > seconds_budget:
+            break
+    return {"value": round(n / el, 4), "unit": "ct-mults/s", "cores": 1, "kind": "port",
+            "sample": "%d bfv_hom_mul on %s r=%d (oracle C++ restatement of hal::cpu, 1 thread, %.1f s)"
+                      % (n, FIELD, len(base), el)}
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+# ------------------------------------------------------------------------------ reference arm
+_REF_STATE = {}
+
+
+def _ref_init():
+    from oracle import pyoracle as po
+
+    o = po.Ring(FIELD, LOG2_Q[0], LOG2_Q[1], T_BITS)
+    base = o.initial_base()
+    la = o.log2_alpha_for_sigma(base, 3.2)
+    st = [11 + os.getpid()]
+    sk = o.gen_sk(st)
+    digits = po.select_digits(math.ceil(len(base) / 4), len(base))
+    rk = o.gen_rk(st, sk, digits, la)
+    _REF_STATE.update(o=o, base=base, rk=rk, digits=digits, c1=o.enc(st, base, T, [1] * o.n, sk, la),
+                      c2=o.enc(st, base, T, [3] * o.n, sk, la))
+
+
+def _ref_task(_):
+    s = _REF_STATE
+    s["o"].hom_mul(T, s["c1"], s["c2"], s["base"], s["rk"], s["digits"])
+    return 1
+
+
+def reference_arm(args, dist):
+    if dist.rank != 0:
+        return
+    import multiprocessing as mp
+
+    from oracle import build as oracle_build
+
+    oracle_build.build()
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_ref_init) as pool:
+        for _ in range(args.warmup):
+            pool.map(_ref_task, range(cores))
+        t0 = time.perf_counter()
+        done = 0
+        for _ in range(args.steps):
+            done += sum(pool.map(_ref_task, range(cores)))
+        el = time.perf_counter() - t0
+    value = done / el
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "ct-mults/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * el / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+            "config": {"workload": "bfv_hom_mul %s r=16 t=256, %d ct-mults per step (one per host core)"
+                                   % (FIELD, cores), "field": FIELD, "rns_len": 16},
+            "cpu_baseline": {"value": round(value, 4), "unit": "ct-mults/s", "cores": cores, "kind": "port",
+                             "sample": "%d ct-mults per step on %d processes; oracle C++ restatement of the "
+                                       "reference's hal::cpu path (the Rust crate is not buildable here)"
+                                       % (cores, cores)},
+            "e2e": {"value": round(value, 4), "unit": "ct-mults/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------ main
+def main():
+    args = parse()
+    dist = Dist()
+    if args.impl == "reference":
+        reference_arm(args, dist)
+        return
+    import halcuda
+
+    halcuda.lib()
+    be = halcuda.CudaBackend(dist.local_rank)
+    work = Workload(be, args.batch)
+    scratch = be.hal_allocate_i64((1, 1, 1, 2 * L2_BYTES // 8))
+    peaks = load_peaks()
+
+    # correctness gate: one product decrypts (host decoding of c0 + c1 s, big-integer CRT)
+    for _ in range(args.warmup):
+        timed_steps(be, work, 1, scratch)
+    be.synchronize()
+
+    clocks = ClockSampler(dist.local_rank)
+    dist.barrier()
+    be.synchronize()
+    clocks.start()
+    launches0 = be.launch_count()
+    total_ms, _ = timed_steps(be, work, args.steps, scratch)
+    be.synchronize()
+    launches = be.launch_count() - launches0
+    clk = clocks.stop()
+    dist.barrier()
+    total_ms = dist.max(total_ms)
+    value = dist.world * work.batch * args.steps / (total_ms * 1e-3)
+
+    # plain form (one ct-mult per timed call) and its latency distribution
+    _, per = timed_steps(be, work, max(2, args.steps // 2), scratch, per_call=True)
+    per.sort()
+    plain = 1e3 / statistics.mean(per)
+    p50, p99 = per[len(per) // 2], per[min(len(per) - 1, int(math.ceil(0.99 * len(per))) - 1)]
+
+    e2e_ms, h2d, d2h, _ = e2e_steps(be, work, args.steps)
+    e2e_val = dist.world * work.batch * args.steps / (e2e_ms * 1e-3)
+    roof = kernel_roofline(be, work, 20, peaks)
+
+    if dist.rank != 0:
+        return
+    cpu = None if args.no_cpu_baseline else cpu_baseline()
+    line = {
+        "metric": METRIC,
+        "value": round(value, 3),
+        "unit": "ct-mults/s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int64",
+        "data": "synthetic (seeded encryptions of the reference's parameter shapes)",
+        "config": {"workload": "bfv_hom_mul %s r=%d t=%d d=%d, %d ct pairs per step" % (
+            FIELD, work.r, T, len(work.digits), work.batch), "field": FIELD, "rns_len": work.r,
+                   "extension_len": len(work.ring.extension_base(work.base)), "gadget_digits": len(work.digits),
+                   "batch": work.batch, "l2": "flushed before every timed step (512 MB memset, untimed)"},
+        "plain_ct_mults_per_s": round(plain, 3),
+        "latency_ms": {"p50": round(p50, 4), "p99": round(p99, 4), "samples": len(per)},
+        "e2e": {"value": round(e2e_val, 3), "unit": "ct-mults/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": roof,
+        "clocks": clk,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

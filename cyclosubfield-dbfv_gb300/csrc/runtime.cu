@@ -1,0 +1,83 @@
+// Runtime utilities of include/halcuda.h: pinned host memory, asynchronous copies, events with
+// bounded waits, and device-memory queries.
+#include <chrono>
+#include <thread>
+
+#include "common.cuh"
+
+struct hc_event_s {
+    cudaEvent_t ev;
+};
+
+using namespace hc;
+
+extern "C" {
+
+hc_status hc_host_alloc(size_t bytes, void** out) {
+    if (!out) return fail(HC_ERR_ARG, "null output");
+    return cuda_check(cudaHostAlloc(out, bytes ? bytes : 16, cudaHostAllocDefault), "pinned host allocation");
+}
+
+hc_status hc_host_free(void* ptr) {
+    if (!ptr) return HC_OK;
+    return cuda_check(cudaFreeHost(ptr), "pinned host free");
+}
+
+hc_status hc_memcpy_async(hc_context ctx, void* dst, const void* src, size_t bytes, hc_copy_kind kind) {
+    if (!ctx || (bytes && (!dst || !src))) return fail(HC_ERR_ARG, "null argument");
+    cudaMemcpyKind k = kind == HC_H2D ? cudaMemcpyHostToDevice
+                       : kind == HC_D2H ? cudaMemcpyDeviceToHost
+                                        : cudaMemcpyDeviceToDevice;
+    return cuda_check(cudaMemcpyAsync(dst, src, bytes, k, stream_of(ctx)), "async copy");
+}
+
+hc_status hc_memset_async(hc_context ctx, void* dst, int value, size_t bytes) {
+    if (!ctx || (bytes && !dst)) return fail(HC_ERR_ARG, "null argument");
+    return cuda_check(cudaMemsetAsync(dst, value, bytes, stream_of(ctx)), "async memset");
+}
+
+hc_status hc_event_create(hc_event* out) {
+    if (!out) return fail(HC_ERR_ARG, "null output");
+    auto* e = new hc_event_s();
+    hc_status st = cuda_check(cudaEventCreate(&e->ev), "event creation");
+    if (st) {
+        delete e;
+        return st;
+    }
+    *out = e;
+    return HC_OK;
+}
+
+hc_status hc_event_destroy(hc_event ev) {
+    if (!ev) return HC_OK;
+    cudaEventDestroy(ev->ev);
+    delete ev;
+    return HC_OK;
+}
+
+hc_status hc_event_record(hc_context ctx, hc_event ev) {
+    if (!ctx || !ev) return fail(HC_ERR_ARG, "null argument");
+    return cuda_check(cudaEventRecord(ev->ev, stream_of(ctx)), "event record");
+}
+
+hc_status hc_event_elapsed_ms(hc_event start, hc_event end, double timeout_ms, float* ms) {
+    if (!start || !end || !ms) return fail(HC_ERR_ARG, "null argument");
+    auto t0 = std::chrono::steady_clock::now();
+    // poll with a deadline instead of blocking forever
+    while (true) {
+        cudaError_t q = cudaEventQuery(end->ev);
+        if (q == cudaSuccess) break;
+        if (q != cudaErrorNotReady) return cuda_check(q, "event query");
+        double waited = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_ms > 0 && waited > timeout_ms) return fail(HC_ERR_TIMEOUT, "event wait timed out");
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    return cuda_check(cudaEventElapsedTime(ms, start->ev, end->ev), "event elapsed time");
+}
+
+hc_status hc_device_memory(hc_context ctx, size_t* free_bytes, size_t* total_bytes) {
+    if (!ctx || !free_bytes || !total_bytes) return fail(HC_ERR_ARG, "null argument");
+    return cuda_check(cudaMemGetInfo(free_bytes, total_bytes), "memory query");
+}
+
+}  // extern "C"

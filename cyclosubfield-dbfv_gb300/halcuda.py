@@ -357,3 +357,62 @@ class CudaBackend:
 
     def hal_permute(self, dst, src, plan, dim):
         check(lib().hc_permute(self.h, dst.view(), src.view(), plan.h, ctypes.c_int(dim)))
+
+
+# ---------------------------------------------------------------------------------- runtime
+class PinnedBuffer:
+    """Page-locked host memory viewed as a numpy int64 array."""
+
+    def __init__(self, shape):
+        self.shape = tuple(shape)
+        nbytes = int(np.prod(self.shape)) * 8
+        p = ctypes.c_void_p()
+        check(lib().hc_host_alloc(ctypes.c_size_t(nbytes), ctypes.byref(p)))
+        self.ptr = p.value
+        self.nbytes = nbytes
+        self.array = np.ctypeslib.as_array((ctypes.c_int64 * (nbytes // 8)).from_address(self.ptr)).reshape(self.shape)
+
+    def __del__(self):
+        try:
+            lib().hc_host_free(ctypes.c_void_p(self.ptr))
+        except Exception:
+            pass
+
+
+H2D, D2H, D2D = 0, 1, 2
+
+
+def memcpy_async(be, dst_ptr, src_ptr, nbytes, kind):
+    check(lib().hc_memcpy_async(be.h, ctypes.c_void_p(dst_ptr), ctypes.c_void_p(src_ptr), ctypes.c_size_t(nbytes),
+                                ctypes.c_int(kind)))
+
+
+def memset_async(be, dst_ptr, value, nbytes):
+    check(lib().hc_memset_async(be.h, ctypes.c_void_p(dst_ptr), ctypes.c_int(value), ctypes.c_size_t(nbytes)))
+
+
+class Event:
+    def __init__(self):
+        h = ctypes.c_void_p()
+        check(lib().hc_event_create(ctypes.byref(h)))
+        self.h = h
+
+    def record(self, be):
+        check(lib().hc_event_record(be.h, self.h))
+
+    def elapsed_ms(self, end, timeout_ms=120000.0):
+        ms = ctypes.c_float()
+        check(lib().hc_event_elapsed_ms(self.h, end.h, ctypes.c_double(timeout_ms), ctypes.byref(ms)))
+        return float(ms.value)
+
+    def __del__(self):
+        try:
+            lib().hc_event_destroy(self.h)
+        except Exception:
+            pass
+
+
+def device_memory(be):
+    f, t = ctypes.c_size_t(), ctypes.c_size_t()
+    check(lib().hc_device_memory(be.h, ctypes.byref(f), ctypes.byref(t)))
+    return int(f.value), int(t.value)

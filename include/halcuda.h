@@ -166,6 +166,25 @@ hc_status hc_create_permutation(hc_context ctx, const size_t* inner_shape, const
 hc_status hc_destroy_permutation(hc_context ctx, hc_perm_plan plan);
 hc_status hc_permute(hc_context ctx, hc_view dst, hc_view src, hc_perm_plan plan, hc_data_dim dim);
 
+/* =============================================================================================
+ * Runtime utilities (no trait counterpart): pinned host memory and asynchronous copies for
+ * streaming keys and requests, CUDA events for timing, free-memory queries for admission.
+ * ============================================================================================= */
+typedef enum { HC_H2D = 0, HC_D2H = 1, HC_D2D = 2 } hc_copy_kind;
+typedef struct hc_event_s* hc_event;
+
+hc_status hc_host_alloc(size_t bytes, void** out); /* page-locked host memory */
+hc_status hc_host_free(void* ptr);
+hc_status hc_memcpy_async(hc_context ctx, void* dst, const void* src, size_t bytes, hc_copy_kind kind);
+hc_status hc_memset_async(hc_context ctx, void* dst, int value, size_t bytes);
+hc_status hc_event_create(hc_event* out);
+hc_status hc_event_destroy(hc_event ev);
+hc_status hc_event_record(hc_context ctx, hc_event ev);
+/* Milliseconds between two recorded events; waits for `end` (bounded by `timeout_ms`, then
+ * HC_ERR_TIMEOUT; timeout_ms <= 0 waits without bound). */
+hc_status hc_event_elapsed_ms(hc_event start, hc_event end, double timeout_ms, float* ms);
+hc_status hc_device_memory(hc_context ctx, size_t* free_bytes, size_t* total_bytes);
+
 #ifdef __cplusplus
 }
 #endif
