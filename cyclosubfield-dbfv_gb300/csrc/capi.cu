@@ -37,6 +37,7 @@ hc_status cuda_check(cudaError_t e, const char* what) {
 }
 cudaStream_t stream_of(hc_context ctx) { return ctx->stream; }
 void count_launch(hc_context ctx, uint64_t n) { ctx->launches += n; }
+uint64_t launch_counter(hc_context ctx) { return ctx->launches; }
 int num_sms(hc_context ctx) { return ctx->sms; }
 size_t max_smem_optin(hc_context ctx) { return ctx->smem_optin; }
 

@@ -17,6 +17,12 @@
 
 namespace {
 
+/// Division by an invariant divisor d (1 <= d < 2^32) with a multiply-high and shifts
+/// (Granlund & Montgomery, "Division by invariant integers using multiplication", 1994, fig. 4.1).
+struct FastDiv {
+    uint32_t d, m, s1, s2;
+};
+
 struct DevStage {
     int32_t radix;      // 2 or 3
     int32_t stride;     // element stride of the factor's digit within the axis (suffix product)
@@ -27,8 +33,21 @@ struct DevStage {
     int32_t reduce_before;
     int32_t skip_ok;    // forward only
     int32_t last;       // last stage of the last factor (fwd: fusable reduction, inv: fused len^-1)
-    int32_t pad;
+    int32_t span;       // (stage_len / radix) * stride: butterflies per group, distance of the legs
+    FastDiv div_span;   // butterfly index -> (group, offset in group)
+    FastDiv div_nblocks;  // group -> twiddle block (group mod flen / stage_len)
 };
+
+FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f;
+    f.d = d;
+    uint32_t l = 0;
+    while (l < 32 && ((uint64_t)1 << l) < d) l++;
+    f.m = (uint32_t)((((uint64_t)1 << 32) * ((((uint64_t)1) << l) - d)) / d + 1);
+    f.s1 = l < 1 ? l : 1;
+    f.s2 = l > 1 ? l - 1 : 0;
+    return f;
+}
 
 struct DevPlanHeader {
     int64_t n;
@@ -99,26 +118,45 @@ struct hc_ntt_plan_s {
 // ---------------------------------------------------------------- device kernel
 namespace {
 
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+    uint32_t t = __umulhi(f.m, n);
+    return (t + ((n - t) >> f.s1)) >> f.s2;
+}
+
+/// Butterfly b of a stage -> position of its first leg (element index within the tile's
+/// transform axis) and its twiddle block. Groups of `span` butterflies share a block; the legs of
+/// a butterfly are `span` elements apart.
+__device__ __forceinline__ int leg0(uint32_t bb, const DevStage& st, int* block) {
+    uint32_t g = fdiv(bb, st.div_span);
+    uint32_t off = bb - g * (uint32_t)st.span;
+    uint32_t q = fdiv(g, st.div_nblocks);
+    *block = (int)(g - q * st.div_nblocks.d);
+    return (int)(g * (uint32_t)(st.stage_len * st.stride) + off);
+}
+
 /// One stage of the forward transform over a tile of `len` x V elements in shared memory
-/// (element e, vector v at s[e * V + v]).
-__device__ __forceinline__ void fwd_stage(int64_t* s, int len, int V, const DevStage& st, const int64_t* tw,
+/// (element e, vector v at s[e * V + v]; V = 1 << logv).
+__device__ __forceinline__ void fwd_stage(int64_t* s, int len, int logv, const DevStage& st, const int64_t* tw,
                                           int64_t n, int64_t one_z, int64_t one_u, bool reduce_output) {
-    const int radix = st.radix, S = st.stride, sub = st.stage_len / radix;
-    const int nblocks = st.flen / st.stage_len;
+    const int radix = st.radix;
     const bool fuse = st.last && reduce_output;
-    const int nbf = (len / radix) * V;
+    const int nbf = (len / radix) << logv;
+    const int vmask = (1 << logv) - 1;
+    const int64_t legs = (int64_t)st.span << logv;
     for (int b = threadIdx.x; b < nbf; b += blockDim.x) {
-        int v = b % V, bb = b / V;
-        int suffix = bb % S, rest = bb / S;
-        int jj = rest % sub, rest2 = rest / sub;
-        int block = rest2 % nblocks, prefix = rest2 / nblocks;
-        int e = (prefix * st.flen + block * st.stage_len + jj) * S + suffix;
-        int64_t* x = s + (int64_t)e * V + v;
-        int64_t* y = x + (int64_t)sub * S * V;
+        int block;
+        int e = leg0((uint32_t)(b >> logv), st, &block);
+        int64_t* x = s + ((int64_t)e << logv) + (b & vmask);
+        int64_t* y = x + legs;
         if (radix == 2) {
             int64_t z = tw[2 * (st.tw_off + block)], u = tw[2 * (st.tw_off + block) + 1];
             bool skip = st.skip_ok && z == 1;
-            int64_t a = *x, t = skip ? *y : bmul(z, u, *y, n);
+            int64_t a = *x, yv = *y;
+            if (st.reduce_before) {  // the reference's reduction pass, applied as the operands are read
+                a = bmul(one_z, one_u, a, n);
+                yv = bmul(one_z, one_u, yv, n);
+            }
+            int64_t t = skip ? yv : bmul(z, u, yv, n);
             int64_t o0 = wadd(a, t), o1 = wsub(a, t);
             if (fuse) {
                 o0 = bmul(one_z, one_u, o0, n);
@@ -127,10 +165,15 @@ __device__ __forceinline__ void fwd_stage(int64_t* s, int len, int V, const DevS
             *x = o0;
             *y = o1;
         } else {
-            int64_t* zp = y + (int64_t)sub * S * V;
+            int64_t* zp = y + legs;
             const int64_t* w = tw + 2 * (st.tw_off + 6 * block);
             bool skip = st.skip_ok && w[0] == 1;
             int64_t a = *x, bv = *y, c = *zp;
+            if (st.reduce_before) {
+                a = bmul(one_z, one_u, a, n);
+                bv = bmul(one_z, one_u, bv, n);
+                c = bmul(one_z, one_u, c, n);
+            }
             int64_t t_b = skip ? bv : bmul(w[0], w[1], bv, n);
             int64_t t_bz = bmul(w[2], w[3], bv, n);
             int64_t t_bzz = bmul(w[4], w[5], bv, n);
@@ -150,20 +193,18 @@ __device__ __forceinline__ void fwd_stage(int64_t* s, int len, int V, const DevS
     }
 }
 
-__device__ __forceinline__ void inv_stage(int64_t* s, int len, int V, const DevStage& st, const int64_t* tw,
-                                          int64_t n, int64_t il_z, int64_t il_u) {
-    const int radix = st.radix, S = st.stride, sub = st.stage_len / radix;
-    const int nblocks = st.flen / st.stage_len;
+__device__ __forceinline__ void inv_stage(int64_t* s, int len, int logv, const DevStage& st, const int64_t* tw,
+                                          int64_t n, int64_t il_z, int64_t il_u, int64_t one_z, int64_t one_u) {
+    const int radix = st.radix;
     const bool fused = st.last;
-    const int nbf = (len / radix) * V;
+    const int nbf = (len / radix) << logv;
+    const int vmask = (1 << logv) - 1;
+    const int64_t legs = (int64_t)st.span << logv;
     for (int b = threadIdx.x; b < nbf; b += blockDim.x) {
-        int v = b % V, bb = b / V;
-        int suffix = bb % S, rest = bb / S;
-        int jj = rest % sub, rest2 = rest / sub;
-        int block = rest2 % nblocks, prefix = rest2 / nblocks;
-        int e = (prefix * st.flen + block * st.stage_len + jj) * S + suffix;
-        int64_t* x = s + (int64_t)e * V + v;
-        int64_t* y = x + (int64_t)sub * S * V;
+        int block;
+        int e = leg0((uint32_t)(b >> logv), st, &block);
+        int64_t* x = s + ((int64_t)e << logv) + (b & vmask);
+        int64_t* y = x + legs;
         if (radix == 2) {
             int64_t yz, yu;
             if (fused) {
@@ -175,11 +216,15 @@ __device__ __forceinline__ void inv_stage(int64_t* s, int len, int V, const DevS
             }
             bool skip = !fused && yz == 1;
             int64_t y0 = *x, y1 = *y;
+            if (st.reduce_before) {
+                y0 = bmul(one_z, one_u, y0, n);
+                y1 = bmul(one_z, one_u, y1, n);
+            }
             int64_t sum = wadd(y0, y1), dif = wsub(y0, y1);
             *x = fused ? bmul(yz, yu, sum, n) : sum;
             *y = skip ? dif : bmul(yz, yu, dif, n);
         } else {
-            int64_t* zp = y + (int64_t)sub * S * V;
+            int64_t* zp = y + legs;
             int64_t yz, yu, zz, zu;
             if (fused) {
                 yz = zz = il_z;
@@ -191,6 +236,11 @@ __device__ __forceinline__ void inv_stage(int64_t* s, int len, int V, const DevS
             bool skip = !fused && yz == 1;
             const int64_t* zt = tw + 2 * st.zeta_off;
             int64_t y0 = *x, y1 = *y, y2 = *zp;
+            if (st.reduce_before) {
+                y0 = bmul(one_z, one_u, y0, n);
+                y1 = bmul(one_z, one_u, y1, n);
+                y2 = bmul(one_z, one_u, y2, n);
+            }
             int64_t y1z = bmul(zt[0], zt[1], y1, n), y1zz = bmul(zt[2], zt[3], y1, n);
             int64_t y2z = bmul(zt[0], zt[1], y2, n), y2zz = bmul(zt[2], zt[3], y2, n);
             int64_t s0 = wadd(wadd(y0, y1), y2);
@@ -210,7 +260,8 @@ struct PlanPtrs {
 /// dim 3: tile = line (i, j, k), element e at l = e.  dim 2: tile = (i, j, column block),
 /// element (e, v) at k = e, l = cb * V + v.
 __global__ void __launch_bounds__(256) ntt_tile_kernel(KView t, PlanPtrs plans, int dim, int mode, KView mul,
-                                                       KMods mods, int V, int ntile2, int use_smem) {
+                                                       KMods mods, int logv, int ntile2, int use_smem) {
+    const int V = 1 << logv, vmask = V - 1;
     extern __shared__ int64_t smem[];
     const int len = dim == 3 ? (int)t.n3 : (int)t.n2;
     int64_t tile = blockIdx.x;
@@ -236,7 +287,7 @@ __global__ void __launch_bounds__(256) ntt_tile_kernel(KView t, PlanPtrs plans, 
     int64_t* s = smem;
     if (use_smem) {
         for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-            int e = idx / V, v = idx % V;
+            int e = idx >> logv, v = idx & vmask;
             s[idx] = v < ncol ? g[e * ge + v] : 0;
         }
         __syncthreads();
@@ -248,12 +299,8 @@ __global__ void __launch_bounds__(256) ntt_tile_kernel(KView t, PlanPtrs plans, 
     const int nst = inverse ? P->ninv : P->nfwd;
     for (int si = 0; si < nst; si++) {
         const DevStage& st = inverse ? P->inv[si] : P->fwd[si];
-        if (st.reduce_before) {
-            for (int idx = threadIdx.x; idx < total; idx += blockDim.x) s[idx] = bmul(P->one_z, P->one_u, s[idx], n);
-            __syncthreads();
-        }
-        if (inverse) inv_stage(s, len, V, st, tw, n, P->invlen_z, P->invlen_u);
-        else fwd_stage(s, len, V, st, tw, n, P->one_z, P->one_u, mode == 0);
+        if (inverse) inv_stage(s, len, logv, st, tw, n, P->invlen_z, P->invlen_u, P->one_z, P->one_u);
+        else fwd_stage(s, len, logv, st, tw, n, P->one_z, P->one_u, mode == 0);
         __syncthreads();
     }
     // plans without factors (length 1): the inverse scales by 1^-1, the reduced forward
@@ -266,7 +313,7 @@ __global__ void __launch_bounds__(256) ntt_tile_kernel(KView t, PlanPtrs plans, 
     if (mode == 2) {
         const int64_t mn = mods.n[j], mi = mods.ninv[j];
         for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-            int e = idx / V, v = idx % V;
+            int e = idx >> logv, v = idx & vmask;
             if (v >= ncol) continue;
             int64_t kk = dim == 3 ? k : e, ll = dim == 3 ? e : cb * V + v;
             int64_t m = *kat<int64_t>(mul, i, j, kk, ll);
@@ -276,7 +323,7 @@ __global__ void __launch_bounds__(256) ntt_tile_kernel(KView t, PlanPtrs plans, 
     }
     if (use_smem) {
         for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-            int e = idx / V, v = idx % V;
+            int e = idx >> logv, v = idx & vmask;
             if (v < ncol) g[e * ge + v] = s[idx];
         }
     }
@@ -385,6 +432,9 @@ hc_status build_plan(hc_context ctx, const hc_modulus* m, const size_t* shape, s
             st.tw_off = hp.next_tw();
             for (int64_t v : fw[s]) hp.push(v);
             st.last = last_factor && s + 1 == nst;
+            st.span = (int32_t)((stage_len / radix) * suffix);
+            st.div_span = make_fastdiv((uint32_t)st.span);
+            st.div_nblocks = make_fastdiv((uint32_t)(flen / stage_len));
             const u128 grow = r2 ? (u128)n : 2 * (u128)n;
             if (fbound + grow > I64MAX) {
                 st.reduce_before = 1;
@@ -410,6 +460,9 @@ hc_status build_plan(hc_context ctx, const hc_modulus* m, const size_t* shape, s
             for (int64_t v : iv[si]) hp.push(v);
             st.zeta_off = zeta_off;
             st.last = last_factor && si == 0;
+            st.span = (int32_t)((sl / radix) * suffix);
+            st.div_span = make_fastdiv((uint32_t)st.span);
+            st.div_nblocks = make_fastdiv((uint32_t)(flen / sl));
             if ((u128)radix * ibound > I64MAX) {
                 st.reduce_before = 1;
                 ibound = (u128)n;
@@ -462,12 +515,13 @@ hc_status launch_ntt(hc_context ctx, const KView& t, const hc_ntt_plan* plans, s
         pp.p[j] = reinterpret_cast<const DevPlanHeader*>(plans[j]->dev);
     }
     if (t.n0 == 0 || t.n1 == 0 || t.n2 == 0 || t.n3 == 0) return HC_OK;
-    int V = 1;
+    int V = 1, logv = 0;
     int64_t ntile2 = 1;
     if (dim == 2) {
         // as many dimension-3 columns per tile as fit into 48 KB of shared memory (<= 64)
         V = 64;
         while (V > 1 && (len * V * 8 > 49152 || V / 2 >= t.n3)) V /= 2;
+        while ((1 << logv) < V) logv++;
         ntile2 = (t.n3 + V - 1) / V;
     }
     size_t smem = (size_t)len * V * 8;
@@ -484,8 +538,8 @@ hc_status launch_ntt(hc_context ctx, const KView& t, const hc_ntt_plan* plans, s
     }
     int64_t tiles = dim == 3 ? t.n0 * t.n1 * t.n2 : t.n0 * t.n1 * ntile2;
     if (tiles > 0x7fffffff) return fail(HC_ERR_UNSUPPORTED, "too many NTT tiles in one call");
-    ntt_tile_kernel<<<(unsigned)tiles, 256, smem, stream_of(ctx)>>>(t, pp, dim, mode, mul, mods, V, (int)ntile2,
-                                                                    use_smem);
+    ntt_tile_kernel<<<(unsigned)tiles, 256, smem, stream_of(ctx)>>>(t, pp, dim, mode, mul, mods, logv,
+                                                                    (int)ntile2, use_smem);
     count_launch(ctx);
     return cuda_check(cudaGetLastError(), "ntt kernel launch");
 }

@@ -357,9 +357,16 @@ struct Tensor {
     int64_t shape[4] = {0, 0, 0, 0};
     bool wide = false;
     Tensor() {}
-    Tensor(hc_context c, int64_t a, int64_t b, int64_t cc, int64_t d, bool w = false) : wide(w) {
+    /// `zero`: zero-filled like the reference's allocate; internal temporaries that are fully
+    /// overwritten before being read skip the fill (it would cost one more pass over HBM)
+    Tensor(hc_context c, int64_t a, int64_t b, int64_t cc, int64_t d, bool w = false, bool zero = true) : wide(w) {
         shape[0] = a, shape[1] = b, shape[2] = cc, shape[3] = d;
-        CK(w ? hc_allocate_i128(c, shape, &buf.p) : hc_allocate_i64(c, shape, &buf.p));
+        if (zero) {
+            CK(w ? hc_allocate_i128(c, shape, &buf.p) : hc_allocate_i64(c, shape, &buf.p));
+        } else {
+            size_t bytes = (size_t)(a * b * cc * d) * (w ? 16 : 8);
+            CK(cuda_check(cudaMallocAsync(&buf.p, bytes ? bytes : 16, stream_of(c)), "temporary allocation"));
+        }
         buf.ctx = c;
     }
     hc_view view() const {
@@ -379,6 +386,14 @@ hc_view vrows(hc_view v, int64_t s, int64_t e, bool wide = false) {
     v.shape[0] = e - s;
     return v;
 }
+/// every `step`-th row starting at `s`, `count` rows
+hc_view vstep(hc_view v, int64_t s, int64_t step, int64_t count) {
+    v.ptr = (char*)v.ptr + s * v.strides[0] * 8;
+    v.shape[0] = count;
+    v.strides[0] *= step;
+    return v;
+}
+Tensor temp(hc_context c, int64_t a, int64_t b, int64_t cc, int64_t d) { return Tensor(c, a, b, cc, d, false, false); }
 /// RNS rows [s, e) of dimension 1
 hc_view vbase(hc_view v, int64_t s, int64_t e, bool wide = false) {
     v.ptr = (char*)v.ptr + s * v.strides[1] * (int64_t)esize_of(wide);
@@ -455,6 +470,7 @@ struct hc_ring_s {
     std::map<std::vector<size_t>, std::unique_ptr<PermCache>> pcache;
     std::map<Base, std::unique_ptr<DBuf>> one_cache;
     std::map<std::pair<Base, i128>, std::unique_ptr<Tensor>> scalar_cache;
+    std::map<std::pair<Base, Base>, std::unique_ptr<Tensor>> qinv_cache;
 
     ~hc_ring_s() {
         cudaStreamSynchronize(stream_of(ctx));
@@ -740,14 +756,16 @@ struct hc_ring_s {
         return *gcache.back();
     }
 
+    /// src [B, r] -> dst [B d, r] (row i d + t: digit t of source i)
     void bconv_gadget(const hc_view& dst, const hc_view& src, const Base& b, const Digits& digits) {
-        check_view(src, 1, (int64_t)b.size(), src.shape[2], src.shape[3], "gadget src");
-        check_view(dst, (int64_t)digits.size(), (int64_t)b.size(), src.shape[2], src.shape[3], "gadget dst");
+        check_view(src, src.shape[0], (int64_t)b.size(), src.shape[2], src.shape[3], "gadget src");
+        check_view(dst, src.shape[0] * (int64_t)digits.size(), (int64_t)b.size(), src.shape[2], src.shape[3],
+                   "gadget dst");
         GadgetCache& c = gadget_cache(b, digits);
         KMods km = kmods(b);
         CK(launch_bconv_fused(ctx, kv(src), kv(dst), c.dinv.as<int64_t>(), c.mat.as<int64_t>(), c.dmodp.as<int64_t>(),
                               c.ucol.as<int32_t>(), (int)b.size(), (int)b.size(), (int)digits.size(), c.shift, c.chunk,
-                              km, km, 1));
+                              km, km, src.shape[0]));
     }
 
     // ---------------------------------------------------------------- Galois
@@ -809,6 +827,17 @@ struct hc_ring_s {
         CK(hc_import(ctx, t->view(), v.data(), v.size()));
         auto& ref = *t;
         scalar_cache[key] = std::move(t);
+        return ref;
+    }
+    /// [1, |of|, 1, 1] tensor of mont(smallest_lift(Q(div)^-1 mod p)) for p in `of`
+    /// (inverse_scalar_tensor, src/ring.rs:1165-1177), cached
+    const Tensor& inv_modulus_tensor(const Base& of, const Base& div) {
+        auto key = std::make_pair(of, div);
+        auto it = qinv_cache.find(key);
+        if (it != qinv_cache.end()) return *it->second;
+        auto t = std::make_unique<Tensor>(scalar_tensor_big(of, [&](int64_t p) { return invm(q_mod(div, p), p); }));
+        auto& ref = *t;
+        qinv_cache[key] = std::move(t);
         return ref;
     }
     /// [1, r, 1, 1] tensor holding mont(smallest_lift(residue(p))) (src/ring.rs:890-902)
@@ -1023,24 +1052,27 @@ void gen_ksk(hc_ring R, const Base& base, const hc_view& old_sk, const hc_view& 
 /// rows needing the full double reduction after accumulating `step_bound` (src/ring.rs:365)
 bool needs_full(u128 bound, int64_t minp) { return bound > ((u128)minp << 63); }
 
-/// gadget_decompose (src/bfv.rs:408-426): digits of a period-basis element, in CRT basis
+/// gadget_decompose (src/bfv.rs:408-426): digits of B period-basis elements, in CRT basis
 Tensor gadget_decompose(hc_ring R, const hc_view& c_pb, const Base& base, const Digits& digits) {
-    Tensor parts(R->ctx, (int64_t)digits.size(), (int64_t)base.size(), R->dl(), R->dk());
+    Tensor parts = temp(R->ctx, c_pb.shape[0] * (int64_t)digits.size(), (int64_t)base.size(), R->dl(), R->dk());
     R->bconv_gadget(parts.view(), c_pb, base, digits);
     R->transform(parts.view(), base, false);
     return parts;
 }
 
-/// acc[0..2] = sum_t parts[t] * key_t (+ summands through mont(1)), reduced (fused)
+/// acc[0..2] = sum_t parts[t] * key_t (+ summands through mont(1)), reduced (fused), for B
+/// ciphertexts at once: parts [B d, r] (row i d + t), summand views with one row per ciphertext,
+/// out [2B, r] (rows 2i, 2i + 1).
 void keyswitch(hc_ring R, const hc_view& parts, const hc_view& keys, const Base& base, size_t nd,
                const hc_view* add0, const hc_view* add1, const hc_view& out, const uint32_t* p2 = nullptr,
                const uint32_t* p3 = nullptr) {
-    const int64_t r = (int64_t)base.size();
+    const int64_t r = (int64_t)base.size(), B = out.shape[0] / 2;
     REQUIRE(keys.shape[1] >= r && keys.shape[0] >= 2 * (int64_t)nd, HC_ERR_SHAPE, "key tensor too small");
+    REQUIRE(parts.shape[0] == B * (int64_t)nd, HC_ERR_SHAPE, "gadget digits per ciphertext");
     std::vector<KView> pv, kvv;
     u128 mp = (u128)R->max_p(base), step = 0;
     for (size_t t = 0; t < nd; t++) {
-        pv.push_back(kv(vrows(parts, (int64_t)t, (int64_t)t + 1)));
+        pv.push_back(kv(vstep(parts, (int64_t)t, (int64_t)nd, B)));
         kvv.push_back(kv(vbase(vrows(keys, 2 * (int64_t)t, 2 * (int64_t)t + 2), 0, r)));
         step += mp * mp;
     }
@@ -1070,7 +1102,7 @@ Tensor lift_to_extended(hc_ring R, const hc_view& pb, const hc_view* crt, const 
     }
     Base lifted = base;
     lifted.insert(lifted.end(), ext.begin(), ext.end());
-    Tensor res(R->ctx, count, (int64_t)lifted.size(), R->dl(), R->dk());
+    Tensor res = temp(R->ctx, count, (int64_t)lifted.size(), R->dl(), R->dk());
     hc_view hi = vbase(res.view(), r, (int64_t)lifted.size());
     R->bconv(hi, ext, pb, base);
     if (crt) {
@@ -1088,13 +1120,13 @@ Tensor rescale_to_base(hc_ring R, const hc_view& x, const Base& lifted, size_t b
     Base base(lifted.begin(), lifted.begin() + base_len), ext(lifted.begin() + base_len, lifted.end());
     std::vector<hc_modulus> ml = R->mods(lifted), me = R->mods(ext);
     CK(hc_mul_mont64(R->ctx, x, R->scalar_tensor(lifted, t).view(), ml.data(), ml.size()));
-    Tensor tmp(R->ctx, count, (int64_t)ext.size(), R->dl(), R->dk());
+    Tensor tmp = temp(R->ctx, count, (int64_t)ext.size(), R->dl(), R->dk());
     hc_view xlo = vbase(x, 0, (int64_t)base_len), xhi = vbase(x, (int64_t)base_len, (int64_t)lifted.size());
     R->bconv(tmp.view(), ext, xlo, base);
     CK(hc_sub_i64(R->ctx, xhi, tmp.view()));
-    Tensor qinv = R->scalar_tensor_big(ext, [&](int64_t p) { return invm(R->q_mod(base, p), p); });
+    const Tensor& qinv = R->inv_modulus_tensor(ext, base);
     CK(hc_mul_mont64(R->ctx, xhi, qinv.view(), me.data(), me.size()));
-    Tensor out(R->ctx, count, (int64_t)base_len, R->dl(), R->dk());
+    Tensor out = temp(R->ctx, count, (int64_t)base_len, R->dl(), R->dk());
     R->bconv(out.view(), base, xhi, ext);
     return out;
 }
@@ -1370,24 +1402,24 @@ hc_status hc_bfv_hom_mul(hc_ring R, const int64_t t[2], hc_view ct1, hc_view ct2
         REQUIRE(R && t, HC_ERR_ARG, "null argument");
         Base b = base_of(base, r);
         const int64_t rr = (int64_t)r;
-        REQUIRE(ct1.shape[0] == 2 && ct2.shape[0] == 2, HC_ERR_SHAPE, "ciphertexts must have 2 rows");
-        check_view(ct1, 2, rr, R->dl(), R->dk(), "ct1");
-        check_view(ct2, 2, rr, R->dl(), R->dk(), "ct2");
-        check_view(out, 2, rr, R->dl(), R->dk(), "output");
+        REQUIRE(ct1.shape[0] >= 2 && ct1.shape[0] % 2 == 0, HC_ERR_SHAPE, "ciphertexts must have 2 rows each");
+        const int64_t B = ct1.shape[0] / 2;  // independent ciphertext pairs, stacked along dimension 0
+        check_view(ct1, 2 * B, rr, R->dl(), R->dk(), "ct1");
+        check_view(ct2, 2 * B, rr, R->dl(), R->dk(), "ct2");
+        check_view(out, 2 * B, rr, R->dl(), R->dk(), "output");
         // lift both operands (src/bfv.rs:762-768)
         auto lift = [&](const hc_view& ct) {
-            Tensor pb(R->ctx, 2, rr, R->dl(), R->dk());
+            Tensor pb = temp(R->ctx, 2 * B, rr, R->dl(), R->dk());
             CK(hc_assign(R->ctx, pb.view(), ct));
             R->transform(pb.view(), b, true);
             return lift_to_extended(R, pb.view(), &ct, b);
         };
         Tensor l = lift(ct1), rt = lift(ct2);
-        Base ext;
-        for (int64_t i = rr; i < l.shape[1]; i++) ext.push_back(R->initial_len + (size_t)(i - rr));
         Base lifted = b;
-        lifted.insert(lifted.end(), ext.begin(), ext.end());
-        // tensor product + reduce_wide (src/bfv.rs:667-683, :769-771)
-        Tensor prod(R->ctx, 3, (int64_t)lifted.size(), R->dl(), R->dk());
+        for (int64_t i = rr; i < l.shape[1]; i++) lifted.push_back(R->initial_len + (size_t)(i - rr));
+        // tensor product + reduce_wide (src/bfv.rs:667-683, :769-771); rows 2i, 2i + 1 hold
+        // (c0, c1) of product i and row 2B + i its c2, so that both groups are contiguous
+        Tensor prod = temp(R->ctx, 3 * B, (int64_t)lifted.size(), R->dl(), R->dk());
         {
             u128 mp = (u128)R->max_p(lifted), s1 = mp * mp;
             int64_t mn = R->min_p(lifted);
@@ -1399,16 +1431,16 @@ hc_status hc_bfv_hom_mul(hc_ring R, const int64_t t[2], hc_view ct1, hc_view ct2
         // relinearisation (src/bfv.rs:699-741)
         Digits dg = clip(digits_of(digits, d), r);
         REQUIRE(rk.shape[0] >= 2 * (int64_t)dg.size() && rk.shape[1] >= rr, HC_ERR_SHAPE, "relinearisation key shape");
-        Tensor parts = gadget_decompose(R, vrows(resc.view(), 2, 3), b, dg);
+        Tensor parts = gadget_decompose(R, vrows(resc.view(), 2 * B, 3 * B), b, dg);
+        hc_view c01 = vrows(resc.view(), 0, 2 * B);
         if (!period_output) {
-            hc_view c01 = vrows(resc.view(), 0, 2);
             R->transform(c01, b, false);
-            hc_view a0 = vrows(c01, 0, 1), a1 = vrows(c01, 1, 2);
+            hc_view a0 = vstep(c01, 0, 2, B), a1 = vstep(c01, 1, 2, B);
             keyswitch(R, parts.view(), rk, b, dg.size(), &a0, &a1, out);
         } else {
             keyswitch(R, parts.view(), rk, b, dg.size(), nullptr, nullptr, out);
             R->transform(out, b, true);
-            CK(hc_add_i64(R->ctx, out, vrows(resc.view(), 0, 2)));
+            CK(hc_add_i64(R->ctx, out, c01));
         }
     });
 }

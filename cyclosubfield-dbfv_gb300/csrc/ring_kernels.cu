@@ -89,13 +89,14 @@ __global__ void __launch_bounds__(256) galois_kernel(KView d, KView s, const uin
 }
 
 struct KsArgs {
-    KView parts[HC_MAX_TERMS];  // [1, r, dl, dk] digit t (dimension 0 broadcast)
+    KView parts[HC_MAX_TERMS];  // [B, r, dl, dk] digit t of each of the B ciphertexts (row stride: s0)
     KView keys[HC_MAX_TERMS];   // [2, r, dl, dk] key t restricted to the ciphertext base
     int nterms;
+    int64_t batch;              // B; output rows 2i, 2i+1 and summand rows i belong to ciphertext i
     KView add0, add1;  // optional (has_add*) CRT-basis summands of rows 0 / 1, multiplied by mont(1)
     int has_add0, has_add1;
     int full0, full1;  // rows needing the full double reduction
-    KView dst;         // [2, r, dl, dk]
+    KView dst;         // [2B, r, dl, dk]
     // optional Galois permutation applied to parts and summands (apply_galois fused into the
     // read, src/bfv.rs:819-820); null means identity
     const uint32_t* p2;
@@ -114,41 +115,46 @@ __global__ void __launch_bounds__(256) keyswitch_kernel(KsArgs a, KMods m, const
         int64_t line = tile / chunks;  // (j, k)
         int64_t l = (tile - line * chunks) * blockDim.x + threadIdx.x;
         if (l >= a.dst.n3) continue;
-        int64_t k = line % a.dst.n2, j = line / a.dst.n2;
+        int64_t k = line % a.dst.n2, r = line / a.dst.n2;
+        int64_t j = r % a.dst.n1, i = r / a.dst.n1;
         const int64_t sk = a.p2 ? (int64_t)a.p2[k] : k, sl = a.p3 ? (int64_t)a.p3[l] : l;
         i128 acc0 = 0, acc1 = 0;
         for (int t = 0; t < a.nterms; t++) {
-            int64_t x = *kat<int64_t>(a.parts[t], 0, j, sk, sl);
+            int64_t x = *kat<int64_t>(a.parts[t], i, j, sk, sl);
             int64_t k0 = *kat<int64_t>(a.keys[t], 0, j, k, l);
             int64_t k1 = *kat<int64_t>(a.keys[t], 1, j, k, l);
             acc0 = (i128)((u128)acc0 + (u128)((i128)x * (i128)k0));
             acc1 = (i128)((u128)acc1 + (u128)((i128)x * (i128)k1));
         }
         const int64_t o = one[j];
-        if (a.has_add0) acc0 = (i128)((u128)acc0 + (u128)((i128)*kat<int64_t>(a.add0, 0, j, sk, sl) * (i128)o));
-        if (a.has_add1) acc1 = (i128)((u128)acc1 + (u128)((i128)*kat<int64_t>(a.add1, 0, j, sk, sl) * (i128)o));
-        *kat<int64_t>(a.dst, 0, j, k, l) = finish_wide(acc0, a.full0, m, (int)j);
-        *kat<int64_t>(a.dst, 1, j, k, l) = finish_wide(acc1, a.full1, m, (int)j);
+        if (a.has_add0) acc0 = (i128)((u128)acc0 + (u128)((i128)*kat<int64_t>(a.add0, i, j, sk, sl) * (i128)o));
+        if (a.has_add1) acc1 = (i128)((u128)acc1 + (u128)((i128)*kat<int64_t>(a.add1, i, j, sk, sl) * (i128)o));
+        *kat<int64_t>(a.dst, 2 * i, j, k, l) = finish_wide(acc0, a.full0, m, (int)j);
+        *kat<int64_t>(a.dst, 2 * i + 1, j, k, l) = finish_wide(acc1, a.full1, m, (int)j);
     }
 }
 
-/// (l0 r0, l0 r1 + l1 r0, l1 r1) of two 2-row ciphertext tensors, reduced per row.
+/// (l0 r0, l0 r1 + l1 r0, l1 r1) of B pairs of 2-row ciphertext tensors ([2B, ...] each),
+/// reduced per row into [3B, ...]: rows 2i and 2i + 1 receive the first two components of pair i,
+/// row 2B + i the third.
 __global__ void __launch_bounds__(256) tensor_kernel(KView d, KView lhs, KView rhs, KMods m, int full0, int full1,
                                                      int full2, int64_t lines, int chunks) {
     const int64_t tiles = lines * chunks;
     for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        int64_t line = tile / chunks;  // (j, k)
+        int64_t line = tile / chunks;  // (i, j, k)
         int64_t l = (tile - line * chunks) * blockDim.x + threadIdx.x;
         if (l >= d.n3) continue;
-        int64_t k = line % d.n2, j = line / d.n2;
-        int64_t l0 = *kat<int64_t>(lhs, 0, j, k, l), l1 = *kat<int64_t>(lhs, 1, j, k, l);
-        int64_t r0 = *kat<int64_t>(rhs, 0, j, k, l), r1 = *kat<int64_t>(rhs, 1, j, k, l);
+        int64_t k = line % d.n2, r = line / d.n2;
+        int64_t j = r % d.n1, i = r / d.n1;
+        int64_t l0 = *kat<int64_t>(lhs, 2 * i, j, k, l), l1 = *kat<int64_t>(lhs, 2 * i + 1, j, k, l);
+        int64_t r0 = *kat<int64_t>(rhs, 2 * i, j, k, l), r1 = *kat<int64_t>(rhs, 2 * i + 1, j, k, l);
         i128 a0 = (i128)l0 * (i128)r0;
         i128 a1 = (i128)((u128)((i128)l0 * (i128)r1) + (u128)((i128)l1 * (i128)r0));
         i128 a2 = (i128)l1 * (i128)r1;
-        *kat<int64_t>(d, 0, j, k, l) = finish_wide(a0, full0, m, (int)j);
-        *kat<int64_t>(d, 1, j, k, l) = finish_wide(a1, full1, m, (int)j);
-        *kat<int64_t>(d, 2, j, k, l) = finish_wide(a2, full2, m, (int)j);
+        const int64_t B = d.n0 / 3;
+        *kat<int64_t>(d, 2 * i, j, k, l) = finish_wide(a0, full0, m, (int)j);
+        *kat<int64_t>(d, 2 * i + 1, j, k, l) = finish_wide(a1, full1, m, (int)j);
+        *kat<int64_t>(d, 2 * B + i, j, k, l) = finish_wide(a2, full2, m, (int)j);
     }
 }
 
@@ -211,7 +217,8 @@ hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys
     a.full0 = full0, a.full1 = full1;
     a.dst = dst;
     a.p2 = p2, a.p3 = p3;
-    int64_t lines = dst.n1 * dst.n2;
+    a.batch = dst.n0 / 2;
+    int64_t lines = a.batch * dst.n1 * dst.n2;
     if (lines == 0 || dst.n3 == 0) return HC_OK;
     int chunks;
     unsigned blocks;
@@ -223,7 +230,7 @@ hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys
 
 hc_status launch_tensor(hc_context ctx, const KView& d, const KView& lhs, const KView& rhs, const KMods& m, int f0,
                         int f1, int f2) {
-    int64_t lines = d.n1 * d.n2;
+    int64_t lines = (d.n0 / 3) * d.n1 * d.n2;
     if (lines == 0 || d.n3 == 0) return HC_OK;
     int chunks;
     unsigned blocks;

@@ -9,6 +9,16 @@ struct hc_event_s {
     cudaEvent_t ev;
 };
 
+struct hc_graph_s {
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    uint64_t launches;  // kernels recorded during capture, credited on every replay
+};
+
+namespace hc {
+uint64_t launch_counter(hc_context ctx);
+}
+
 using namespace hc;
 
 extern "C" {
@@ -73,6 +83,49 @@ hc_status hc_event_elapsed_ms(hc_event start, hc_event end, double timeout_ms, f
         std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
     return cuda_check(cudaEventElapsedTime(ms, start->ev, end->ev), "event elapsed time");
+}
+
+namespace {
+thread_local uint64_t g_capture_start = 0;
+}
+
+hc_status hc_graph_begin_capture(hc_context ctx) {
+    if (!ctx) return fail(HC_ERR_ARG, "null context");
+    g_capture_start = launch_counter(ctx);
+    return cuda_check(cudaStreamBeginCapture(stream_of(ctx), cudaStreamCaptureModeRelaxed), "begin capture");
+}
+
+hc_status hc_graph_end_capture(hc_context ctx, hc_graph* out) {
+    if (!ctx || !out) return fail(HC_ERR_ARG, "null argument");
+    cudaGraph_t g = nullptr;
+    hc_status st = cuda_check(cudaStreamEndCapture(stream_of(ctx), &g), "end capture");
+    if (st) return st;
+    auto* h = new hc_graph_s();
+    h->graph = g;
+    h->launches = launch_counter(ctx) - g_capture_start;
+    count_launch(ctx, 0);
+    st = cuda_check(cudaGraphInstantiate(&h->exec, g, 0), "graph instantiation");
+    if (st) {
+        cudaGraphDestroy(g);
+        delete h;
+        return st;
+    }
+    *out = h;
+    return HC_OK;
+}
+
+hc_status hc_graph_launch(hc_context ctx, hc_graph graph) {
+    if (!ctx || !graph) return fail(HC_ERR_ARG, "null argument");
+    count_launch(ctx, graph->launches);
+    return cuda_check(cudaGraphLaunch(graph->exec, stream_of(ctx)), "graph launch");
+}
+
+hc_status hc_graph_destroy(hc_graph graph) {
+    if (!graph) return HC_OK;
+    cudaGraphExecDestroy(graph->exec);
+    cudaGraphDestroy(graph->graph);
+    delete graph;
+    return HC_OK;
 }
 
 hc_status hc_device_memory(hc_context ctx, size_t* free_bytes, size_t* total_bytes) {

@@ -416,3 +416,27 @@ def device_memory(be):
     f, t = ctypes.c_size_t(), ctypes.c_size_t()
     check(lib().hc_device_memory(be.h, ctypes.byref(f), ctypes.byref(t)))
     return int(f.value), int(t.value)
+
+
+class Graph:
+    """A captured sequence of calls (hc_graph_*), replayed with launch()."""
+
+    def __init__(self, be, fn):
+        self.be = be
+        check(lib().hc_graph_begin_capture(be.h))
+        try:
+            fn()
+        finally:
+            h = ctypes.c_void_p()
+            rc = lib().hc_graph_end_capture(be.h, ctypes.byref(h))
+        check(rc)
+        self.h = h
+
+    def launch(self):
+        check(lib().hc_graph_launch(self.be.h, self.h))
+
+    def __del__(self):
+        try:
+            lib().hc_graph_destroy(self.h)
+        except Exception:
+            pass

@@ -220,7 +220,7 @@ class RingContext:
         return out
 
     def hom_mul(self, t, ct1, ct2, base, rk, digits, period_output=False, out=None):
-        out = out if out is not None else self.allocate(2, len(base))
+        out = out if out is not None else self.allocate(ct1.shape[0], len(base))
         dg, nd = _digits(digits)
         check(lib().hc_bfv_hom_mul(self.h, _i128(t), ct1.view(), ct2.view(), _sz(base), ctypes.c_size_t(len(base)),
                                    rk.view(), dg, nd, ctypes.c_int(int(period_output)), out.view()))

@@ -185,6 +185,17 @@ hc_status hc_event_record(hc_context ctx, hc_event ev);
 hc_status hc_event_elapsed_ms(hc_event start, hc_event end, double timeout_ms, float* ms);
 hc_status hc_device_memory(hc_context ctx, size_t* free_bytes, size_t* total_bytes);
 
+/* CUDA-graph capture of a sequence of calls on the context's stream (for launch-bound loops):
+ * every call between begin and end is recorded, not executed; hc_graph_launch replays it. The
+ * recorded calls must not synchronise with the host (hc_import / hc_export and first-use
+ * set-up of ring caches do; run one uncaptured call first). Tensors allocated inside the capture
+ * are graph-owned and released when the replay finishes. */
+typedef struct hc_graph_s* hc_graph;
+hc_status hc_graph_begin_capture(hc_context ctx);
+hc_status hc_graph_end_capture(hc_context ctx, hc_graph* out);
+hc_status hc_graph_launch(hc_context ctx, hc_graph graph);
+hc_status hc_graph_destroy(hc_graph graph);
+
 #ifdef __cplusplus
 }
 #endif
