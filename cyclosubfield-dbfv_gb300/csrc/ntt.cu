@@ -49,15 +49,34 @@ FastDiv make_fastdiv(uint32_t d) {
     return f;
 }
 
+/// A pass of the kernel: either one stage through shared memory (kind 0, any radix), or k <= 3
+/// consecutive radix-2 stages of one factor executed in registers (kind 1): each thread loads a
+/// group of 2^k elements `span` apart, applies the k stages' butterflies to it in the
+/// reference's order, and stores it back.
+struct DevPass {
+    int32_t kind;
+    int32_t k;
+    int32_t first;  // index of the pass's first stage in the (forward or inverse) program
+    int32_t span;   // distance of consecutive group elements
+    int32_t glen;   // extent of the block a group lies in (stage_len * stride)
+    int32_t nb;     // blocks of that stage within the factor (twiddle block of a group)
+    FastDiv div_span;
+    FastDiv div_nb;
+};
+
 struct DevPlanHeader {
     int64_t n;
     int32_t len;
     int32_t nfwd;
     int32_t ninv;
     int32_t ntw;
+    int32_t nfpass;
+    int32_t nipass;
     int64_t one_z, one_u, invlen_z, invlen_u;
     DevStage fwd[HC_MAX_STAGES];
     DevStage inv[HC_MAX_STAGES];
+    DevPass fpass[HC_MAX_STAGES];
+    DevPass ipass[HC_MAX_STAGES];
     // followed by the twiddle table: ntw pairs (z, u)
 };
 
@@ -123,6 +142,12 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
     return (t + ((n - t) >> f.s1)) >> f.s2;
 }
 
+/// Shared-memory slot of tile element i: for single lines (one vector) the low four index bits
+/// are XOR-ed with the next four, so that groups of consecutive elements read by consecutive
+/// threads fall into distinct banks; blocks of 16 stay in place, so the map is a permutation
+/// whenever the line length is a multiple of 16.
+__device__ __forceinline__ int sw(int i, bool on) { return on ? (i ^ ((i >> 4) & 15)) : i; }
+
 /// Butterfly b of a stage -> position of its first leg (element index within the tile's
 /// transform axis) and its twiddle block. Groups of `span` butterflies share a block; the legs of
 /// a butterfly are `span` elements apart.
@@ -134,24 +159,29 @@ __device__ __forceinline__ int leg0(uint32_t bb, const DevStage& st, int* block)
     return (int)(g * (uint32_t)(st.stage_len * st.stride) + off);
 }
 
-/// One stage of the forward transform over a tile of `len` x V elements in shared memory
-/// (element e, vector v at s[e * V + v]; V = 1 << logv).
-__device__ __forceinline__ void fwd_stage(int64_t* s, int len, int logv, const DevStage& st, const int64_t* tw,
-                                          int64_t n, int64_t one_z, int64_t one_u, bool reduce_output) {
+struct Tile {
+    int64_t* s;
+    int len, logv;
+    bool swz;
+    __device__ __forceinline__ int64_t& at(int e, int v) const { return s[sw((e << logv) + v, swz)]; }
+};
+
+/// One forward stage (radix 2 or 3) over the tile in shared memory.
+__device__ __forceinline__ void fwd_stage(const Tile& T, const DevStage& st, const int64_t* tw, int64_t n,
+                                          int64_t one_z, int64_t one_u, bool reduce_output) {
     const int radix = st.radix;
     const bool fuse = st.last && reduce_output;
-    const int nbf = (len / radix) << logv;
-    const int vmask = (1 << logv) - 1;
-    const int64_t legs = (int64_t)st.span << logv;
+    const int nbf = (T.len / radix) << T.logv;
+    const int vmask = (1 << T.logv) - 1;
     for (int b = threadIdx.x; b < nbf; b += blockDim.x) {
         int block;
-        int e = leg0((uint32_t)(b >> logv), st, &block);
-        int64_t* x = s + ((int64_t)e << logv) + (b & vmask);
-        int64_t* y = x + legs;
+        const int e = leg0((uint32_t)(b >> T.logv), st, &block), v = b & vmask;
+        int64_t& x = T.at(e, v);
+        int64_t& y = T.at(e + st.span, v);
         if (radix == 2) {
             int64_t z = tw[2 * (st.tw_off + block)], u = tw[2 * (st.tw_off + block) + 1];
             bool skip = st.skip_ok && z == 1;
-            int64_t a = *x, yv = *y;
+            int64_t a = x, yv = y;
             if (st.reduce_before) {  // the reference's reduction pass, applied as the operands are read
                 a = bmul(one_z, one_u, a, n);
                 yv = bmul(one_z, one_u, yv, n);
@@ -162,13 +192,13 @@ __device__ __forceinline__ void fwd_stage(int64_t* s, int len, int logv, const D
                 o0 = bmul(one_z, one_u, o0, n);
                 o1 = bmul(one_z, one_u, o1, n);
             }
-            *x = o0;
-            *y = o1;
+            x = o0;
+            y = o1;
         } else {
-            int64_t* zp = y + legs;
+            int64_t& zr = T.at(e + 2 * st.span, v);
             const int64_t* w = tw + 2 * (st.tw_off + 6 * block);
             bool skip = st.skip_ok && w[0] == 1;
-            int64_t a = *x, bv = *y, c = *zp;
+            int64_t a = x, bv = y, c = zr;
             if (st.reduce_before) {
                 a = bmul(one_z, one_u, a, n);
                 bv = bmul(one_z, one_u, bv, n);
@@ -186,25 +216,25 @@ __device__ __forceinline__ void fwd_stage(int64_t* s, int len, int logv, const D
                 o1 = bmul(one_z, one_u, o1, n);
                 o2 = bmul(one_z, one_u, o2, n);
             }
-            *x = o0;
-            *y = o1;
-            *zp = o2;
+            x = o0;
+            y = o1;
+            zr = o2;
         }
     }
 }
 
-__device__ __forceinline__ void inv_stage(int64_t* s, int len, int logv, const DevStage& st, const int64_t* tw,
-                                          int64_t n, int64_t il_z, int64_t il_u, int64_t one_z, int64_t one_u) {
+/// One inverse stage (radix 2 or 3) over the tile in shared memory.
+__device__ __forceinline__ void inv_stage(const Tile& T, const DevStage& st, const int64_t* tw, int64_t n,
+                                          int64_t il_z, int64_t il_u, int64_t one_z, int64_t one_u) {
     const int radix = st.radix;
     const bool fused = st.last;
-    const int nbf = (len / radix) << logv;
-    const int vmask = (1 << logv) - 1;
-    const int64_t legs = (int64_t)st.span << logv;
+    const int nbf = (T.len / radix) << T.logv;
+    const int vmask = (1 << T.logv) - 1;
     for (int b = threadIdx.x; b < nbf; b += blockDim.x) {
         int block;
-        int e = leg0((uint32_t)(b >> logv), st, &block);
-        int64_t* x = s + ((int64_t)e << logv) + (b & vmask);
-        int64_t* y = x + legs;
+        const int e = leg0((uint32_t)(b >> T.logv), st, &block), v = b & vmask;
+        int64_t& x = T.at(e, v);
+        int64_t& y = T.at(e + st.span, v);
         if (radix == 2) {
             int64_t yz, yu;
             if (fused) {
@@ -215,16 +245,16 @@ __device__ __forceinline__ void inv_stage(int64_t* s, int len, int logv, const D
                 yu = tw[2 * (st.tw_off + block) + 1];
             }
             bool skip = !fused && yz == 1;
-            int64_t y0 = *x, y1 = *y;
+            int64_t y0 = x, y1 = y;
             if (st.reduce_before) {
                 y0 = bmul(one_z, one_u, y0, n);
                 y1 = bmul(one_z, one_u, y1, n);
             }
             int64_t sum = wadd(y0, y1), dif = wsub(y0, y1);
-            *x = fused ? bmul(yz, yu, sum, n) : sum;
-            *y = skip ? dif : bmul(yz, yu, dif, n);
+            x = fused ? bmul(yz, yu, sum, n) : sum;
+            y = skip ? dif : bmul(yz, yu, dif, n);
         } else {
-            int64_t* zp = y + legs;
+            int64_t& zr = T.at(e + 2 * st.span, v);
             int64_t yz, yu, zz, zu;
             if (fused) {
                 yz = zz = il_z;
@@ -235,7 +265,7 @@ __device__ __forceinline__ void inv_stage(int64_t* s, int len, int logv, const D
             }
             bool skip = !fused && yz == 1;
             const int64_t* zt = tw + 2 * st.zeta_off;
-            int64_t y0 = *x, y1 = *y, y2 = *zp;
+            int64_t y0 = x, y1 = y, y2 = zr;
             if (st.reduce_before) {
                 y0 = bmul(one_z, one_u, y0, n);
                 y1 = bmul(one_z, one_u, y1, n);
@@ -245,10 +275,112 @@ __device__ __forceinline__ void inv_stage(int64_t* s, int len, int logv, const D
             int64_t y2z = bmul(zt[0], zt[1], y2, n), y2zz = bmul(zt[2], zt[3], y2, n);
             int64_t s0 = wadd(wadd(y0, y1), y2);
             int64_t sy = wadd(wadd(y0, y1zz), y2z), sz = wadd(wadd(y0, y1z), y2zz);
-            *x = fused ? bmul(yz, yu, s0, n) : s0;
-            *y = skip ? sy : bmul(yz, yu, sy, n);
-            *zp = skip ? sz : bmul(zz, zu, sz, n);
+            x = fused ? bmul(yz, yu, s0, n) : s0;
+            y = skip ? sy : bmul(yz, yu, sy, n);
+            zr = skip ? sz : bmul(zz, zu, sz, n);
         }
+    }
+}
+
+/// K consecutive forward radix-2 stages of one factor in registers. Group element m lies at
+/// g * glen + o + m * span; at the q-th stage of the pass the butterflies pair m with
+/// m + 2^(K-1-q) and use the twiddle of block block0 * 2^q + (m >> (K-q)).
+template <int K>
+__device__ __forceinline__ void fwd_pass_r2(const Tile& T, const DevPass& ps, const DevStage* sts, const int64_t* tw,
+                                            int64_t n, int64_t one_z, int64_t one_u, bool reduce_output) {
+    constexpr int M = 1 << K;
+    const int ng = (T.len >> K) << T.logv;
+    const int vmask = (1 << T.logv) - 1;
+    for (int gi = threadIdx.x; gi < ng; gi += blockDim.x) {
+        const int v = gi & vmask;
+        const uint32_t gg = (uint32_t)(gi >> T.logv);
+        const uint32_t g = fdiv(gg, ps.div_span);
+        const int o = (int)(gg - g * (uint32_t)ps.span);
+        const int block0 = (int)(g - fdiv(g, ps.div_nb) * (uint32_t)ps.nb);
+        const int base = (int)g * ps.glen + o;
+        int64_t x[M];
+#pragma unroll
+        for (int m = 0; m < M; m++) x[m] = T.at(base + m * ps.span, v);
+#pragma unroll
+        for (int q = 0; q < K; q++) {
+            const DevStage& st = sts[ps.first + q];
+            if (st.reduce_before) {
+#pragma unroll
+                for (int m = 0; m < M; m++) x[m] = bmul(one_z, one_u, x[m], n);
+            }
+            const bool fuse = st.last && reduce_output;
+            const int half = M >> (q + 1);
+#pragma unroll
+            for (int j = 0; j < M / 2; j++) {
+                const int m1 = ((j / half) * 2 * half) + (j % half), m2 = m1 + half;
+                const int tb = block0 * (1 << q) + (m1 >> (K - q));
+                const int64_t z = tw[2 * (st.tw_off + tb)], u = tw[2 * (st.tw_off + tb) + 1];
+                const bool skip = st.skip_ok && z == 1;
+                const int64_t a = x[m1];
+                const int64_t t = skip ? x[m2] : bmul(z, u, x[m2], n);
+                int64_t o0 = wadd(a, t), o1 = wsub(a, t);
+                if (fuse) {
+                    o0 = bmul(one_z, one_u, o0, n);
+                    o1 = bmul(one_z, one_u, o1, n);
+                }
+                x[m1] = o0;
+                x[m2] = o1;
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < M; m++) T.at(base + m * ps.span, v) = x[m];
+    }
+}
+
+/// K consecutive inverse radix-2 stages (stage lengths growing) in registers: at the q-th stage
+/// of the pass the butterflies pair m with m + 2^q and use the twiddle of block
+/// blockK * 2^(K-1-q) + (m >> (q+1)), blockK being the group's block at the pass's last stage.
+template <int K>
+__device__ __forceinline__ void inv_pass_r2(const Tile& T, const DevPass& ps, const DevStage* sts, const int64_t* tw,
+                                            int64_t n, int64_t il_z, int64_t il_u, int64_t one_z, int64_t one_u) {
+    constexpr int M = 1 << K;
+    const int ng = (T.len >> K) << T.logv;
+    const int vmask = (1 << T.logv) - 1;
+    for (int gi = threadIdx.x; gi < ng; gi += blockDim.x) {
+        const int v = gi & vmask;
+        const uint32_t gg = (uint32_t)(gi >> T.logv);
+        const uint32_t g = fdiv(gg, ps.div_span);
+        const int o = (int)(gg - g * (uint32_t)ps.span);
+        const int blockK = (int)(g - fdiv(g, ps.div_nb) * (uint32_t)ps.nb);
+        const int base = (int)g * ps.glen + o;
+        int64_t x[M];
+#pragma unroll
+        for (int m = 0; m < M; m++) x[m] = T.at(base + m * ps.span, v);
+#pragma unroll
+        for (int q = 0; q < K; q++) {
+            const DevStage& st = sts[ps.first + q];
+            if (st.reduce_before) {
+#pragma unroll
+                for (int m = 0; m < M; m++) x[m] = bmul(one_z, one_u, x[m], n);
+            }
+            const bool fused = st.last;
+            const int dist = 1 << q;
+#pragma unroll
+            for (int j = 0; j < M / 2; j++) {
+                const int m1 = ((j >> q) << (q + 1)) | (j & (dist - 1)), m2 = m1 + dist;
+                const int tb = blockK * (1 << (K - 1 - q)) + (m1 >> (q + 1));
+                int64_t yz, yu;
+                if (fused) {
+                    yz = il_z;
+                    yu = il_u;
+                } else {
+                    yz = tw[2 * (st.tw_off + tb)];
+                    yu = tw[2 * (st.tw_off + tb) + 1];
+                }
+                const bool skip = !fused && yz == 1;
+                const int64_t y0 = x[m1], y1 = x[m2];
+                const int64_t sum = wadd(y0, y1), dif = wsub(y0, y1);
+                x[m1] = fused ? bmul(yz, yu, sum, n) : sum;
+                x[m2] = skip ? dif : bmul(yz, yu, dif, n);
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < M; m++) T.at(base + m * ps.span, v) = x[m];
     }
 }
 
@@ -261,8 +393,8 @@ struct PlanPtrs {
 /// element (e, v) at k = e, l = cb * V + v.
 __global__ void __launch_bounds__(256) ntt_tile_kernel(KView t, PlanPtrs plans, int dim, int mode, KView mul,
                                                        KMods mods, int logv, int ntile2, int use_smem) {
-    const int V = 1 << logv, vmask = V - 1;
     extern __shared__ int64_t smem[];
+    const int V = 1 << logv, vmask = V - 1;
     const int len = dim == 3 ? (int)t.n3 : (int)t.n2;
     int64_t tile = blockIdx.x;
     int64_t i, j, k = 0, cb = 0;
@@ -284,30 +416,42 @@ __global__ void __launch_bounds__(256) ntt_tile_kernel(KView t, PlanPtrs plans, 
     const int64_t ge = dim == 3 ? 1 : t.s2;  // global stride of element e
     const int64_t ncol = dim == 3 ? 1 : t.n3 - cb * V;
     const int total = len * V;
-    int64_t* s = smem;
+    // without shared memory (lines too long for it) the tile is worked on in place in global
+    // memory; this is only valid for dim 3 (V == 1, unit element stride)
+    Tile T{use_smem ? smem : g, len, logv, use_smem && logv == 0 && (len & 15) == 0};
     if (use_smem) {
         for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
             int e = idx >> logv, v = idx & vmask;
-            s[idx] = v < ncol ? g[e * ge + v] : 0;
+            T.at(e, v) = v < ncol ? g[e * ge + v] : 0;
         }
         __syncthreads();
     }
-    // without shared memory (lines too long for it) the tile is worked on in place in global
-    // memory; this is only valid for dim 3 (V == 1, unit element stride)
-    if (!use_smem) s = g;
     const bool inverse = mode == 1;
-    const int nst = inverse ? P->ninv : P->nfwd;
-    for (int si = 0; si < nst; si++) {
-        const DevStage& st = inverse ? P->inv[si] : P->fwd[si];
-        if (inverse) inv_stage(s, len, logv, st, tw, n, P->invlen_z, P->invlen_u, P->one_z, P->one_u);
-        else fwd_stage(s, len, logv, st, tw, n, P->one_z, P->one_u, mode == 0);
+    const int npass = inverse ? P->nipass : P->nfpass;
+    for (int pi = 0; pi < npass; pi++) {
+        const DevPass& ps = inverse ? P->ipass[pi] : P->fpass[pi];
+        if (ps.kind == 0) {
+            if (inverse) inv_stage(T, P->inv[ps.first], tw, n, P->invlen_z, P->invlen_u, P->one_z, P->one_u);
+            else fwd_stage(T, P->fwd[ps.first], tw, n, P->one_z, P->one_u, mode == 0);
+        } else if (inverse) {
+            if (ps.k == 3) inv_pass_r2<3>(T, ps, P->inv, tw, n, P->invlen_z, P->invlen_u, P->one_z, P->one_u);
+            else if (ps.k == 2) inv_pass_r2<2>(T, ps, P->inv, tw, n, P->invlen_z, P->invlen_u, P->one_z, P->one_u);
+            else inv_pass_r2<1>(T, ps, P->inv, tw, n, P->invlen_z, P->invlen_u, P->one_z, P->one_u);
+        } else {
+            if (ps.k == 3) fwd_pass_r2<3>(T, ps, P->fwd, tw, n, P->one_z, P->one_u, mode == 0);
+            else if (ps.k == 2) fwd_pass_r2<2>(T, ps, P->fwd, tw, n, P->one_z, P->one_u, mode == 0);
+            else fwd_pass_r2<1>(T, ps, P->fwd, tw, n, P->one_z, P->one_u, mode == 0);
+        }
         __syncthreads();
     }
     // plans without factors (length 1): the inverse scales by 1^-1, the reduced forward
     // reduces; an unreduced forward leaves the data unchanged
-    if (nst == 0 && (mode == 0 || mode == 1)) {
+    if (npass == 0 && (mode == 0 || mode == 1)) {
         int64_t fz = inverse ? P->invlen_z : P->one_z, fu = inverse ? P->invlen_u : P->one_u;
-        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) s[idx] = bmul(fz, fu, s[idx], n);
+        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+            int e = idx >> logv, v = idx & vmask;
+            T.at(e, v) = bmul(fz, fu, T.at(e, v), n);
+        }
         __syncthreads();
     }
     if (mode == 2) {
@@ -317,14 +461,14 @@ __global__ void __launch_bounds__(256) ntt_tile_kernel(KView t, PlanPtrs plans, 
             if (v >= ncol) continue;
             int64_t kk = dim == 3 ? k : e, ll = dim == 3 ? e : cb * V + v;
             int64_t m = *kat<int64_t>(mul, i, j, kk, ll);
-            s[idx] = mul_mont(s[idx], m, mn, mi);
+            T.at(e, v) = mul_mont(T.at(e, v), m, mn, mi);
         }
         __syncthreads();
     }
     if (use_smem) {
         for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
             int e = idx >> logv, v = idx & vmask;
-            if (v < ncol) g[e * ge + v] = s[idx];
+            if (v < ncol) g[e * ge + v] = T.at(e, v);
         }
     }
 }
@@ -421,6 +565,7 @@ hc_status build_plan(hc_context ctx, const hc_modulus* m, const size_t* shape, s
             hp.push(zeta2);
         }
         // forward program (src/hal/ntt.rs:312-353, :355-411)
+        const int fstart = hp.h.nfwd, istart = hp.h.ninv;
         size_t stage_len = flen;
         for (size_t s = 0; s < nst; s++) {
             if (hp.h.nfwd >= HC_MAX_STAGES) return fail(HC_ERR_UNSUPPORTED, "too many NTT stages");
@@ -468,6 +613,38 @@ hc_status build_plan(hc_context ctx, const hc_modulus* m, const size_t* shape, s
                 ibound = (u128)n;
             }
             ibound = st.last ? (u128)n : (u128)radix * ibound;
+        }
+        // passes: radix-2 stages in register groups of up to three, radix-3 stages one by one
+        auto add_pass = [&](bool fwd, int kind, int k, int first, int span, int glen, int nb) {
+            int32_t& cnt = fwd ? hp.h.nfpass : hp.h.nipass;
+            DevPass& ps = (fwd ? hp.h.fpass : hp.h.ipass)[cnt++];
+            ps.kind = kind, ps.k = k, ps.first = first, ps.span = span, ps.glen = glen, ps.nb = nb;
+            ps.div_span = make_fastdiv((uint32_t)(span > 0 ? span : 1));
+            ps.div_nb = make_fastdiv((uint32_t)(nb > 0 ? nb : 1));
+        };
+        const int S = (int)suffix, F = (int)flen, NST = (int)nst;
+        for (int c = 0; c < NST;) {
+            if (!r2) {
+                add_pass(true, 0, 1, fstart + c, 0, 0, 0);
+                c++;
+                continue;
+            }
+            int k = std::min(3, NST - c);
+            int L = F >> c;  // stage length at the pass's first stage
+            add_pass(true, 1, k, fstart + c, (L >> k) * S, L * S, F / L);
+            c += k;
+        }
+        for (int c = 0; c < NST;) {
+            if (!r2) {
+                add_pass(false, 0, 1, istart + c, 0, 0, 0);
+                c++;
+                continue;
+            }
+            int k = std::min(3, NST - c);
+            int Lp = 2 << c;  // stage length of the first processed stage (si = nst - 1 - c)
+            int Llast = Lp << (k - 1);
+            add_pass(false, 1, k, istart + c, (Lp / 2) * S, Llast * S, F / Llast);
+            c += k;
         }
     }
     hp.h.ntw = hp.next_tw();
@@ -538,7 +715,10 @@ hc_status launch_ntt(hc_context ctx, const KView& t, const hc_ntt_plan* plans, s
     }
     int64_t tiles = dim == 3 ? t.n0 * t.n1 * t.n2 : t.n0 * t.n1 * ntile2;
     if (tiles > 0x7fffffff) return fail(HC_ERR_UNSUPPORTED, "too many NTT tiles in one call");
-    ntt_tile_kernel<<<(unsigned)tiles, 256, smem, stream_of(ctx)>>>(t, pp, dim, mode, mul, mods, logv,
+    // about 24 elements (three groups of eight) per thread, 64..256 threads
+    int64_t threads = ((len * V / 24) + 31) / 32 * 32;
+    threads = threads < 64 ? 64 : (threads > 256 ? 256 : threads);
+    ntt_tile_kernel<<<(unsigned)tiles, (unsigned)threads, smem, stream_of(ctx)>>>(t, pp, dim, mode, mul, mods, logv,
                                                                     (int)ntile2, use_smem);
     count_launch(ctx);
     return cuda_check(cudaGetLastError(), "ntt kernel launch");
