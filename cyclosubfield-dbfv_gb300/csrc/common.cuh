@@ -56,11 +56,20 @@ __device__ __forceinline__ int64_t wsub(int64_t a, int64_t b) { return (int64_t)
 
 /// Barrett multiplication by the constant (z, u): q = floor((u x + 2^63) / 2^64), result
 /// z x + q n in wrapping 64-bit arithmetic (|result| <= 3n/4 for |x| <= 2^63).
+/// The signed 128-bit product u x is assembled from the four 32 x 32 -> 64 partial products of
+/// the unsigned operands (each a single wide multiply-add) and corrected for the signs in its
+/// high word: u x = U X - 2^64 ([u < 0] X + [x < 0] U). Bit 63 of the low word, the rounding
+/// bit of the "+ 2^63", is bit 31 of the second partial sum.
 __device__ __forceinline__ int64_t bmul(int64_t z, int64_t u, int64_t x, int64_t n) {
-    int64_t hi = __mul64hi(u, x);
-    uint64_t lo = (uint64_t)u * (uint64_t)x;
-    int64_t q = hi + (int64_t)(lo >> 63);
-    return (int64_t)((uint64_t)z * (uint64_t)x + (uint64_t)q * (uint64_t)n);
+    const uint64_t uu = (uint64_t)u, xx = (uint64_t)x;
+    const uint32_t u0 = (uint32_t)uu, u1 = (uint32_t)(uu >> 32), x0 = (uint32_t)xx, x1 = (uint32_t)(xx >> 32);
+    const uint64_t p00 = (uint64_t)u0 * x0;
+    const uint64_t mid = (uint64_t)u0 * x1 + (p00 >> 32);
+    const uint64_t mid2 = (uint64_t)u1 * x0 + (uint32_t)mid;
+    uint64_t hi = (uint64_t)u1 * x1 + (mid >> 32) + (mid2 >> 32);
+    hi -= (u < 0 ? xx : 0) + (x < 0 ? uu : 0);
+    const int64_t q = (int64_t)hi + (int64_t)((mid2 >> 31) & 1);
+    return (int64_t)((uint64_t)z * xx + (uint64_t)q * (uint64_t)n);
 }
 
 /// Montgomery reduction of the 128-bit value hi:lo: ((x + m n) >> 64) with m = lo * (-n^-1).

@@ -10,6 +10,7 @@
 // held in shared memory: a dimension-3 line (one CTA per line), or a block of dimension-2
 // columns (one CTA per column block). Each butterfly performs exactly the reference's integer
 // formula, so outputs are bit-identical; stages are not algebraically merged.
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -131,6 +132,7 @@ struct hc_ntt_plan_s {
     void* dev;        // DevPlanHeader + twiddles
     int64_t n;
     int32_t len;
+    int32_t ntw;      // twiddle pairs
     size_t bytes;
 };
 
@@ -160,15 +162,15 @@ __device__ __forceinline__ int leg0(uint32_t bb, const DevStage& st, int* block)
 }
 
 struct Tile {
-    int64_t* s;
+    int64_t* __restrict__ s;
     int len, logv;
     bool swz;
     __device__ __forceinline__ int64_t& at(int e, int v) const { return s[sw((e << logv) + v, swz)]; }
 };
 
 /// One forward stage (radix 2 or 3) over the tile in shared memory.
-__device__ __forceinline__ void fwd_stage(const Tile& T, const DevStage& st, const int64_t* tw, int64_t n,
-                                          int64_t one_z, int64_t one_u, bool reduce_output) {
+__device__ __forceinline__ void fwd_stage(const Tile& T, const DevStage st, const int64_t* __restrict__ tw,
+                                          int64_t n, int64_t one_z, int64_t one_u, bool reduce_output) {
     const int radix = st.radix;
     const bool fuse = st.last && reduce_output;
     const int nbf = (T.len / radix) << T.logv;
@@ -224,8 +226,8 @@ __device__ __forceinline__ void fwd_stage(const Tile& T, const DevStage& st, con
 }
 
 /// One inverse stage (radix 2 or 3) over the tile in shared memory.
-__device__ __forceinline__ void inv_stage(const Tile& T, const DevStage& st, const int64_t* tw, int64_t n,
-                                          int64_t il_z, int64_t il_u, int64_t one_z, int64_t one_u) {
+__device__ __forceinline__ void inv_stage(const Tile& T, const DevStage st, const int64_t* __restrict__ tw,
+                                          int64_t n, int64_t il_z, int64_t il_u, int64_t one_z, int64_t one_u) {
     const int radix = st.radix;
     const bool fused = st.last;
     const int nbf = (T.len / radix) << T.logv;
@@ -286,9 +288,21 @@ __device__ __forceinline__ void inv_stage(const Tile& T, const DevStage& st, con
 /// g * glen + o + m * span; at the q-th stage of the pass the butterflies pair m with
 /// m + 2^(K-1-q) and use the twiddle of block block0 * 2^q + (m >> (K-q)).
 template <int K>
-__device__ __forceinline__ void fwd_pass_r2(const Tile& T, const DevPass& ps, const DevStage* sts, const int64_t* tw,
-                                            int64_t n, int64_t one_z, int64_t one_u, bool reduce_output) {
+__device__ __forceinline__ void fwd_pass_r2(const Tile& T, const DevPass ps, const DevStage* sts,
+                                            const int64_t* __restrict__ tw, int64_t n, int64_t one_z, int64_t one_u,
+                                            bool reduce_output) {
     constexpr int M = 1 << K;
+    // the stage parameters, read once into registers
+    int tw_off[K];
+    bool red[K], skip_ok[K], fuse[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        const DevStage& st = sts[ps.first + q];
+        tw_off[q] = st.tw_off;
+        red[q] = st.reduce_before;
+        skip_ok[q] = st.skip_ok;
+        fuse[q] = st.last && reduce_output;
+    }
     const int ng = (T.len >> K) << T.logv;
     const int vmask = (1 << T.logv) - 1;
     for (int gi = threadIdx.x; gi < ng; gi += blockDim.x) {
@@ -303,23 +317,21 @@ __device__ __forceinline__ void fwd_pass_r2(const Tile& T, const DevPass& ps, co
         for (int m = 0; m < M; m++) x[m] = T.at(base + m * ps.span, v);
 #pragma unroll
         for (int q = 0; q < K; q++) {
-            const DevStage& st = sts[ps.first + q];
-            if (st.reduce_before) {
+            if (red[q]) {
 #pragma unroll
                 for (int m = 0; m < M; m++) x[m] = bmul(one_z, one_u, x[m], n);
             }
-            const bool fuse = st.last && reduce_output;
             const int half = M >> (q + 1);
 #pragma unroll
             for (int j = 0; j < M / 2; j++) {
                 const int m1 = ((j / half) * 2 * half) + (j % half), m2 = m1 + half;
                 const int tb = block0 * (1 << q) + (m1 >> (K - q));
-                const int64_t z = tw[2 * (st.tw_off + tb)], u = tw[2 * (st.tw_off + tb) + 1];
-                const bool skip = st.skip_ok && z == 1;
+                const int64_t z = tw[2 * (tw_off[q] + tb)], u = tw[2 * (tw_off[q] + tb) + 1];
+                const bool skip = skip_ok[q] && z == 1;
                 const int64_t a = x[m1];
                 const int64_t t = skip ? x[m2] : bmul(z, u, x[m2], n);
                 int64_t o0 = wadd(a, t), o1 = wsub(a, t);
-                if (fuse) {
+                if (fuse[q]) {
                     o0 = bmul(one_z, one_u, o0, n);
                     o1 = bmul(one_z, one_u, o1, n);
                 }
@@ -336,9 +348,19 @@ __device__ __forceinline__ void fwd_pass_r2(const Tile& T, const DevPass& ps, co
 /// of the pass the butterflies pair m with m + 2^q and use the twiddle of block
 /// blockK * 2^(K-1-q) + (m >> (q+1)), blockK being the group's block at the pass's last stage.
 template <int K>
-__device__ __forceinline__ void inv_pass_r2(const Tile& T, const DevPass& ps, const DevStage* sts, const int64_t* tw,
-                                            int64_t n, int64_t il_z, int64_t il_u, int64_t one_z, int64_t one_u) {
+__device__ __forceinline__ void inv_pass_r2(const Tile& T, const DevPass ps, const DevStage* sts,
+                                            const int64_t* __restrict__ tw, int64_t n, int64_t il_z, int64_t il_u,
+                                            int64_t one_z, int64_t one_u) {
     constexpr int M = 1 << K;
+    int tw_off[K];
+    bool red[K], fused[K];
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+        const DevStage& st = sts[ps.first + q];
+        tw_off[q] = st.tw_off;
+        red[q] = st.reduce_before;
+        fused[q] = st.last;
+    }
     const int ng = (T.len >> K) << T.logv;
     const int vmask = (1 << T.logv) - 1;
     for (int gi = threadIdx.x; gi < ng; gi += blockDim.x) {
@@ -353,29 +375,27 @@ __device__ __forceinline__ void inv_pass_r2(const Tile& T, const DevPass& ps, co
         for (int m = 0; m < M; m++) x[m] = T.at(base + m * ps.span, v);
 #pragma unroll
         for (int q = 0; q < K; q++) {
-            const DevStage& st = sts[ps.first + q];
-            if (st.reduce_before) {
+            if (red[q]) {
 #pragma unroll
                 for (int m = 0; m < M; m++) x[m] = bmul(one_z, one_u, x[m], n);
             }
-            const bool fused = st.last;
             const int dist = 1 << q;
 #pragma unroll
             for (int j = 0; j < M / 2; j++) {
                 const int m1 = ((j >> q) << (q + 1)) | (j & (dist - 1)), m2 = m1 + dist;
                 const int tb = blockK * (1 << (K - 1 - q)) + (m1 >> (q + 1));
                 int64_t yz, yu;
-                if (fused) {
+                if (fused[q]) {
                     yz = il_z;
                     yu = il_u;
                 } else {
-                    yz = tw[2 * (st.tw_off + tb)];
-                    yu = tw[2 * (st.tw_off + tb) + 1];
+                    yz = tw[2 * (tw_off[q] + tb)];
+                    yu = tw[2 * (tw_off[q] + tb) + 1];
                 }
-                const bool skip = !fused && yz == 1;
+                const bool skip = !fused[q] && yz == 1;
                 const int64_t y0 = x[m1], y1 = x[m2];
                 const int64_t sum = wadd(y0, y1), dif = wsub(y0, y1);
-                x[m1] = fused ? bmul(yz, yu, sum, n) : sum;
+                x[m1] = fused[q] ? bmul(yz, yu, sum, n) : sum;
                 x[m2] = skip ? dif : bmul(yz, yu, dif, n);
             }
         }
@@ -388,10 +408,14 @@ struct PlanPtrs {
     const DevPlanHeader* p[HC_MAX_MODS];
 };
 
+#ifndef HC_NTT_MIN_BLOCKS
+#define HC_NTT_MIN_BLOCKS 3  // resident CTAs per SM the register allocation must allow
+#endif
+
 /// mode 0: forward (reduced), 1: inverse, 2: forward unreduced + Montgomery multiplication by `mul`.
 /// dim 3: tile = line (i, j, k), element e at l = e.  dim 2: tile = (i, j, column block),
 /// element (e, v) at k = e, l = cb * V + v.
-__global__ void __launch_bounds__(256) ntt_tile_kernel(KView t, PlanPtrs plans, int dim, int mode, KView mul,
+__global__ void __launch_bounds__(256, HC_NTT_MIN_BLOCKS) ntt_tile_kernel(KView t, PlanPtrs plans, int dim, int mode, KView mul,
                                                        KMods mods, int logv, int ntile2, int use_smem) {
     extern __shared__ int64_t smem[];
     const int V = 1 << logv, vmask = V - 1;
@@ -411,7 +435,13 @@ __global__ void __launch_bounds__(256) ntt_tile_kernel(KView t, PlanPtrs plans, 
     }
     const DevPlanHeader* P = plans.p[j];
     const int64_t n = P->n;
-    const int64_t* tw = reinterpret_cast<const int64_t*>(P + 1);
+    // the plan's twiddle constants are staged in shared memory, behind the tile
+    int64_t* tws = smem + (use_smem ? (size_t)len * V : 0);
+    {
+        const int64_t* twg = reinterpret_cast<const int64_t*>(P + 1);
+        for (int idx = threadIdx.x; idx < 2 * P->ntw; idx += blockDim.x) tws[idx] = twg[idx];
+    }
+    const int64_t* tw = tws;
     int64_t* g = reinterpret_cast<int64_t*>(t.p) + i * t.s0 + j * t.s1 + (dim == 3 ? k * t.s2 : cb * V);
     const int64_t ge = dim == 3 ? 1 : t.s2;  // global stride of element e
     const int64_t ncol = dim == 3 ? 1 : t.n3 - cb * V;
@@ -424,23 +454,24 @@ __global__ void __launch_bounds__(256) ntt_tile_kernel(KView t, PlanPtrs plans, 
             int e = idx >> logv, v = idx & vmask;
             T.at(e, v) = v < ncol ? g[e * ge + v] : 0;
         }
-        __syncthreads();
     }
+    __syncthreads();
     const bool inverse = mode == 1;
     const int npass = inverse ? P->nipass : P->nfpass;
+    const int64_t one_z = P->one_z, one_u = P->one_u, il_z = P->invlen_z, il_u = P->invlen_u;
     for (int pi = 0; pi < npass; pi++) {
-        const DevPass& ps = inverse ? P->ipass[pi] : P->fpass[pi];
+        const DevPass ps = inverse ? P->ipass[pi] : P->fpass[pi];
         if (ps.kind == 0) {
-            if (inverse) inv_stage(T, P->inv[ps.first], tw, n, P->invlen_z, P->invlen_u, P->one_z, P->one_u);
-            else fwd_stage(T, P->fwd[ps.first], tw, n, P->one_z, P->one_u, mode == 0);
+            if (inverse) inv_stage(T, P->inv[ps.first], tw, n, il_z, il_u, one_z, one_u);
+            else fwd_stage(T, P->fwd[ps.first], tw, n, one_z, one_u, mode == 0);
         } else if (inverse) {
-            if (ps.k == 3) inv_pass_r2<3>(T, ps, P->inv, tw, n, P->invlen_z, P->invlen_u, P->one_z, P->one_u);
-            else if (ps.k == 2) inv_pass_r2<2>(T, ps, P->inv, tw, n, P->invlen_z, P->invlen_u, P->one_z, P->one_u);
-            else inv_pass_r2<1>(T, ps, P->inv, tw, n, P->invlen_z, P->invlen_u, P->one_z, P->one_u);
+            if (ps.k == 3) inv_pass_r2<3>(T, ps, P->inv, tw, n, il_z, il_u, one_z, one_u);
+            else if (ps.k == 2) inv_pass_r2<2>(T, ps, P->inv, tw, n, il_z, il_u, one_z, one_u);
+            else inv_pass_r2<1>(T, ps, P->inv, tw, n, il_z, il_u, one_z, one_u);
         } else {
-            if (ps.k == 3) fwd_pass_r2<3>(T, ps, P->fwd, tw, n, P->one_z, P->one_u, mode == 0);
-            else if (ps.k == 2) fwd_pass_r2<2>(T, ps, P->fwd, tw, n, P->one_z, P->one_u, mode == 0);
-            else fwd_pass_r2<1>(T, ps, P->fwd, tw, n, P->one_z, P->one_u, mode == 0);
+            if (ps.k == 3) fwd_pass_r2<3>(T, ps, P->fwd, tw, n, one_z, one_u, mode == 0);
+            else if (ps.k == 2) fwd_pass_r2<2>(T, ps, P->fwd, tw, n, one_z, one_u, mode == 0);
+            else fwd_pass_r2<1>(T, ps, P->fwd, tw, n, one_z, one_u, mode == 0);
         }
         __syncthreads();
     }
@@ -663,6 +694,7 @@ hc_status build_plan(hc_context ctx, const hc_modulus* m, const size_t* shape, s
     plan->dev = dev;
     plan->n = n;
     plan->len = (int32_t)len;
+    plan->ntw = hp.h.ntw;
     plan->bytes = bytes;
     *out = plan;
     return HC_OK;
@@ -686,10 +718,12 @@ hc_status launch_ntt(hc_context ctx, const KView& t, const hc_ntt_plan* plans, s
     if (nplans > HC_MAX_MODS) return fail(HC_ERR_UNSUPPORTED, "too many RNS rows in one call");
     const int64_t len = dim == 3 ? t.n3 : t.n2;
     PlanPtrs pp;
+    int32_t max_tw = 0;
     for (size_t j = 0; j < nplans; j++) {
         if (!plans[j]) return fail(HC_ERR_ARG, "null NTT plan");
         if (plans[j]->len != len) return fail(HC_ERR_SHAPE, "NTT plan length does not match the transformed dimension");
         pp.p[j] = reinterpret_cast<const DevPlanHeader*>(plans[j]->dev);
+        max_tw = std::max(max_tw, plans[j]->ntw);
     }
     if (t.n0 == 0 || t.n1 == 0 || t.n2 == 0 || t.n3 == 0) return HC_OK;
     int V = 1, logv = 0;
@@ -701,13 +735,15 @@ hc_status launch_ntt(hc_context ctx, const KView& t, const hc_ntt_plan* plans, s
         while ((1 << logv) < V) logv++;
         ntile2 = (t.n3 + V - 1) / V;
     }
-    size_t smem = (size_t)len * V * 8;
+    const size_t tw_bytes = (size_t)max_tw * 16;
+    size_t smem = (size_t)len * V * 8 + tw_bytes;
     int use_smem = 1;
     size_t maxs = max_smem_optin(ctx);
     if (smem > maxs) {
         if (dim == 2) return fail(HC_ERR_UNSUPPORTED, "dimension-2 NTT length too large");
         use_smem = 0;
-        smem = 0;
+        smem = tw_bytes;
+        if (smem > maxs) return fail(HC_ERR_UNSUPPORTED, "NTT twiddle table too large");
     }
     if (smem > 49152) {
         cudaError_t e = cudaFuncSetAttribute(ntt_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
