@@ -40,6 +40,7 @@ void count_launch(hc_context ctx, uint64_t n) { ctx->launches += n; }
 uint64_t launch_counter(hc_context ctx) { return ctx->launches; }
 int num_sms(hc_context ctx) { return ctx->sms; }
 size_t max_smem_optin(hc_context ctx) { return ctx->smem_optin; }
+int device_of(hc_context ctx) { return ctx->device; }
 
 // defined in ntt.cu / ops.cu
 hc_status build_plan(hc_context ctx, const hc_modulus* m, const size_t* shape, size_t k, hc_ntt_plan* out);

@@ -130,5 +130,6 @@ cudaStream_t stream_of(hc_context ctx);
 void count_launch(hc_context ctx, uint64_t n = 1);
 int num_sms(hc_context ctx);
 size_t max_smem_optin(hc_context ctx);
+int device_of(hc_context ctx);
 
 }  // namespace hc

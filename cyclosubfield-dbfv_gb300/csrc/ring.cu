@@ -13,6 +13,7 @@
 #include <functional>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <set>
 #include <unordered_map>
 #include <vector>
@@ -1473,3 +1474,83 @@ hc_status hc_bfv_hom_gal(hc_ring R, hc_view ct, const size_t* base, size_t r, co
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------- key switching without allocation
+//
+// hc_bfv_key_switch_noalloc is hc_bfv_key_switch for callers that must not allocate device memory:
+// hosts whose device memory is handed out by their own arena or budget (a language runtime or a
+// serving process that reserves HBM up front), and code paths where cudaMalloc / cudaFree are not
+// permitted or would synchronise the device at the wrong moment. The only scratch it needs, the
+// gadget digits of c1 (d x r x deg_L' x deg_K residues), lives in the static array below, which
+// every GPU that loads this library holds until the process exits.
+
+/// Words (i64) of the scratch array: 32 MiB per GPU.
+#define HC_KS_NOALLOC_WORDS ((size_t)1 << 22)
+
+/// Gadget digits of the no-allocation key switch. Host code never dereferences this name: its
+/// device address comes from cudaGetSymbolAddress, once per device.
+static __device__ __align__(256) int64_t hc_ks_noalloc_scratch[HC_KS_NOALLOC_WORDS];
+
+namespace {
+
+std::mutex ks_noalloc_mu;
+std::map<int, int64_t*> ks_noalloc_addr;  // device ordinal -> address of the scratch array there
+
+/// Address of the scratch array on `device`, looked up on the first call for that device with
+/// the device made current for the lookup (and the caller's current device restored).
+int64_t* ks_noalloc_scratch(int device) {
+    std::lock_guard<std::mutex> lock(ks_noalloc_mu);
+    auto it = ks_noalloc_addr.find(device);
+    if (it != ks_noalloc_addr.end()) return it->second;
+    int prev = 0;
+    CK(cuda_check(cudaGetDevice(&prev), "cudaGetDevice"));
+    if (prev != device) CK(cuda_check(cudaSetDevice(device), "cudaSetDevice"));
+    int64_t* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void**)&p, hc_ks_noalloc_scratch);
+    if (prev != device) cudaSetDevice(prev);
+    CK(cuda_check(e, "address of the key-switch scratch array"));
+    ks_noalloc_addr[device] = p;
+    return p;
+}
+
+/// Whether the ring already holds every device table the key switch reads for this base and
+/// digit split (CRT kernels, gadget conversion constants, Montgomery ones), so that no call below
+/// has to build and upload one.
+bool ks_tables_ready(hc_ring R, const Base& b, const Digits& dg) {
+    bool t = false, g = false;
+    for (auto& c : R->tcache) t = t || c->base == b;
+    for (auto& c : R->gcache) g = g || (c->base == b && c->digits == dg);
+    return t && g && R->one_cache.count(b) > 0;
+}
+
+}  // namespace
+
+extern "C" hc_status hc_bfv_key_switch_noalloc(hc_ring R, hc_view c0, hc_view c1_pb, const size_t* base, size_t r,
+                                               hc_view keys, const size_t* digits, size_t d, hc_view out) {
+    return guard([&] {
+        REQUIRE(R, HC_ERR_ARG, "null ring");
+        Base b = base_of(base, r);
+        check_view(out, 2, (int64_t)r, R->dl(), R->dk(), "key switch output");
+        check_view(c1_pb, 1, (int64_t)r, R->dl(), R->dk(), "key switch c1");
+        Digits dg = clip(digits_of(digits, d), r);
+        REQUIRE(!dg.empty(), HC_ERR_ARG, "at least one gadget digit required");
+        const size_t words = dg.size() * r * (size_t)R->dl() * (size_t)R->dk();
+        REQUIRE(words <= HC_KS_NOALLOC_WORDS, HC_ERR_UNSUPPORTED,
+                "no-allocation key switch: digits x RNS factors x ring degree = " + std::to_string(words) +
+                    " exceeds the scratch array of " + std::to_string(HC_KS_NOALLOC_WORDS) + " words (32 MiB)");
+        REQUIRE(ks_tables_ready(R, b, dg), HC_ERR_ARG,
+                "no-allocation key switch: the ring has no tables for this base and digit split yet; one "
+                "hc_bfv_key_switch call with the same base and digits builds them");
+        int64_t* scratch = ks_noalloc_scratch(device_of(R->ctx));
+        hc_view parts;
+        parts.ptr = scratch;
+        parts.shape[0] = (int64_t)dg.size(), parts.shape[1] = (int64_t)r, parts.shape[2] = R->dl();
+        parts.shape[3] = R->dk();
+        parts.strides[3] = 1, parts.strides[2] = R->dk(), parts.strides[1] = R->dl() * R->dk();
+        parts.strides[0] = (int64_t)r * R->dl() * R->dk();
+        // every digit residue is written by the conversion before it is read: nothing to clear
+        R->bconv_gadget(parts, c1_pb, b, dg);
+        R->transform(parts, b, false);
+        keyswitch(R, parts, keys, b, dg.size(), &c0, nullptr, out);
+    });
+}

@@ -200,6 +200,15 @@ class RingContext:
                                       keys.view(), dg, nd, out.view()))
         return out
 
+    def key_switch_noalloc(self, c0, c1_pb, base, keys, digits, out):
+        """hc_bfv_key_switch_noalloc: key_switch into a caller-provided `out` [2, r] without any
+        device allocation (scratch in the library's static array; tables built by an earlier
+        key_switch with the same base and digits)."""
+        dg, nd = _digits(digits)
+        check(lib().hc_bfv_key_switch_noalloc(self.h, c0.view(), c1_pb.view(), _sz(base), ctypes.c_size_t(len(base)),
+                                              keys.view(), dg, nd, out.view()))
+        return out
+
     def lift_to_extended(self, pb, base, crt=None):
         ext = self.extension_base(base)
         out = self.allocate(pb.shape[0], len(base) + len(ext))

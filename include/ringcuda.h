@@ -99,6 +99,23 @@ hc_status hc_bfv_hom_mul(hc_ring ring, const int64_t t[2], hc_view ct1, hc_view 
 hc_status hc_bfv_hom_gal(hc_ring ring, hc_view ct, const size_t* base, size_t r, const uint64_t* gs, size_t ngs,
                          hc_view gks, const size_t* digits, size_t d, hc_view out);
 
+/* No counterpart in the reference (its CPU backend allocates freely): hc_bfv_key_switch with the
+ * same arguments and the same result, for callers that cannot allocate device memory - a host
+ * whose HBM is handed out by its own arena or budget, or a code path where cudaMalloc / cudaFree
+ * are not permitted or would synchronise the device at the wrong moment. It allocates nothing:
+ * the gadget digits are kept in a static device array of 32 MiB (2^22 i64 words) that every GPU
+ * loading this library holds until the process exits.
+ *  - d x r x deg_L' x deg_K must be at most 2^22 (field_36864: d r <= 113), else
+ *    HC_ERR_UNSUPPORTED.
+ *  - The ring's tables for this base and digit split must exist: one hc_bfv_key_switch call with
+ *    the same base and digits builds them; without it the call fails with HC_ERR_ARG.
+ *  - The first call on a device looks up the array's device address (cudaGetSymbolAddress); make
+ *    that first call before any stream capture.
+ *  - All calls share the one array: calls whose kernels may overlap on the GPU (other streams,
+ *    other contexts on the same device) race and corrupt each other's results. */
+hc_status hc_bfv_key_switch_noalloc(hc_ring ring, hc_view c0_crt, hc_view c1_pb, const size_t* base, size_t r,
+                                    hc_view keys, const size_t* digits, size_t d, hc_view out);
+
 #ifdef __cplusplus
 }
 #endif
