@@ -39,6 +39,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=8, help="ciphertext pairs multiplied per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-crt-batch", action="store_true", help="skip the batched CRT-transform workload")
     return ap.parse_args()
 
 
@@ -156,6 +157,95 @@ class Workload:
         """One ct-mult per call, the reference's calling pattern."""
         self.ring.hom_mul(T, self.ct1.rows(2 * b, 2 * b + 2), self.ct2.rows(2 * b, 2 * b + 2), self.base, self.rk,
                           self.digits, out=self.out.rows(2 * b, 2 * b + 2))
+
+
+class CrtWorkload:
+    """Batched CRT transforms: `elements` ring elements, the field drawn uniformly from
+    {field_36864, field_49152} and the RNS length uniformly from 4..24 (seeded); each element goes
+    period basis -> CRT basis, Montgomery product with a seeded operand, CRT basis -> period
+    basis. Residues are uniform in [-2^56, 2^56), below every 57-bit factor. Elements of the same
+    field and length share one tensor; the batch runs them all in one persistent launch."""
+
+    FIELDS = (("field_36864", 900, 930, 8), ("field_49152", 1280, 1310, 2))
+
+    def __init__(self, be, elements=512, seed=3):
+        import numpy as np
+
+        import ringcuda
+
+        self.be = be
+        self.rings = [ringcuda.RingContext(f, lo, hi, tb, backend=be) for f, lo, hi, tb in self.FIELDS]
+        g = np.random.default_rng(seed)
+        fields = g.integers(0, 2, size=elements)
+        lens = g.integers(4, 25, size=elements)
+        groups = {}
+        for f, r in zip(fields.tolist(), lens.tolist()):
+            groups[(f, r)] = groups.get((f, r), 0) + 1
+        block = g.integers(-(1 << 56), 1 << 56, size=1 << 22, dtype=np.int64)
+        self.items, self.elements, self.residues = [], elements, 0
+        for (f, r), c in sorted(groups.items()):
+            R = self.rings[f]
+            shape = R.shape(c, r)
+            size = c * r * R.dl * R.dk
+            reps = -(-size // block.size)
+            x = be.tensor(np.tile(block, reps)[:size].reshape(shape))
+            op = be.tensor(np.tile(block[::-1], reps)[:size].reshape(shape))
+            self.items.append((R, x, op, list(range(r))))
+            self.residues += size
+        self.batch = ringcuda.CrtBatch(self.items, ringcuda.CRT_FORWARD | ringcuda.CRT_MUL | ringcuda.CRT_INVERSE,
+                                       backend=be)
+        self.launch = self.batch.tune(reps=2)
+        self.batch.run()
+        be.synchronize()
+        import halcuda
+
+        self.graph = halcuda.Graph(be, self.batch.run)
+
+    def plain_element(self, R, x, op, base, mods, i):
+        """One element with the HAL/ring calls of the reference, one launch per pass."""
+        xi, oi = x.rows(i, i + 1), op.rows(i, i + 1)
+        R.pb_to_crt(xi, base)
+        self.be.hal_mul_mont64(xi, oi, mods)
+        R.crt_to_pb(xi, base)
+
+
+def crt_batch_bench(be, steps, warmup):
+    """CRT transforms/s (2 per element: forward and inverse) batched (graph replay of the persistent
+    launch) and plain (one element at a time); inputs ~2.5 GB, larger than L2."""
+    import halcuda
+
+    w = CrtWorkload(be)
+    ev0, ev1 = halcuda.Event(), halcuda.Event()
+    for _ in range(warmup):
+        w.graph.launch()
+    be.synchronize()
+    l0 = be.launch_count()
+    ev0.record(be)
+    for _ in range(steps):
+        w.graph.launch()
+    ev1.record(be)
+    ms = ev0.elapsed_ms(ev1) / steps
+    launches = (be.launch_count() - l0) // steps
+    # host-side modulus lists are built outside the timed region
+    plain_items = [(R, x, op, base, R.mods_for(base)) for R, x, op, base in w.items]
+    w.plain_element(*plain_items[0], 0)
+    be.synchronize()
+    ev0.record(be)
+    for R, x, op, base, mods in plain_items:
+        for i in range(x.shape[0]):
+            w.plain_element(R, x, op, base, mods, i)
+    ev1.record(be)
+    plain_ms = ev0.elapsed_ms(ev1)
+    n = w.elements
+    return {"workload": "%d elements, field uniform in {field_36864, field_49152}, RNS length uniform in 4..24; "
+                        "each pb->crt, mul_mont64 by an operand, crt->pb" % n,
+            "elements": n, "slabs": w.batch.num_slabs, "residues": w.residues,
+            "crt_transforms_per_s": round(2 * n / (ms * 1e-3), 1),
+            "plain_crt_transforms_per_s": round(2 * n / (plain_ms * 1e-3), 1),
+            "ms_per_batch": round(ms, 4), "plain_ms_per_batch": round(plain_ms, 4),
+            "launches_per_batch": launches, "plain_launches_per_batch": 9 * n,
+            "launch_shape": {"threads": w.launch[0], "ctas_per_sm": w.launch[1], "dim2_columns": 1 << w.launch[2]},
+            "autotuned": True, "l2": "inputs 2 x %.1f GB, larger than L2" % (w.residues * 8 / 1e9)}
 
 
 def flush_l2(be, scratch):
@@ -391,6 +481,7 @@ def main():
     e2e_ms, h2d, d2h, _ = e2e_steps(be, work, args.steps)
     e2e_val = dist.world * work.batch * args.steps / (e2e_ms * 1e-3)
     roof = kernel_roofline(be, work, 20, peaks)
+    crt = None if args.no_crt_batch else crt_batch_bench(be, max(3, args.steps // 2), args.warmup)
 
     if dist.rank != 0:
         return
@@ -421,6 +512,8 @@ def main():
         "roofline": roof,
         "clocks": clk,
     }
+    if crt:
+        line["crt_batch"] = crt
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)

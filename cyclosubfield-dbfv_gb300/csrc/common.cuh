@@ -13,6 +13,7 @@
 #include <string>
 
 #include "../../include/halcuda.h"
+#include "../../include/ringcuda.h"
 
 typedef __int128 i128;
 typedef unsigned __int128 u128;
@@ -117,6 +118,34 @@ __device__ __forceinline__ void st128(void* p, i128 x) {
     v.y = (long long)(x >> 64);
     *reinterpret_cast<longlong2*>(p) = v;
 }
+
+// ------------------------------------------------------------------------------------------
+// Batched CRT transforms
+// ------------------------------------------------------------------------------------------
+
+/// One (ring element, RNS factor) slab of a batched transform: deg_L' rows of deg_K residues.
+struct CrtSlab {
+    const void* plan2;     // NTT plan along dimension 2 (length deg_L')
+    const void* plan3;     // NTT plan along dimension 3 (length deg_K)
+    int64_t* data;         // row k at data + k * s2, contiguous
+    const int64_t* op;     // operand slab (HC_CRT_MUL), row k at op + k * op_s2
+    const int64_t* kl;     // CRT kernel of this factor along dimension 2 (deg_L' entries)
+    const int64_t* kk;     // ... along dimension 3 (deg_K entries)
+    const int64_t* ikl;    // inverse kernels
+    const int64_t* ikk;
+    int64_t s2, op_s2;
+    int64_t n, ninv;       // Montgomery modulus of the factor
+    int32_t dl, dk;
+    int32_t ops;           // HC_CRT_* bits
+    int32_t pad;
+};
+
+/// Launch shape of the persistent batched-transform kernel (chosen by the autotuner).
+struct CrtLaunch {
+    int threads;      // per CTA
+    int ctas_per_sm;  // persistent grid = SMs x this
+    int logv;         // dimension-2 tile: 2^logv columns
+};
 
 // ------------------------------------------------------------------------------------------
 // Host-side helpers shared by the translation units

@@ -412,51 +412,38 @@ struct PlanPtrs {
 #define HC_NTT_MIN_BLOCKS 3  // resident CTAs per SM the register allocation must allow
 #endif
 
-/// mode 0: forward (reduced), 1: inverse, 2: forward unreduced + Montgomery multiplication by `mul`.
-/// dim 3: tile = line (i, j, k), element e at l = e.  dim 2: tile = (i, j, column block),
-/// element (e, v) at k = e, l = cb * V + v.
-__global__ void __launch_bounds__(256, HC_NTT_MIN_BLOCKS) ntt_tile_kernel(KView t, PlanPtrs plans, int dim, int mode, KView mul,
-                                                       KMods mods, int logv, int ntile2, int use_smem) {
-    extern __shared__ int64_t smem[];
+/// Where one tile lives in global memory and where its Montgomery multiplier (modes 2 and 3)
+/// comes from: element (e, v) of the tile is g[e * ge + v] and is multiplied by
+/// mulp[e * me + v * mv] modulo (mn, mi).
+struct TileIO {
+    int64_t* g;
+    int64_t ge;
+    int64_t ncol;  // valid columns of the tile (a dimension-2 block at the end of the axis)
+    const int64_t* mulp;
+    int64_t me, mv;
+    int64_t mn, mi;
+};
+
+/// One tile transformed by plan P, twiddles `tw` already staged. mode 0: forward (reduced),
+/// 1: inverse, 2: forward unreduced + Montgomery multiplication, 3: inverse + Montgomery
+/// multiplication. With `use_smem` the tile is copied to `s` (len x 2^logv elements) and back;
+/// otherwise (single lines too long for shared memory) it is worked on in place in global memory.
+/// Ends with a block barrier, so the caller may reuse the shared memory at once.
+__device__ __forceinline__ void tile_run(const DevPlanHeader* __restrict__ P, const int64_t* __restrict__ tw,
+                                         int64_t* s, int len, int logv, bool use_smem, int mode,
+                                         const TileIO& io) {
     const int V = 1 << logv, vmask = V - 1;
-    const int len = dim == 3 ? (int)t.n3 : (int)t.n2;
-    int64_t tile = blockIdx.x;
-    int64_t i, j, k = 0, cb = 0;
-    if (dim == 3) {
-        k = tile % t.n2;
-        int64_t r = tile / t.n2;
-        j = r % t.n1;
-        i = r / t.n1;
-    } else {
-        cb = tile % ntile2;
-        int64_t r = tile / ntile2;
-        j = r % t.n1;
-        i = r / t.n1;
-    }
-    const DevPlanHeader* P = plans.p[j];
     const int64_t n = P->n;
-    // the plan's twiddle constants are staged in shared memory, behind the tile
-    int64_t* tws = smem + (use_smem ? (size_t)len * V : 0);
-    {
-        const int64_t* twg = reinterpret_cast<const int64_t*>(P + 1);
-        for (int idx = threadIdx.x; idx < 2 * P->ntw; idx += blockDim.x) tws[idx] = twg[idx];
-    }
-    const int64_t* tw = tws;
-    int64_t* g = reinterpret_cast<int64_t*>(t.p) + i * t.s0 + j * t.s1 + (dim == 3 ? k * t.s2 : cb * V);
-    const int64_t ge = dim == 3 ? 1 : t.s2;  // global stride of element e
-    const int64_t ncol = dim == 3 ? 1 : t.n3 - cb * V;
     const int total = len * V;
-    // without shared memory (lines too long for it) the tile is worked on in place in global
-    // memory; this is only valid for dim 3 (V == 1, unit element stride)
-    Tile T{use_smem ? smem : g, len, logv, use_smem && logv == 0 && (len & 15) == 0};
+    Tile T{use_smem ? s : io.g, len, logv, use_smem && logv == 0 && (len & 15) == 0};
     if (use_smem) {
         for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
             int e = idx >> logv, v = idx & vmask;
-            T.at(e, v) = v < ncol ? g[e * ge + v] : 0;
+            T.at(e, v) = v < io.ncol ? io.g[e * io.ge + v] : 0;
         }
     }
     __syncthreads();
-    const bool inverse = mode == 1;
+    const bool inverse = mode & 1;
     const int npass = inverse ? P->nipass : P->nfpass;
     const int64_t one_z = P->one_z, one_u = P->one_u, il_z = P->invlen_z, il_u = P->invlen_u;
     for (int pi = 0; pi < npass; pi++) {
@@ -477,7 +464,7 @@ __global__ void __launch_bounds__(256, HC_NTT_MIN_BLOCKS) ntt_tile_kernel(KView 
     }
     // plans without factors (length 1): the inverse scales by 1^-1, the reduced forward
     // reduces; an unreduced forward leaves the data unchanged
-    if (npass == 0 && (mode == 0 || mode == 1)) {
+    if (npass == 0 && (mode == 0 || inverse)) {
         int64_t fz = inverse ? P->invlen_z : P->one_z, fu = inverse ? P->invlen_u : P->one_u;
         for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
             int e = idx >> logv, v = idx & vmask;
@@ -485,21 +472,137 @@ __global__ void __launch_bounds__(256, HC_NTT_MIN_BLOCKS) ntt_tile_kernel(KView 
         }
         __syncthreads();
     }
-    if (mode == 2) {
-        const int64_t mn = mods.n[j], mi = mods.ninv[j];
+    if (mode & 2) {
         for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
             int e = idx >> logv, v = idx & vmask;
-            if (v >= ncol) continue;
-            int64_t kk = dim == 3 ? k : e, ll = dim == 3 ? e : cb * V + v;
-            int64_t m = *kat<int64_t>(mul, i, j, kk, ll);
-            T.at(e, v) = mul_mont(T.at(e, v), m, mn, mi);
+            if (v >= io.ncol) continue;
+            T.at(e, v) = mul_mont(T.at(e, v), io.mulp[e * io.me + v * io.mv], io.mn, io.mi);
         }
         __syncthreads();
     }
     if (use_smem) {
         for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
             int e = idx >> logv, v = idx & vmask;
-            if (v < ncol) g[e * ge + v] = T.at(e, v);
+            if (v < io.ncol) io.g[e * io.ge + v] = T.at(e, v);
+        }
+    }
+    __syncthreads();
+}
+
+/// Copies the twiddle table of plan P to shared memory (no barrier).
+__device__ __forceinline__ void stage_twiddles(const DevPlanHeader* P, int64_t* dst) {
+    const int64_t* twg = reinterpret_cast<const int64_t*>(P + 1);
+    for (int idx = threadIdx.x; idx < 2 * P->ntw; idx += blockDim.x) dst[idx] = twg[idx];
+}
+
+/// mode 0: forward (reduced), 1: inverse, 2: forward unreduced + Montgomery multiplication by `mul`.
+/// dim 3: tile = line (i, j, k), element e at l = e.  dim 2: tile = (i, j, column block),
+/// element (e, v) at k = e, l = cb * V + v.
+__global__ void __launch_bounds__(256, HC_NTT_MIN_BLOCKS) ntt_tile_kernel(KView t, PlanPtrs plans, int dim, int mode, KView mul,
+                                                       KMods mods, int logv, int ntile2, int use_smem) {
+    extern __shared__ int64_t smem[];
+    const int V = 1 << logv;
+    const int len = dim == 3 ? (int)t.n3 : (int)t.n2;
+    int64_t tile = blockIdx.x;
+    int64_t i, j, k = 0, cb = 0;
+    if (dim == 3) {
+        k = tile % t.n2;
+        int64_t r = tile / t.n2;
+        j = r % t.n1;
+        i = r / t.n1;
+    } else {
+        cb = tile % ntile2;
+        int64_t r = tile / ntile2;
+        j = r % t.n1;
+        i = r / t.n1;
+    }
+    const DevPlanHeader* P = plans.p[j];
+    // the plan's twiddle constants are staged in shared memory, behind the tile
+    int64_t* tws = smem + (use_smem ? (size_t)len * V : 0);
+    stage_twiddles(P, tws);
+    TileIO io;
+    io.g = reinterpret_cast<int64_t*>(t.p) + i * t.s0 + j * t.s1 + (dim == 3 ? k * t.s2 : cb * V);
+    io.ge = dim == 3 ? 1 : t.s2;
+    io.ncol = dim == 3 ? 1 : t.n3 - cb * V;
+    io.mulp = nullptr, io.me = io.mv = 0, io.mn = io.mi = 0;
+    if (mode == 2) {
+        io.mulp = kat<int64_t>(mul, i, j, dim == 3 ? k : 0, dim == 3 ? 0 : cb * V);
+        io.me = dim == 3 ? (mul.b3 ? 0 : 1) : mul.s2;
+        io.mv = dim == 3 ? 0 : (mul.b3 ? 0 : 1);
+        io.mn = mods.n[j], io.mi = mods.ninv[j];
+    }
+    tile_run(P, tws, smem, len, logv, use_smem, mode, io);
+}
+
+/// One pass of a batched transform over a whole slab: its deg_L' lines (dimension 3) or its
+/// column blocks of 2^logv columns (dimension 2). Modes as tile_run; `mulrow` is the CRT kernel
+/// row of the pass (modes 2 and 3 along dimension 2, mode 2 along dimension 3), while mode 3
+/// along dimension 3 multiplies by the slab's operand.
+__device__ __forceinline__ void slab_pass(const CrtSlab& S, const DevPlanHeader* P, const int64_t* tw, int64_t* s,
+                                          int dim, int mode, const int64_t* mulrow, int logv) {
+    TileIO io;
+    io.mn = S.n, io.mi = S.ninv;
+    io.me = 1, io.mv = 0;
+    if (dim == 3) {
+        io.ge = 1, io.ncol = 1;
+        for (int k = 0; k < S.dl; k++) {
+            io.g = S.data + k * S.s2;
+            io.mulp = mode == 3 ? S.op + k * S.op_s2 : mulrow;
+            tile_run(P, tw, s, S.dk, 0, true, mode, io);
+        }
+    } else {
+        const int V = 1 << logv;
+        io.ge = S.s2;
+        io.mulp = mulrow;
+        for (int c0 = 0; c0 < S.dk; c0 += V) {
+            io.g = S.data + c0;
+            io.ncol = S.dk - c0 < V ? S.dk - c0 : V;
+            tile_run(P, tw, s, S.dl, logv, true, mode, io);
+        }
+    }
+}
+
+/// Persistent batched CRT transforms: every CTA takes the next slab from `counter` and runs the
+/// slab's whole operation (period -> CRT, Montgomery product with the operand, CRT -> period, as
+/// its `ops` say) before taking another. Slabs of different fields and RNS lengths mix freely;
+/// the passes are the HAL transforms' passes in the same order (src/ring.rs:1118-1161), the
+/// operand product fused into the epilogue of the forward transform's last pass.
+__global__ void __launch_bounds__(256, HC_NTT_MIN_BLOCKS)
+    crt_batch_kernel(const CrtSlab* __restrict__ slabs, int nslabs, int* counter, int logv, int tile_words) {
+    extern __shared__ int64_t smem[];
+    __shared__ int s_next;
+    for (;;) {
+        __syncthreads();  // every thread has read s_next and left the previous slab's tiles
+        if (threadIdx.x == 0) s_next = atomicAdd(counter, 1);
+        __syncthreads();
+        const int si = s_next;
+        if (si >= nslabs) return;
+        const CrtSlab S = slabs[si];
+        const DevPlanHeader* P2 = reinterpret_cast<const DevPlanHeader*>(S.plan2);
+        const DevPlanHeader* P3 = reinterpret_cast<const DevPlanHeader*>(S.plan3);
+        int64_t* tw2 = smem + tile_words;
+        int64_t* tw3 = tw2 + 2 * P2->ntw;
+        stage_twiddles(P2, tw2);  // visible after the first barrier of the first tile
+        stage_twiddles(P3, tw3);
+        if (S.ops & HC_CRT_FORWARD) {
+            slab_pass(S, P2, tw2, smem, 2, 2, S.kl, logv);
+            slab_pass(S, P3, tw3, smem, 3, 2, S.kk, logv);
+            slab_pass(S, P2, tw2, smem, 2, 1, nullptr, logv);
+            slab_pass(S, P3, tw3, smem, 3, (S.ops & HC_CRT_MUL) ? 3 : 1, nullptr, logv);
+        } else if (S.ops & HC_CRT_MUL) {
+            const int total = S.dl * S.dk;
+            for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+                const int k = idx / S.dk, l = idx - k * S.dk;
+                int64_t* x = S.data + k * S.s2 + l;
+                *x = mul_mont(*x, S.op[k * S.op_s2 + l], S.n, S.ninv);
+            }
+            __syncthreads();
+        }
+        if (S.ops & HC_CRT_INVERSE) {
+            slab_pass(S, P2, tw2, smem, 2, 2, S.ikl, logv);
+            slab_pass(S, P3, tw3, smem, 3, 2, S.ikk, logv);
+            slab_pass(S, P2, tw2, smem, 2, 1, nullptr, logv);
+            slab_pass(S, P3, tw3, smem, 3, 1, nullptr, logv);
         }
     }
 }
@@ -710,6 +813,34 @@ hc_status destroy_plan(hc_ntt_plan p) {
 int64_t plan_modulus(hc_ntt_plan p) { return p->n; }
 int32_t plan_len(hc_ntt_plan p) { return p->len; }
 const void* plan_device(hc_ntt_plan p) { return p->dev; }
+int32_t plan_ntw(hc_ntt_plan p) { return p->ntw; }
+
+/// Launches the persistent batched-transform kernel over `nslabs` device slab descriptors.
+/// `tile_words`: largest tile (deg_K, or deg_L' x 2^logv); `tw_words`: largest pair of twiddle
+/// tables (dimension-2 + dimension-3 plan) of a slab. `counter` is reset on the stream first.
+hc_status launch_crt_batch(hc_context ctx, const CrtSlab* slabs, int nslabs, int* counter, size_t tile_words,
+                           size_t tw_words, const CrtLaunch& L) {
+    if (nslabs <= 0) return HC_OK;
+    if (L.threads < 32 || L.threads > 256 || L.threads % 32) return fail(HC_ERR_ARG, "batched transform: threads per CTA");
+    if (L.logv < 0 || L.logv > 6) return fail(HC_ERR_ARG, "batched transform: dimension-2 tile width");
+    const size_t smem = (tile_words + tw_words) * 8;
+    if (smem > max_smem_optin(ctx)) return fail(HC_ERR_UNSUPPORTED, "batched transform: slab tiles exceed shared memory");
+    cudaError_t e = cudaFuncSetAttribute(crt_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_check(e, "batched transform smem attribute");
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, crt_batch_kernel, L.threads, smem);
+    if (e != cudaSuccess) return cuda_check(e, "batched transform occupancy");
+    if (occ < 1) return fail(HC_ERR_UNSUPPORTED, "batched transform: launch shape does not fit an SM");
+    int per = L.ctas_per_sm < 1 ? 1 : (L.ctas_per_sm < occ ? L.ctas_per_sm : occ);
+    int64_t grid = (int64_t)num_sms(ctx) * per;
+    if (grid > nslabs) grid = nslabs;
+    hc_status st = cuda_check(cudaMemsetAsync(counter, 0, sizeof(int), stream_of(ctx)), "batched transform counter");
+    if (st) return st;
+    crt_batch_kernel<<<(unsigned)grid, (unsigned)L.threads, smem, stream_of(ctx)>>>(slabs, nslabs, counter, L.logv,
+                                                                                  (int)tile_words);
+    count_launch(ctx);
+    return cuda_check(cudaGetLastError(), "batched transform launch");
+}
 
 /// Launches the tile kernel for one HAL NTT call (mode 0 ntt, 1 intt, 2 ntt_mul).
 hc_status launch_ntt(hc_context ctx, const KView& t, const hc_ntt_plan* plans, size_t nplans, int dim, int mode,

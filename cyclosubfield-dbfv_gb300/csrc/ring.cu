@@ -15,6 +15,8 @@
 #include <memory>
 #include <mutex>
 #include <set>
+#include <string>
+#include <tuple>
 #include <unordered_map>
 #include <vector>
 
@@ -1554,3 +1556,214 @@ extern "C" hc_status hc_bfv_key_switch_noalloc(hc_ring R, hc_view c0, hc_view c1
         keyswitch(R, parts, keys, b, dg.size(), &c0, nullptr, out);
     });
 }
+
+// ------------------------------------------------------------------------- batched CRT transforms
+
+namespace hc {
+hc_status launch_crt_batch(hc_context ctx, const CrtSlab* slabs, int nslabs, int* counter, size_t tile_words,
+                           size_t tw_words, const CrtLaunch& L);
+const void* plan_device(hc_ntt_plan p);
+int32_t plan_ntw(hc_ntt_plan p);
+}  // namespace hc
+
+struct hc_crt_batch_s {
+    hc_context ctx = nullptr;
+    std::vector<CrtSlab> host;  // sorted: largest slabs first
+    DBuf dev;                   // the descriptors on the device
+    DBuf counter;               // next slab of the running launch
+    size_t tile_words = 0, tw_words = 0;
+    CrtLaunch launch{256, 3, 6};
+    std::string signature;      // composition of the batch, key of the autotuner's memory
+};
+
+namespace {
+
+std::mutex crt_tune_mu;
+std::map<std::string, CrtLaunch> crt_tuned;  // signature -> launch shape chosen by the autotuner
+
+/// The batch's slabs grouped by (deg_L', deg_K, ops), with their counts: batches with the same
+/// composition share a tuned launch shape.
+std::string crt_signature(const std::vector<CrtSlab>& v) {
+    std::map<std::tuple<int, int, int>, size_t> m;
+    for (const CrtSlab& s : v) m[std::make_tuple(s.dl, s.dk, s.ops)]++;
+    std::string out;
+    for (auto& kv : m) {
+        // counts rounded to powers of two: nearby batch sizes tune alike
+        size_t c = 1;
+        while (c < kv.second) c <<= 1;
+        out += std::to_string(std::get<0>(kv.first)) + "x" + std::to_string(std::get<1>(kv.first)) + "/" +
+               std::to_string(std::get<2>(kv.first)) + ":" + std::to_string(c) + ";";
+    }
+    return out;
+}
+
+size_t crt_tile_words(const CrtSlab& s, int logv) {
+    return std::max<size_t>((size_t)s.dk, (size_t)s.dl << logv);
+}
+
+}  // namespace
+
+extern "C" {
+
+hc_status hc_crt_batch_create(hc_context ctx, const hc_crt_item* items, size_t n, int ops, hc_crt_batch* out) {
+    return guard([&] {
+        REQUIRE(ctx && out && (items || n == 0), HC_ERR_ARG, "null argument");
+        REQUIRE(ops > 0 && ops <= (HC_CRT_FORWARD | HC_CRT_MUL | HC_CRT_INVERSE), HC_ERR_ARG,
+                "batched transform: ops must combine HC_CRT_FORWARD, HC_CRT_MUL, HC_CRT_INVERSE");
+        auto b = std::make_unique<hc_crt_batch_s>();
+        b->ctx = ctx;
+        for (size_t it = 0; it < n; it++) {
+            const hc_crt_item& I = items[it];
+            hc_ring R = I.ring;
+            REQUIRE(R && R->ctx == ctx, HC_ERR_ARG, "batched transform: item ring missing or of another context");
+            Base base = base_of(I.base, I.r);
+            const int64_t count = I.data.shape[0], r = (int64_t)I.r;
+            check_view(I.data, count, r, R->dl(), R->dk(), "batched transform data");
+            const bool mul = ops & HC_CRT_MUL;
+            if (mul) {
+                REQUIRE(I.op.shape[0] == count || I.op.shape[0] == 1, HC_ERR_SHAPE,
+                        "batched transform operand: one element per data element, or one for all");
+                check_view(I.op, I.op.shape[0], r, R->dl(), R->dk(), "batched transform operand");
+            }
+            if (count == 0 || r == 0) continue;
+            TransformCache& tc = R->transform_cache(base);
+            for (int64_t i = 0; i < count; i++)
+                for (int64_t j = 0; j < r; j++) {
+                    CrtSlab s;
+                    std::memset(&s, 0, sizeof(s));
+                    s.plan2 = plan_device(tc.plp[j]);
+                    s.plan3 = plan_device(tc.pk[j]);
+                    s.data = (int64_t*)I.data.ptr + i * I.data.strides[0] + j * I.data.strides[1];
+                    s.s2 = I.data.strides[2];
+                    if (mul) {
+                        s.op = (const int64_t*)I.op.ptr + (I.op.shape[0] == 1 ? 0 : i) * I.op.strides[0] +
+                               j * I.op.strides[1];
+                        s.op_s2 = I.op.strides[2];
+                    }
+                    s.kl = (const int64_t*)tc.kl.view().ptr + j * R->dl();
+                    s.kk = (const int64_t*)tc.kk.view().ptr + j * R->dk();
+                    s.ikl = (const int64_t*)tc.ikl.view().ptr + j * R->dl();
+                    s.ikk = (const int64_t*)tc.ikk.view().ptr + j * R->dk();
+                    s.n = tc.mods[j].n, s.ninv = tc.mods[j].neg_inv_n;
+                    s.dl = (int32_t)R->dl(), s.dk = (int32_t)R->dk();
+                    s.ops = ops;
+                    b->host.push_back(s);
+                    b->tw_words = std::max<size_t>(b->tw_words, 2 * (size_t)(plan_ntw(tc.plp[j]) + plan_ntw(tc.pk[j])));
+                }
+        }
+        REQUIRE(b->host.size() < (size_t)INT32_MAX, HC_ERR_UNSUPPORTED, "batched transform: too many slabs");
+        // largest slabs first: the persistent CTAs finish on the small ones
+        std::stable_sort(b->host.begin(), b->host.end(),
+                         [](const CrtSlab& x, const CrtSlab& y) { return (int64_t)x.dl * x.dk > (int64_t)y.dl * y.dk; });
+        b->signature = crt_signature(b->host);
+        {
+            std::lock_guard<std::mutex> lock(crt_tune_mu);
+            auto it = crt_tuned.find(b->signature);
+            if (it != crt_tuned.end()) b->launch = it->second;
+        }
+        if (!b->host.empty()) b->dev = DBuf(ctx, b->host.data(), b->host.size() * sizeof(CrtSlab));
+        b->counter = DBuf(ctx, sizeof(int));
+        *out = b.release();
+    });
+}
+
+hc_status hc_crt_batch_run(hc_crt_batch b) {
+    return guard([&] {
+        REQUIRE(b, HC_ERR_ARG, "null batch");
+        size_t tile = 0;
+        for (const CrtSlab& s : b->host) tile = std::max(tile, crt_tile_words(s, b->launch.logv));
+        CK(launch_crt_batch(b->ctx, b->dev.as<CrtSlab>(), (int)b->host.size(), b->counter.as<int>(), tile, b->tw_words,
+                            b->launch));
+    });
+}
+
+hc_status hc_crt_batch_set_launch(hc_crt_batch b, const hc_crt_launch* l) {
+    return guard([&] {
+        REQUIRE(b && l, HC_ERR_ARG, "null argument");
+        REQUIRE(l->threads >= 32 && l->threads <= 256 && l->threads % 32 == 0, HC_ERR_ARG, "threads per CTA");
+        REQUIRE(l->ctas_per_sm >= 1 && l->logv >= 0 && l->logv <= 6, HC_ERR_ARG, "launch shape");
+        b->launch = CrtLaunch{l->threads, l->ctas_per_sm, l->logv};
+    });
+}
+
+hc_status hc_crt_batch_get_launch(hc_crt_batch b, hc_crt_launch* out) {
+    return guard([&] {
+        REQUIRE(b && out, HC_ERR_ARG, "null argument");
+        out->threads = b->launch.threads, out->ctas_per_sm = b->launch.ctas_per_sm, out->logv = b->launch.logv;
+    });
+}
+
+size_t hc_crt_batch_num_slabs(hc_crt_batch b) { return b ? b->host.size() : 0; }
+
+hc_status hc_crt_batch_tune(hc_crt_batch b, int reps, hc_crt_launch* chosen) {
+    return guard([&] {
+        REQUIRE(b, HC_ERR_ARG, "null batch");
+        if (reps < 1) reps = 1;
+        if (!b->host.empty()) {
+            hc_context ctx = b->ctx;
+            cudaStream_t st = stream_of(ctx);
+            // a sample of at most 1024 slabs, every k-th, each given its own rows in a scratch
+            // buffer (the operands stay the batch's own, they are only read)
+            const size_t k = (b->host.size() + 1023) / 1024;
+            std::vector<CrtSlab> sample;
+            size_t words = 0;
+            for (size_t i = 0; i < b->host.size(); i += k) {
+                sample.push_back(b->host[i]);
+                words += (size_t)b->host[i].dl * b->host[i].dk;
+            }
+            DBuf scratch(ctx, words * 8);
+            CK(cuda_check(cudaMemsetAsync(scratch.p, 0, words * 8, st), "tuning scratch"));
+            size_t off = 0;
+            for (CrtSlab& s : sample) {
+                s.data = scratch.as<int64_t>() + off;
+                s.s2 = s.dk;
+                off += (size_t)s.dl * s.dk;
+            }
+            DBuf sdev(ctx, sample.data(), sample.size() * sizeof(CrtSlab));
+            DBuf cnt(ctx, sizeof(int));
+            cudaEvent_t e0, e1;
+            CK(cuda_check(cudaEventCreate(&e0), "tuning event"));
+            CK(cuda_check(cudaEventCreate(&e1), "tuning event"));
+            CrtLaunch best = b->launch;
+            float best_ms = -1;
+            const int threads[] = {128, 256};
+            const int per_sm[] = {1, 2, 3, 4};
+            const int logvs[] = {4, 5, 6};
+            for (int th : threads)
+                for (int ps : per_sm)
+                    for (int lv : logvs) {
+                        CrtLaunch L{th, ps, lv};
+                        size_t tile = 0;
+                        for (const CrtSlab& s : sample) tile = std::max(tile, crt_tile_words(s, lv));
+                        hc_status rc = launch_crt_batch(ctx, sdev.as<CrtSlab>(), (int)sample.size(), cnt.as<int>(),
+                                                        tile, b->tw_words, L);
+                        if (rc == HC_ERR_UNSUPPORTED) continue;  // shape does not fit an SM
+                        CK(rc);
+                        cudaEventRecord(e0, st);
+                        for (int r = 0; r < reps; r++)
+                            CK(launch_crt_batch(ctx, sdev.as<CrtSlab>(), (int)sample.size(), cnt.as<int>(), tile,
+                                                b->tw_words, L));
+                        cudaEventRecord(e1, st);
+                        CK(cuda_check(cudaEventSynchronize(e1), "tuning run"));
+                        float ms = 0;
+                        cudaEventElapsedTime(&ms, e0, e1);
+                        if (best_ms < 0 || ms < best_ms) best_ms = ms, best = L;
+                    }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            CK(cuda_check(cudaStreamSynchronize(st), "tuning"));
+            b->launch = best;
+            std::lock_guard<std::mutex> lock(crt_tune_mu);
+            crt_tuned[b->signature] = best;
+        }
+        if (chosen) chosen->threads = b->launch.threads, chosen->ctas_per_sm = b->launch.ctas_per_sm,
+                    chosen->logv = b->launch.logv;
+    });
+}
+
+hc_status hc_crt_batch_destroy(hc_crt_batch b) {
+    delete b;
+    return HC_OK;
+}
+
+}  // extern "C"

@@ -242,3 +242,78 @@ class RingContext:
         check(lib().hc_bfv_hom_gal(self.h, ct.view(), _sz(base), ctypes.c_size_t(len(base)), garr,
                                    ctypes.c_size_t(len(gs)), gks.view(), dg, nd, out.view()))
         return out
+
+
+CRT_FORWARD, CRT_MUL, CRT_INVERSE = 1, 2, 4
+
+
+class _CrtItem(ctypes.Structure):
+    _fields_ = [("ring", ctypes.c_void_p), ("data", halcuda.HcView), ("op", halcuda.HcView),
+                ("base", ctypes.POINTER(ctypes.c_size_t)), ("r", ctypes.c_size_t)]
+
+
+class CrtLaunch(ctypes.Structure):
+    _fields_ = [("threads", ctypes.c_int), ("ctas_per_sm", ctypes.c_int), ("logv", ctypes.c_int)]
+
+    def as_tuple(self):
+        return (self.threads, self.ctas_per_sm, self.logv)
+
+
+class CrtBatch:
+    """hc_crt_batch: batched CRT transforms of (ring, data, op, base) items in one persistent
+    launch; `ops` combines CRT_FORWARD, CRT_MUL and CRT_INVERSE. The tensors and rings must outlive
+    the batch."""
+
+    def __init__(self, items, ops, backend=None):
+        if not items:
+            raise ValueError("empty batch")
+        self.backend = backend or items[0][0].backend
+        # the batch holds device pointers into the items' tensors and rings: keep them alive
+        self._items = list(items)
+        self._keep = []
+        arr = (_CrtItem * len(items))()
+        for it, (ring, data, op, base) in enumerate(items):
+            b = _sz(base)
+            self._keep.append(b)
+            arr[it].ring = ring.h
+            arr[it].data = data.view()
+            arr[it].op = op.view() if op is not None else _null_view()
+            arr[it].base = ctypes.cast(b, ctypes.POINTER(ctypes.c_size_t))
+            arr[it].r = len(base)
+        h = ctypes.c_void_p()
+        check(lib().hc_crt_batch_create(self.backend.h, arr, ctypes.c_size_t(len(items)), ctypes.c_int(ops),
+                                        ctypes.byref(h)))
+        self.h = h
+        self.backend.add_dependent(self)
+        lib().hc_crt_batch_num_slabs.restype = ctypes.c_size_t
+        lib().hc_crt_batch_num_slabs.argtypes = [ctypes.c_void_p]
+        self.num_slabs = int(lib().hc_crt_batch_num_slabs(h))
+
+    def run(self):
+        check(lib().hc_crt_batch_run(self.h))
+
+    def tune(self, reps=3):
+        out = CrtLaunch()
+        check(lib().hc_crt_batch_tune(self.h, ctypes.c_int(reps), ctypes.byref(out)))
+        return out.as_tuple()
+
+    @property
+    def launch(self):
+        out = CrtLaunch()
+        check(lib().hc_crt_batch_get_launch(self.h, ctypes.byref(out)))
+        return out.as_tuple()
+
+    @launch.setter
+    def launch(self, shape):
+        check(lib().hc_crt_batch_set_launch(self.h, ctypes.byref(CrtLaunch(*shape))))
+
+    def close(self):
+        if self.h and self.backend.h:
+            lib().hc_crt_batch_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -99,6 +99,42 @@ hc_status hc_bfv_hom_mul(hc_ring ring, const int64_t t[2], hc_view ct1, hc_view 
 hc_status hc_bfv_hom_gal(hc_ring ring, hc_view ct, const size_t* base, size_t r, const uint64_t* gs, size_t ngs,
                          hc_view gks, const size_t* digits, size_t d, hc_view out);
 
+/* Batched CRT transforms of many ring elements of different fields and RNS lengths in one
+ * persistent launch. Each item is a tensor of elements of one ring over one base; per element
+ * and factor ("slab") the batch runs, as `ops` says, pb_to_crt (src/ring.rs:1118-1138), a
+ * Montgomery product with the item's operand (hal_mul_mont64, src/hal/cpu.rs:823-836) and
+ * crt_to_pb (:1140-1161), in place and bit-identical to those calls made one by one. The batch
+ * keeps device pointers to the items' tensors and to the rings' tables: both must outlive it.
+ * Running it issues a counter reset and one kernel on the context's stream (graph-capturable). */
+#define HC_CRT_FORWARD 1 /* period basis -> CRT basis (input bound 2) */
+#define HC_CRT_MUL 2     /* Montgomery product with `op` (CRT basis) */
+#define HC_CRT_INVERSE 4 /* CRT basis -> period basis */
+typedef struct hc_crt_batch_s* hc_crt_batch;
+typedef struct {
+    hc_ring ring;
+    hc_view data;        /* [count, r, deg_L', deg_K], transformed in place */
+    hc_view op;          /* [count | 1, r, deg_L', deg_K] for HC_CRT_MUL, else ptr NULL */
+    const size_t* base;  /* r factor indices of the ring */
+    size_t r;
+} hc_crt_item;
+/* Launch shape of the persistent kernel: threads per CTA (32..256), CTAs per SM, and 2^logv
+ * columns per dimension-2 tile (logv 0..6). */
+typedef struct {
+    int threads;
+    int ctas_per_sm;
+    int logv;
+} hc_crt_launch;
+hc_status hc_crt_batch_create(hc_context ctx, const hc_crt_item* items, size_t n, int ops, hc_crt_batch* out);
+hc_status hc_crt_batch_run(hc_crt_batch b);
+/* Autotuner: times every launch shape of a fixed candidate set on a scratch copy of (a sample of)
+ * the batch's slabs - the transforms are data-oblivious - and keeps the fastest; the choice is
+ * remembered for batches of the same composition. Synchronises; not during stream capture. */
+hc_status hc_crt_batch_tune(hc_crt_batch b, int reps, hc_crt_launch* chosen);
+hc_status hc_crt_batch_set_launch(hc_crt_batch b, const hc_crt_launch* l);
+hc_status hc_crt_batch_get_launch(hc_crt_batch b, hc_crt_launch* out);
+size_t hc_crt_batch_num_slabs(hc_crt_batch b);
+hc_status hc_crt_batch_destroy(hc_crt_batch b);
+
 /* No counterpart in the reference (its CPU backend allocates freely): hc_bfv_key_switch with the
  * same arguments and the same result, for callers that cannot allocate device memory - a host
  * whose HBM is handed out by its own arena or budget, or a code path where cudaMalloc / cudaFree
