@@ -57,20 +57,28 @@ __device__ __forceinline__ int64_t wsub(int64_t a, int64_t b) { return (int64_t)
 
 /// Barrett multiplication by the constant (z, u): q = floor((u x + 2^63) / 2^64), result
 /// z x + q n in wrapping 64-bit arithmetic (|result| <= 3n/4 for |x| <= 2^63).
-/// The signed 128-bit product u x is assembled from the four 32 x 32 -> 64 partial products of
-/// the unsigned operands (each a single wide multiply-add) and corrected for the signs in its
-/// high word: u x = U X - 2^64 ([u < 0] X + [x < 0] U). Bit 63 of the low word, the rounding
-/// bit of the "+ 2^63", is bit 31 of the second partial sum.
+/// The high word of the unsigned 128-bit product U X is accumulated from 32-bit limbs with one
+/// carry chain; the signed product follows from u x = U X - 2^64 ([u < 0] X + [x < 0] U), and the
+/// rounding bit of "+ 2^63" is bit 63 of the low word (bit 31 of its upper limb).
 __device__ __forceinline__ int64_t bmul(int64_t z, int64_t u, int64_t x, int64_t n) {
-    const uint64_t uu = (uint64_t)u, xx = (uint64_t)x;
-    const uint32_t u0 = (uint32_t)uu, u1 = (uint32_t)(uu >> 32), x0 = (uint32_t)xx, x1 = (uint32_t)(xx >> 32);
-    const uint64_t p00 = (uint64_t)u0 * x0;
-    const uint64_t mid = (uint64_t)u0 * x1 + (p00 >> 32);
-    const uint64_t mid2 = (uint64_t)u1 * x0 + (uint32_t)mid;
-    uint64_t hi = (uint64_t)u1 * x1 + (mid >> 32) + (mid2 >> 32);
-    hi -= (u < 0 ? xx : 0) + (x < 0 ? uu : 0);
-    const int64_t q = (int64_t)hi + (int64_t)((mid2 >> 31) & 1);
-    return (int64_t)((uint64_t)z * xx + (uint64_t)q * (uint64_t)n);
+    const uint32_t u0 = (uint32_t)u, u1 = (uint32_t)((uint64_t)u >> 32);
+    const uint32_t x0 = (uint32_t)x, x1 = (uint32_t)((uint64_t)x >> 32);
+    uint32_t r1, r2, r3;
+    asm("{\n\t"
+        "mul.hi.u32 %0, %3, %5;\n\t"
+        "mad.lo.cc.u32 %0, %3, %6, %0;\n\t"
+        "madc.hi.u32 %1, %3, %6, 0;\n\t"
+        "mad.lo.cc.u32 %0, %4, %5, %0;\n\t"
+        "madc.hi.cc.u32 %1, %4, %5, %1;\n\t"
+        "madc.hi.u32 %2, %4, %6, 0;\n\t"
+        "mad.lo.cc.u32 %1, %4, %6, %1;\n\t"
+        "addc.u32 %2, %2, 0;\n\t"
+        "}"
+        : "=&r"(r1), "=&r"(r2), "=&r"(r3)
+        : "r"(u0), "r"(u1), "r"(x0), "r"(x1));
+    const uint64_t mx = (uint64_t)(x >> 63), mu = (uint64_t)(u >> 63);
+    const uint64_t q = ((((uint64_t)r3 << 32) | r2) - ((uint64_t)u & mx) - ((uint64_t)x & mu)) + (r1 >> 31);
+    return (int64_t)((uint64_t)z * (uint64_t)x + q * (uint64_t)n);
 }
 
 /// Montgomery reduction of the 128-bit value hi:lo: ((x + m n) >> 64) with m = lo * (-n^-1).
@@ -137,7 +145,7 @@ struct CrtSlab {
     int64_t n, ninv;       // Montgomery modulus of the factor
     int32_t dl, dk;
     int32_t ops;           // HC_CRT_* bits
-    int32_t pad;
+    int32_t shapes;        // specialised kernel shapes: dimension 3 | dimension 2 << 8 (0: generic)
 };
 
 /// Launch shape of the persistent batched-transform kernel (chosen by the autotuner).

@@ -133,6 +133,7 @@ struct hc_ntt_plan_s {
     int64_t n;
     int32_t len;
     int32_t ntw;      // twiddle pairs
+    int32_t shape;    // HC_SHAPE_*: factorisation with a specialised kernel
     size_t bytes;
 };
 
@@ -495,6 +496,129 @@ __device__ __forceinline__ void stage_twiddles(const DevPlanHeader* P, int64_t* 
     for (int idx = threadIdx.x; idx < 2 * P->ntw; idx += blockDim.x) dst[idx] = twg[idx];
 }
 
+}  // namespace
+
+#include "ntt_fast.cuh"
+
+namespace {
+
+#define HC_SHAPE_GENERIC 0
+#define HC_SHAPE_L3072 1   // dimension-3 line [2, 3, 8, 64]
+#define HC_SHAPE_L12288 2  // dimension-3 line [3, 64, 64]
+#define HC_SHAPE_C12 3     // dimension-2 column [4, 3]
+#define HC_SHAPE_C4 4      // dimension-2 column [4]
+
+__host__ __device__ constexpr int line_len(int shape) { return shape == HC_SHAPE_L3072 ? 3072 : 12288; }
+__host__ __device__ constexpr int line_tile_words(int shape) { return line_len(shape) + line_len(shape) / 8; }
+
+__device__ __forceinline__ fast::Ctx make_ctx(const DevPlanHeader* P, const int64_t* tw) {
+    fast::Ctx c;
+    c.n = P->n, c.one_z = P->one_z, c.one_u = P->one_u, c.il_z = P->invlen_z, c.il_u = P->invlen_u;
+    c.tw = tw;
+    return c;
+}
+
+/// One specialised line of shape SHAPE (twiddles already staged, barrier passed).
+template <int SHAPE>
+__device__ __forceinline__ void run_line(const DevPlanHeader* P, const fast::Ctx& c, int64_t* s, int64_t* g, int mode,
+                                         const int64_t* mulp, int64_t me, int64_t mn, int64_t mi) {
+    if (SHAPE == HC_SHAPE_L3072) fast::line3072(P, c, s, g, mode, mulp, me, mn, mi);
+    else fast::line12288(P, c, s, g, mode, mulp, me, mn, mi);
+}
+
+/// Specialised dimension-3 NTT: one line (i, j, k) per CTA.
+template <int SHAPE, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) ntt_line_kernel(KView t, PlanPtrs plans, int mode, KView mul,
+                                                                 KMods mods) {
+    extern __shared__ int64_t smem[];
+    const int64_t tile = blockIdx.x;
+    const int64_t k = tile % t.n2, r = tile / t.n2;
+    const int64_t j = r % t.n1, i = r / t.n1;
+    const DevPlanHeader* P = plans.p[j];
+    int64_t* tws = smem + line_tile_words(SHAPE);
+    stage_twiddles(P, tws);
+    __syncthreads();
+    const fast::Ctx c = make_ctx(P, tws);
+    int64_t* g = reinterpret_cast<int64_t*>(t.p) + i * t.s0 + j * t.s1 + k * t.s2;
+    const int64_t* mulp = nullptr;
+    int64_t me = 0, mn = 0, mi = 0;
+    if (mode == 2) {
+        mulp = kat<int64_t>(mul, i, j, k, 0);
+        me = mul.b3 ? 0 : 1;
+        mn = mods.n[j], mi = mods.ninv[j];
+    }
+    run_line<SHAPE>(P, c, smem, g, mode, mulp, me, mn, mi);
+}
+
+/// One specialised column (global element stride ge) of shape SHAPE, in registers.
+template <int SHAPE>
+__device__ __forceinline__ void run_column(const DevPlanHeader* P, const fast::Ctx& c, int64_t* g, int64_t ge, int mode,
+                                           const int64_t* mulp, int64_t mstride, int64_t mn, int64_t mi) {
+    const bool inv = mode & 1;
+    const DevStage* st = inv ? P->inv : P->fwd;
+    if (SHAPE == HC_SHAPE_C12) {
+        fast::SF f[3];
+#pragma unroll
+        for (int q = 0; q < 3; q++) f[q] = fast::sflags(st[q]);
+        int64_t x[4][3];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 3; b++) x[a][b] = g[(3 * a + b) * ge];
+        fast::col12(c, f, inv, mode == 0, x);
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 3; b++) {
+                int64_t v = x[a][b];
+                if (mode & 2) v = mul_mont(v, mulp[(3 * a + b) * mstride], mn, mi);
+                g[(3 * a + b) * ge] = v;
+            }
+    } else {
+        fast::SF f[2];
+        f[0] = fast::sflags(st[0]);
+        f[1] = fast::sflags(st[1]);
+        int64_t x[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) x[a] = g[a * ge];
+        fast::col4(c, f, inv, mode == 0, x);
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            int64_t v = x[a];
+            if (mode & 2) v = mul_mont(v, mulp[a * mstride], mn, mi);
+            g[a * ge] = v;
+        }
+    }
+}
+
+#define HC_COL_THREADS 256
+#define HC_COL_TW 128  // twiddle words a column plan may have (checked at dispatch)
+
+/// Specialised dimension-2 NTT: one thread per column (i, j, l), CTAs over (i, j, column block).
+template <int SHAPE>
+__global__ void __launch_bounds__(HC_COL_THREADS, 3) ntt_col_kernel(KView t, PlanPtrs plans, int mode, KView mul,
+                                                                 KMods mods, int ncb) {
+    __shared__ __align__(16) int64_t tws[HC_COL_TW];
+    const int64_t tile = blockIdx.x;
+    const int64_t cb = tile % ncb, r = tile / ncb;
+    const int64_t j = r % t.n1, i = r / t.n1;
+    const DevPlanHeader* P = plans.p[j];
+    stage_twiddles(P, tws);
+    __syncthreads();
+    const int64_t l = cb * HC_COL_THREADS + threadIdx.x;
+    if (l >= t.n3) return;
+    const fast::Ctx c = make_ctx(P, tws);
+    int64_t* g = reinterpret_cast<int64_t*>(t.p) + i * t.s0 + j * t.s1 + l;
+    const int64_t* mulp = nullptr;
+    int64_t ms = 0, mn = 0, mi = 0;
+    if (mode == 2) {
+        mulp = kat<int64_t>(mul, i, j, 0, l);
+        ms = mul.s2;
+        mn = mods.n[j], mi = mods.ninv[j];
+    }
+    run_column<SHAPE>(P, c, g, t.s2, mode, mulp, ms, mn, mi);
+}
+
 /// mode 0: forward (reduced), 1: inverse, 2: forward unreduced + Montgomery multiplication by `mul`.
 /// dim 3: tile = line (i, j, k), element e at l = e.  dim 2: tile = (i, j, column block),
 /// element (e, v) at k = e, l = cb * V + v.
@@ -540,6 +664,27 @@ __global__ void __launch_bounds__(256, HC_NTT_MIN_BLOCKS) ntt_tile_kernel(KView 
 /// along dimension 3 multiplies by the slab's operand.
 __device__ __forceinline__ void slab_pass(const CrtSlab& S, const DevPlanHeader* P, const int64_t* tw, int64_t* s,
                                           int dim, int mode, const int64_t* mulrow, int logv) {
+    const int shape = dim == 3 ? (S.shapes & 0xff) : (S.shapes >> 8);
+    if (dim == 3 && (shape == HC_SHAPE_L3072 || shape == HC_SHAPE_L12288)) {
+        const fast::Ctx c = make_ctx(P, tw);
+        for (int k = 0; k < S.dl; k++) {
+            int64_t* g = S.data + k * S.s2;
+            const int64_t* mulp = mode == 3 ? S.op + k * S.op_s2 : mulrow;
+            if (shape == HC_SHAPE_L3072) run_line<HC_SHAPE_L3072>(P, c, s, g, mode, mulp, 1, S.n, S.ninv);
+            else run_line<HC_SHAPE_L12288>(P, c, s, g, mode, mulp, 1, S.n, S.ninv);
+            __syncthreads();
+        }
+        return;
+    }
+    if (dim == 2 && (shape == HC_SHAPE_C12 || shape == HC_SHAPE_C4)) {
+        const fast::Ctx c = make_ctx(P, tw);
+        for (int l = threadIdx.x; l < S.dk; l += blockDim.x) {
+            if (shape == HC_SHAPE_C12) run_column<HC_SHAPE_C12>(P, c, S.data + l, S.s2, mode, mulrow, 1, S.n, S.ninv);
+            else run_column<HC_SHAPE_C4>(P, c, S.data + l, S.s2, mode, mulrow, 1, S.n, S.ninv);
+        }
+        __syncthreads();
+        return;
+    }
     TileIO io;
     io.mn = S.n, io.mi = S.ninv;
     io.me = 1, io.mv = 0;
@@ -582,8 +727,9 @@ __global__ void __launch_bounds__(256, HC_NTT_MIN_BLOCKS)
         const DevPlanHeader* P3 = reinterpret_cast<const DevPlanHeader*>(S.plan3);
         int64_t* tw2 = smem + tile_words;
         int64_t* tw3 = tw2 + 2 * P2->ntw;
-        stage_twiddles(P2, tw2);  // visible after the first barrier of the first tile
+        stage_twiddles(P2, tw2);
         stage_twiddles(P3, tw3);
+        __syncthreads();
         if (S.ops & HC_CRT_FORWARD) {
             slab_pass(S, P2, tw2, smem, 2, 2, S.kl, logv);
             slab_pass(S, P3, tw3, smem, 3, 2, S.kk, logv);
@@ -794,6 +940,11 @@ hc_status build_plan(hc_context ctx, const hc_modulus* m, const size_t* shape, s
         return st;
     }
     auto* plan = new hc_ntt_plan_s();
+    plan->shape = HC_SHAPE_GENERIC;
+    if (factors == std::vector<size_t>{2, 3, 8, 64}) plan->shape = HC_SHAPE_L3072;
+    else if (factors == std::vector<size_t>{3, 64, 64}) plan->shape = HC_SHAPE_L12288;
+    else if (factors == std::vector<size_t>{4, 3}) plan->shape = HC_SHAPE_C12;
+    else if (factors == std::vector<size_t>{4}) plan->shape = HC_SHAPE_C4;
     plan->dev = dev;
     plan->n = n;
     plan->len = (int32_t)len;
@@ -814,6 +965,10 @@ int64_t plan_modulus(hc_ntt_plan p) { return p->n; }
 int32_t plan_len(hc_ntt_plan p) { return p->len; }
 const void* plan_device(hc_ntt_plan p) { return p->dev; }
 int32_t plan_ntw(hc_ntt_plan p) { return p->ntw; }
+int32_t plan_shape(hc_ntt_plan p) { return p->shape; }
+int32_t plan_tile_words(hc_ntt_plan p) {
+    return p->shape == HC_SHAPE_L3072 || p->shape == HC_SHAPE_L12288 ? line_tile_words(p->shape) : 0;
+}
 
 /// Launches the persistent batched-transform kernel over `nslabs` device slab descriptors.
 /// `tile_words`: largest tile (deg_K, or deg_L' x 2^logv); `tw_words`: largest pair of twiddle
@@ -857,6 +1012,45 @@ hc_status launch_ntt(hc_context ctx, const KView& t, const hc_ntt_plan* plans, s
         max_tw = std::max(max_tw, plans[j]->ntw);
     }
     if (t.n0 == 0 || t.n1 == 0 || t.n2 == 0 || t.n3 == 0) return HC_OK;
+    int shape = plans[0]->shape;
+    for (size_t j = 1; j < nplans; j++)
+        if (plans[j]->shape != shape) shape = HC_SHAPE_GENERIC;
+    if (dim == 3 && (shape == HC_SHAPE_L3072 || shape == HC_SHAPE_L12288)) {
+        const size_t smem = ((size_t)line_tile_words(shape) + 2 * (size_t)max_tw) * 8;
+        const int64_t tiles = t.n0 * t.n1 * t.n2;
+        if (smem <= max_smem_optin(ctx) && tiles <= 0x7fffffff) {
+            cudaError_t e;
+            if (shape == HC_SHAPE_L3072) {
+                e = cudaFuncSetAttribute(ntt_line_kernel<HC_SHAPE_L3072, 128, 6>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (e != cudaSuccess) return cuda_check(e, "ntt smem attribute");
+                ntt_line_kernel<HC_SHAPE_L3072, 128, 6>
+                    <<<(unsigned)tiles, 128, smem, stream_of(ctx)>>>(t, pp, mode, mul, mods);
+            } else {
+                e = cudaFuncSetAttribute(ntt_line_kernel<HC_SHAPE_L12288, 256, 2>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (e != cudaSuccess) return cuda_check(e, "ntt smem attribute");
+                ntt_line_kernel<HC_SHAPE_L12288, 256, 2>
+                    <<<(unsigned)tiles, 256, smem, stream_of(ctx)>>>(t, pp, mode, mul, mods);
+            }
+            count_launch(ctx);
+            return cuda_check(cudaGetLastError(), "ntt kernel launch");
+        }
+    }
+    if (dim == 2 && (shape == HC_SHAPE_C12 || shape == HC_SHAPE_C4) && 2 * max_tw <= HC_COL_TW) {
+        const int64_t ncb = (t.n3 + HC_COL_THREADS - 1) / HC_COL_THREADS;
+        const int64_t tiles = t.n0 * t.n1 * ncb;
+        if (tiles <= 0x7fffffff) {
+            if (shape == HC_SHAPE_C12)
+                ntt_col_kernel<HC_SHAPE_C12>
+                    <<<(unsigned)tiles, HC_COL_THREADS, 0, stream_of(ctx)>>>(t, pp, mode, mul, mods, (int)ncb);
+            else
+                ntt_col_kernel<HC_SHAPE_C4>
+                    <<<(unsigned)tiles, HC_COL_THREADS, 0, stream_of(ctx)>>>(t, pp, mode, mul, mods, (int)ncb);
+            count_launch(ctx);
+            return cuda_check(cudaGetLastError(), "ntt kernel launch");
+        }
+    }
     int V = 1, logv = 0;
     int64_t ntile2 = 1;
     if (dim == 2) {

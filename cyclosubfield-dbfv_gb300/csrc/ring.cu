@@ -1564,6 +1564,7 @@ hc_status launch_crt_batch(hc_context ctx, const CrtSlab* slabs, int nslabs, int
                            size_t tw_words, const CrtLaunch& L);
 const void* plan_device(hc_ntt_plan p);
 int32_t plan_ntw(hc_ntt_plan p);
+int32_t plan_shape(hc_ntt_plan p);
 }  // namespace hc
 
 struct hc_crt_batch_s {
@@ -1597,8 +1598,12 @@ std::string crt_signature(const std::vector<CrtSlab>& v) {
     return out;
 }
 
+/// Shared-memory tile of a slab: a padded line for the specialised line kernels, else the
+/// larger of a line and a column block; rounded to an even word count (16-byte aligned twiddles).
 size_t crt_tile_words(const CrtSlab& s, int logv) {
-    return std::max<size_t>((size_t)s.dk, (size_t)s.dl << logv);
+    size_t w = std::max<size_t>((size_t)s.dk, (size_t)s.dl << logv);
+    if ((s.shapes & 0xff) != 0) w = std::max<size_t>(w, (size_t)s.dk + (size_t)s.dk / 8);
+    return (w + 1) & ~(size_t)1;
 }
 
 }  // namespace
@@ -1647,6 +1652,7 @@ hc_status hc_crt_batch_create(hc_context ctx, const hc_crt_item* items, size_t n
                     s.n = tc.mods[j].n, s.ninv = tc.mods[j].neg_inv_n;
                     s.dl = (int32_t)R->dl(), s.dk = (int32_t)R->dk();
                     s.ops = ops;
+                    s.shapes = plan_shape(tc.pk[j]) | (plan_shape(tc.plp[j]) << 8);
                     b->host.push_back(s);
                     b->tw_words = std::max<size_t>(b->tw_words, 2 * (size_t)(plan_ntw(tc.plp[j]) + plan_ntw(tc.pk[j])));
                 }

@@ -171,6 +171,10 @@ def test_montgomery_family(be, po, primes36864):
     assert (d.to_numpy() == exp).all()
 
 
+# primes = 1 mod 192 of 40, 47, 52, 55, 58, 60, 61 and 61.4 bits
+FAST_PRIMES = [1099511625409, 140737488355201, 4503599627367553, 36028797018963841, 288230376151711681,
+               1152921504606844417, 2305843009213692097, 3074457345618256321]
+
 NTT_CASES = [
     # (primes fixture or list, inner shape, tensor shape, dim)
     ("36864", [4, 3], (2, 16, 12, 3072), 2),
@@ -189,6 +193,14 @@ NTT_CASES = [
     ([Q62, Q62], [16, 2], (2, 2, 32, 3), 2),
     ([Q61], [27, 1], (2, 1, 4, 27), 3),
     ([Q61], [81], (1, 1, 81, 70), 2),
+] + [
+    # the factorisations with specialised kernels, over primes of 40..61.4 bits: the reduction
+    # and skip schedule of the plan differs with the prime's size
+    (FAST_PRIMES, [2, 3, 8, 64], (1, 8, 12, 3072), 3),
+    (FAST_PRIMES, [4, 3], (2, 8, 12, 3072), 2),
+    (FAST_PRIMES, [3, 64, 64], (1, 8, 4, 12288), 3),
+    (FAST_PRIMES, [4], (1, 8, 4, 12288), 2),
+    (FAST_PRIMES[:3], [4, 3], (1, 3, 12, 300), 2),
 ]
 
 
@@ -215,6 +227,23 @@ def test_ntt_family(be, po, case, primes36864, primes49152):
             be.hal_ntt_mul_mont64_dim(d, plans, dim, be.tensor(kern), M)
         got = d.to_numpy()
         assert (got == exp).all(), (mode, np.argwhere(got != exp)[:5])
+
+
+@pytest.mark.parametrize("inner,shape,dim", [([2, 3, 8, 64], (2, 4, 12, 3072), 3), ([4, 3], (2, 4, 12, 3072), 2),
+                                             ([3, 64, 64], (1, 4, 4, 12288), 3), ([4], (2, 4, 4, 12288), 2)])
+def test_ntt_mul_full_operand(be, po, inner, shape, dim, primes36864, primes49152):
+    """ntt_mul with a multiplier of the full tensor shape (no broadcasting) on the specialised shapes."""
+    pr = list((primes36864 if shape[3] == 3072 else primes49152)[:shape[1]])
+    g = rng(17)
+    data = residues(g, shape, pr, bound=2)
+    kern = residues(g, shape, pr)
+    M = mods(be, pr)
+    plans = [be.hal_create_ntt_plan(m, inner) for m in M]
+    exp = data.copy()
+    po.ntt_dim(exp, pr, inner, dim, "ntt_mul", kern)
+    d = be.tensor(data)
+    be.hal_ntt_mul_mont64_dim(d, plans, dim, be.tensor(kern), M)
+    assert (d.to_numpy() == exp).all()
 
 
 def test_ntt_strided_view(be, po, primes36864):
