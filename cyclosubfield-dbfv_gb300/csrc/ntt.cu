@@ -134,6 +134,7 @@ struct hc_ntt_plan_s {
     int32_t len;
     int32_t ntw;      // twiddle pairs
     int32_t shape;    // HC_SHAPE_*: factorisation with a specialised kernel
+    bool fixed;       // the plan's schedule is the shape's compiled-in schedule
     size_t bytes;
 };
 
@@ -518,18 +519,42 @@ __device__ __forceinline__ fast::Ctx make_ctx(const DevPlanHeader* P, const int6
     return c;
 }
 
-/// One specialised line of shape SHAPE (twiddles already staged, barrier passed).
-template <int SHAPE>
-__device__ __forceinline__ void run_line(const DevPlanHeader* P, const fast::Ctx& c, int64_t* s, int64_t* g, int mode,
+/// The reduction / skip / fused-final schedule that the plans of primes just below 2^57 have
+/// (the primes the rings sample), per shape and direction: bit s = the flag of stage s.
+struct SchedMasks {
+    uint32_t fred, fskip, flast, ired, ilast;
+};
+__host__ __device__ constexpr SchedMasks fixed_masks(int shape) {
+    return shape == HC_SHAPE_L3072    ? SchedMasks{0u, 0xFu, 1u << 10, 0x410u, 1u << 10}
+           : shape == HC_SHAPE_L12288 ? SchedMasks{0u, 0xFu, 1u << 12, 0x410u, 1u << 12}
+           : shape == HC_SHAPE_C12    ? SchedMasks{0u, 0x7u, 1u << 2, 0u, 1u << 2}
+           : shape == HC_SHAPE_C4     ? SchedMasks{0u, 0x3u, 1u << 1, 0u, 1u << 1}
+                                      : SchedMasks{0u, 0u, 0u, 0u, 0u};
+}
+template <int SHAPE, bool INV>
+using FixedSched = fast::FixSched<INV ? fixed_masks(SHAPE).ired : fixed_masks(SHAPE).fred,
+                                  INV ? 0u : fixed_masks(SHAPE).fskip,
+                                  INV ? fixed_masks(SHAPE).ilast : fixed_masks(SHAPE).flast>;
+
+/// One specialised line (twiddles staged, barrier passed); FIX: the plan has the fixed schedule.
+template <int SHAPE, int MODE, bool FIX>
+__device__ __forceinline__ void run_line(const DevPlanHeader* P, const fast::Ctx& c, int64_t* s, int64_t* g,
                                          const int64_t* mulp, int64_t me, int64_t mn, int64_t mi) {
-    if (SHAPE == HC_SHAPE_L3072) fast::line3072(P, c, s, g, mode, mulp, me, mn, mi);
-    else fast::line12288(P, c, s, g, mode, mulp, me, mn, mi);
+    const DevStage* st = (MODE & 1) ? P->inv : P->fwd;
+    if constexpr (FIX) {
+        const FixedSched<SHAPE, (MODE & 1) != 0> sch{st};
+        if constexpr (SHAPE == HC_SHAPE_L3072) fast::line3072<MODE>(sch, c, s, g, mulp, me, mn, mi);
+        else fast::line12288<MODE>(sch, c, s, g, mulp, me, mn, mi);
+    } else {
+        const fast::DynSched sch{st};
+        if constexpr (SHAPE == HC_SHAPE_L3072) fast::line3072<MODE>(sch, c, s, g, mulp, me, mn, mi);
+        else fast::line12288<MODE>(sch, c, s, g, mulp, me, mn, mi);
+    }
 }
 
 /// Specialised dimension-3 NTT: one line (i, j, k) per CTA.
-template <int SHAPE, int THREADS, int MINB>
-__global__ void __launch_bounds__(THREADS, MINB) ntt_line_kernel(KView t, PlanPtrs plans, int mode, KView mul,
-                                                                 KMods mods) {
+template <int SHAPE, int MODE, bool FIX, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) ntt_line_kernel(KView t, PlanPtrs plans, KView mul, KMods mods) {
     extern __shared__ int64_t smem[];
     const int64_t tile = blockIdx.x;
     const int64_t k = tile % t.n2, r = tile / t.n2;
@@ -542,50 +567,55 @@ __global__ void __launch_bounds__(THREADS, MINB) ntt_line_kernel(KView t, PlanPt
     int64_t* g = reinterpret_cast<int64_t*>(t.p) + i * t.s0 + j * t.s1 + k * t.s2;
     const int64_t* mulp = nullptr;
     int64_t me = 0, mn = 0, mi = 0;
-    if (mode == 2) {
+    if (MODE == 2) {
         mulp = kat<int64_t>(mul, i, j, k, 0);
         me = mul.b3 ? 0 : 1;
         mn = mods.n[j], mi = mods.ninv[j];
     }
-    run_line<SHAPE>(P, c, smem, g, mode, mulp, me, mn, mi);
+    run_line<SHAPE, MODE, FIX>(P, c, smem, g, mulp, me, mn, mi);
 }
 
 /// One specialised column (global element stride ge) of shape SHAPE, in registers.
-template <int SHAPE>
-__device__ __forceinline__ void run_column(const DevPlanHeader* P, const fast::Ctx& c, int64_t* g, int64_t ge, int mode,
+template <int SHAPE, int MODE, bool FIX>
+__device__ __forceinline__ void run_column(const DevPlanHeader* P, const fast::Ctx& c, int64_t* g, int64_t ge,
                                            const int64_t* mulp, int64_t mstride, int64_t mn, int64_t mi) {
-    const bool inv = mode & 1;
+    constexpr bool inv = MODE & 1;
     const DevStage* st = inv ? P->inv : P->fwd;
-    if (SHAPE == HC_SHAPE_C12) {
-        fast::SF f[3];
+    constexpr int NST = SHAPE == HC_SHAPE_C12 ? 3 : 2;
+    fast::SF f[NST];
+    if constexpr (FIX) {
+        const FixedSched<SHAPE, inv> sch{st};
 #pragma unroll
-        for (int q = 0; q < 3; q++) f[q] = fast::sflags(st[q]);
+        for (int q = 0; q < NST; q++) f[q] = fast::sflags(sch, q);
+    } else {
+        const fast::DynSched sch{st};
+#pragma unroll
+        for (int q = 0; q < NST; q++) f[q] = fast::sflags(sch, q);
+    }
+    if constexpr (SHAPE == HC_SHAPE_C12) {
         int64_t x[4][3];
 #pragma unroll
         for (int a = 0; a < 4; a++)
 #pragma unroll
             for (int b = 0; b < 3; b++) x[a][b] = g[(3 * a + b) * ge];
-        fast::col12(c, f, inv, mode == 0, x);
+        fast::col12(c, f, inv, MODE == 0, x);
 #pragma unroll
         for (int a = 0; a < 4; a++)
 #pragma unroll
             for (int b = 0; b < 3; b++) {
                 int64_t v = x[a][b];
-                if (mode & 2) v = mul_mont(v, mulp[(3 * a + b) * mstride], mn, mi);
+                if (MODE & 2) v = mul_mont(v, mulp[(3 * a + b) * mstride], mn, mi);
                 g[(3 * a + b) * ge] = v;
             }
     } else {
-        fast::SF f[2];
-        f[0] = fast::sflags(st[0]);
-        f[1] = fast::sflags(st[1]);
         int64_t x[4];
 #pragma unroll
         for (int a = 0; a < 4; a++) x[a] = g[a * ge];
-        fast::col4(c, f, inv, mode == 0, x);
+        fast::col4(c, f, inv, MODE == 0, x);
 #pragma unroll
         for (int a = 0; a < 4; a++) {
             int64_t v = x[a];
-            if (mode & 2) v = mul_mont(v, mulp[a * mstride], mn, mi);
+            if (MODE & 2) v = mul_mont(v, mulp[a * mstride], mn, mi);
             g[a * ge] = v;
         }
     }
@@ -595,9 +625,9 @@ __device__ __forceinline__ void run_column(const DevPlanHeader* P, const fast::C
 #define HC_COL_TW 128  // twiddle words a column plan may have (checked at dispatch)
 
 /// Specialised dimension-2 NTT: one thread per column (i, j, l), CTAs over (i, j, column block).
-template <int SHAPE>
-__global__ void __launch_bounds__(HC_COL_THREADS, 3) ntt_col_kernel(KView t, PlanPtrs plans, int mode, KView mul,
-                                                                 KMods mods, int ncb) {
+template <int SHAPE, int MODE, bool FIX>
+__global__ void __launch_bounds__(HC_COL_THREADS, SHAPE == HC_SHAPE_C12 ? 2 : 4) ntt_col_kernel(KView t, PlanPtrs plans, KView mul, KMods mods,
+                                                                    int ncb) {
     __shared__ __align__(16) int64_t tws[HC_COL_TW];
     const int64_t tile = blockIdx.x;
     const int64_t cb = tile % ncb, r = tile / ncb;
@@ -611,12 +641,42 @@ __global__ void __launch_bounds__(HC_COL_THREADS, 3) ntt_col_kernel(KView t, Pla
     int64_t* g = reinterpret_cast<int64_t*>(t.p) + i * t.s0 + j * t.s1 + l;
     const int64_t* mulp = nullptr;
     int64_t ms = 0, mn = 0, mi = 0;
-    if (mode == 2) {
+    if (MODE == 2) {
         mulp = kat<int64_t>(mul, i, j, 0, l);
         ms = mul.s2;
         mn = mods.n[j], mi = mods.ninv[j];
     }
-    run_column<SHAPE>(P, c, g, t.s2, mode, mulp, ms, mn, mi);
+    run_column<SHAPE, MODE, FIX>(P, c, g, t.s2, mulp, ms, mn, mi);
+}
+
+/// Host: launches the specialised kernel of (shape, mode, fixed schedule).
+template <int SHAPE, int MODE, bool FIX>
+hc_status launch_special(hc_context ctx, const KView& t, const PlanPtrs& pp, const KView& mul, const KMods& mods,
+                         size_t smem, int64_t tiles, int ncb) {
+    if constexpr (SHAPE == HC_SHAPE_L3072 || SHAPE == HC_SHAPE_L12288) {
+        constexpr int TH = SHAPE == HC_SHAPE_L3072 ? 128 : 256, MB = SHAPE == HC_SHAPE_L3072 ? 6 : 2;
+        auto kern = ntt_line_kernel<SHAPE, MODE, FIX, TH, MB>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return hc::cuda_check(e, "ntt smem attribute");
+        kern<<<(unsigned)tiles, TH, smem, hc::stream_of(ctx)>>>(t, pp, mul, mods);
+    } else {
+        ntt_col_kernel<SHAPE, MODE, FIX><<<(unsigned)tiles, HC_COL_THREADS, 0, hc::stream_of(ctx)>>>(t, pp, mul, mods, ncb);
+    }
+    hc::count_launch(ctx);
+    return hc::cuda_check(cudaGetLastError(), "ntt kernel launch");
+}
+
+template <int SHAPE>
+hc_status launch_special_mode(hc_context ctx, int mode, bool fix, const KView& t, const PlanPtrs& pp, const KView& mul,
+                              const KMods& mods, size_t smem, int64_t tiles, int ncb) {
+    if (fix) {
+        if (mode == 0) return launch_special<SHAPE, 0, true>(ctx, t, pp, mul, mods, smem, tiles, ncb);
+        if (mode == 1) return launch_special<SHAPE, 1, true>(ctx, t, pp, mul, mods, smem, tiles, ncb);
+        return launch_special<SHAPE, 2, true>(ctx, t, pp, mul, mods, smem, tiles, ncb);
+    }
+    if (mode == 0) return launch_special<SHAPE, 0, false>(ctx, t, pp, mul, mods, smem, tiles, ncb);
+    if (mode == 1) return launch_special<SHAPE, 1, false>(ctx, t, pp, mul, mods, smem, tiles, ncb);
+    return launch_special<SHAPE, 2, false>(ctx, t, pp, mul, mods, smem, tiles, ncb);
 }
 
 /// mode 0: forward (reduced), 1: inverse, 2: forward unreduced + Montgomery multiplication by `mul`.
@@ -664,23 +724,38 @@ __global__ void __launch_bounds__(256, HC_NTT_MIN_BLOCKS) ntt_tile_kernel(KView 
 /// along dimension 3 multiplies by the slab's operand.
 __device__ __forceinline__ void slab_pass(const CrtSlab& S, const DevPlanHeader* P, const int64_t* tw, int64_t* s,
                                           int dim, int mode, const int64_t* mulrow, int logv) {
-    const int shape = dim == 3 ? (S.shapes & 0xff) : (S.shapes >> 8);
-    if (dim == 3 && (shape == HC_SHAPE_L3072 || shape == HC_SHAPE_L12288)) {
+    // specialised kernels for slabs whose plans have the fixed schedule (bit 16: dimension-3
+    // plan, bit 17: dimension-2 plan), the generic tile programme otherwise
+    const int shape = dim == 3 ? (S.shapes & 0xff) : ((S.shapes >> 8) & 0xff);
+    const bool fix = (S.shapes >> (dim == 3 ? 16 : 17)) & 1;
+    if (fix && dim == 3 && (shape == HC_SHAPE_L3072 || shape == HC_SHAPE_L12288)) {
         const fast::Ctx c = make_ctx(P, tw);
         for (int k = 0; k < S.dl; k++) {
             int64_t* g = S.data + k * S.s2;
             const int64_t* mulp = mode == 3 ? S.op + k * S.op_s2 : mulrow;
-            if (shape == HC_SHAPE_L3072) run_line<HC_SHAPE_L3072>(P, c, s, g, mode, mulp, 1, S.n, S.ninv);
-            else run_line<HC_SHAPE_L12288>(P, c, s, g, mode, mulp, 1, S.n, S.ninv);
+            if (shape == HC_SHAPE_L3072) {
+                if (mode == 2) run_line<HC_SHAPE_L3072, 2, true>(P, c, s, g, mulp, 1, S.n, S.ninv);
+                else if (mode == 3) run_line<HC_SHAPE_L3072, 3, true>(P, c, s, g, mulp, 1, S.n, S.ninv);
+                else run_line<HC_SHAPE_L3072, 1, true>(P, c, s, g, mulp, 1, S.n, S.ninv);
+            } else {
+                if (mode == 2) run_line<HC_SHAPE_L12288, 2, true>(P, c, s, g, mulp, 1, S.n, S.ninv);
+                else if (mode == 3) run_line<HC_SHAPE_L12288, 3, true>(P, c, s, g, mulp, 1, S.n, S.ninv);
+                else run_line<HC_SHAPE_L12288, 1, true>(P, c, s, g, mulp, 1, S.n, S.ninv);
+            }
             __syncthreads();
         }
         return;
     }
-    if (dim == 2 && (shape == HC_SHAPE_C12 || shape == HC_SHAPE_C4)) {
+    if (fix && dim == 2 && (shape == HC_SHAPE_C12 || shape == HC_SHAPE_C4)) {
         const fast::Ctx c = make_ctx(P, tw);
         for (int l = threadIdx.x; l < S.dk; l += blockDim.x) {
-            if (shape == HC_SHAPE_C12) run_column<HC_SHAPE_C12>(P, c, S.data + l, S.s2, mode, mulrow, 1, S.n, S.ninv);
-            else run_column<HC_SHAPE_C4>(P, c, S.data + l, S.s2, mode, mulrow, 1, S.n, S.ninv);
+            if (shape == HC_SHAPE_C12) {
+                if (mode == 2) run_column<HC_SHAPE_C12, 2, true>(P, c, S.data + l, S.s2, mulrow, 1, S.n, S.ninv);
+                else run_column<HC_SHAPE_C12, 1, true>(P, c, S.data + l, S.s2, mulrow, 1, S.n, S.ninv);
+            } else {
+                if (mode == 2) run_column<HC_SHAPE_C4, 2, true>(P, c, S.data + l, S.s2, mulrow, 1, S.n, S.ninv);
+                else run_column<HC_SHAPE_C4, 1, true>(P, c, S.data + l, S.s2, mulrow, 1, S.n, S.ninv);
+            }
         }
         __syncthreads();
         return;
@@ -712,7 +787,7 @@ __device__ __forceinline__ void slab_pass(const CrtSlab& S, const DevPlanHeader*
 /// its `ops` say) before taking another. Slabs of different fields and RNS lengths mix freely;
 /// the passes are the HAL transforms' passes in the same order (src/ring.rs:1118-1161), the
 /// operand product fused into the epilogue of the forward transform's last pass.
-__global__ void __launch_bounds__(256, HC_NTT_MIN_BLOCKS)
+__global__ void __launch_bounds__(256, 2)
     crt_batch_kernel(const CrtSlab* __restrict__ slabs, int nslabs, int* counter, int logv, int tile_words) {
     extern __shared__ int64_t smem[];
     __shared__ int s_next;
@@ -945,6 +1020,21 @@ hc_status build_plan(hc_context ctx, const hc_modulus* m, const size_t* shape, s
     else if (factors == std::vector<size_t>{3, 64, 64}) plan->shape = HC_SHAPE_L12288;
     else if (factors == std::vector<size_t>{4, 3}) plan->shape = HC_SHAPE_C12;
     else if (factors == std::vector<size_t>{4}) plan->shape = HC_SHAPE_C4;
+    {
+        SchedMasks m{0u, 0u, 0u, 0u, 0u};
+        for (int i = 0; i < hp.h.nfwd; i++) {
+            m.fred |= (uint32_t)(hp.h.fwd[i].reduce_before != 0) << i;
+            m.fskip |= (uint32_t)(hp.h.fwd[i].skip_ok != 0) << i;
+            m.flast |= (uint32_t)(hp.h.fwd[i].last != 0) << i;
+        }
+        for (int i = 0; i < hp.h.ninv; i++) {
+            m.ired |= (uint32_t)(hp.h.inv[i].reduce_before != 0) << i;
+            m.ilast |= (uint32_t)(hp.h.inv[i].last != 0) << i;
+        }
+        const SchedMasks f = fixed_masks(plan->shape);
+        plan->fixed = plan->shape != HC_SHAPE_GENERIC && m.fred == f.fred && m.fskip == f.fskip &&
+                      m.flast == f.flast && m.ired == f.ired && m.ilast == f.ilast;
+    }
     plan->dev = dev;
     plan->n = n;
     plan->len = (int32_t)len;
@@ -965,7 +1055,7 @@ int64_t plan_modulus(hc_ntt_plan p) { return p->n; }
 int32_t plan_len(hc_ntt_plan p) { return p->len; }
 const void* plan_device(hc_ntt_plan p) { return p->dev; }
 int32_t plan_ntw(hc_ntt_plan p) { return p->ntw; }
-int32_t plan_shape(hc_ntt_plan p) { return p->shape; }
+int32_t plan_shape(hc_ntt_plan p) { return p->shape | (p->fixed ? 0x100 : 0); }
 int32_t plan_tile_words(hc_ntt_plan p) {
     return p->shape == HC_SHAPE_L3072 || p->shape == HC_SHAPE_L12288 ? line_tile_words(p->shape) : 0;
 }
@@ -1015,26 +1105,15 @@ hc_status launch_ntt(hc_context ctx, const KView& t, const hc_ntt_plan* plans, s
     int shape = plans[0]->shape;
     for (size_t j = 1; j < nplans; j++)
         if (plans[j]->shape != shape) shape = HC_SHAPE_GENERIC;
+    bool fix = true;
+    for (size_t j = 0; j < nplans; j++) fix = fix && plans[j]->fixed;
     if (dim == 3 && (shape == HC_SHAPE_L3072 || shape == HC_SHAPE_L12288)) {
         const size_t smem = ((size_t)line_tile_words(shape) + 2 * (size_t)max_tw) * 8;
         const int64_t tiles = t.n0 * t.n1 * t.n2;
         if (smem <= max_smem_optin(ctx) && tiles <= 0x7fffffff) {
-            cudaError_t e;
-            if (shape == HC_SHAPE_L3072) {
-                e = cudaFuncSetAttribute(ntt_line_kernel<HC_SHAPE_L3072, 128, 6>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                if (e != cudaSuccess) return cuda_check(e, "ntt smem attribute");
-                ntt_line_kernel<HC_SHAPE_L3072, 128, 6>
-                    <<<(unsigned)tiles, 128, smem, stream_of(ctx)>>>(t, pp, mode, mul, mods);
-            } else {
-                e = cudaFuncSetAttribute(ntt_line_kernel<HC_SHAPE_L12288, 256, 2>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                if (e != cudaSuccess) return cuda_check(e, "ntt smem attribute");
-                ntt_line_kernel<HC_SHAPE_L12288, 256, 2>
-                    <<<(unsigned)tiles, 256, smem, stream_of(ctx)>>>(t, pp, mode, mul, mods);
-            }
-            count_launch(ctx);
-            return cuda_check(cudaGetLastError(), "ntt kernel launch");
+            if (shape == HC_SHAPE_L3072)
+                return launch_special_mode<HC_SHAPE_L3072>(ctx, mode, fix, t, pp, mul, mods, smem, tiles, 0);
+            return launch_special_mode<HC_SHAPE_L12288>(ctx, mode, fix, t, pp, mul, mods, smem, tiles, 0);
         }
     }
     if (dim == 2 && (shape == HC_SHAPE_C12 || shape == HC_SHAPE_C4) && 2 * max_tw <= HC_COL_TW) {
@@ -1042,13 +1121,8 @@ hc_status launch_ntt(hc_context ctx, const KView& t, const hc_ntt_plan* plans, s
         const int64_t tiles = t.n0 * t.n1 * ncb;
         if (tiles <= 0x7fffffff) {
             if (shape == HC_SHAPE_C12)
-                ntt_col_kernel<HC_SHAPE_C12>
-                    <<<(unsigned)tiles, HC_COL_THREADS, 0, stream_of(ctx)>>>(t, pp, mode, mul, mods, (int)ncb);
-            else
-                ntt_col_kernel<HC_SHAPE_C4>
-                    <<<(unsigned)tiles, HC_COL_THREADS, 0, stream_of(ctx)>>>(t, pp, mode, mul, mods, (int)ncb);
-            count_launch(ctx);
-            return cuda_check(cudaGetLastError(), "ntt kernel launch");
+                return launch_special_mode<HC_SHAPE_C12>(ctx, mode, fix, t, pp, mul, mods, 0, tiles, (int)ncb);
+            return launch_special_mode<HC_SHAPE_C4>(ctx, mode, fix, t, pp, mul, mods, 0, tiles, (int)ncb);
         }
     }
     int V = 1, logv = 0;

@@ -41,10 +41,29 @@ struct SF {
     int tw_off, zeta_off;
     bool red, skip_ok, last;
 };
-__device__ __forceinline__ SF sflags(const DevStage& s) {
+
+/// The plan's reduction / skip / fused-final schedule read at run time (any prime).
+struct DynSched {
+    const DevStage* st;
+    __device__ __forceinline__ bool red(int s) const { return st[s].reduce_before; }
+    __device__ __forceinline__ bool skip(int s) const { return st[s].skip_ok; }
+    __device__ __forceinline__ bool last(int s) const { return st[s].last; }
+};
+/// A schedule known at compile time (bit s = the flag of stage s), for primes whose plan has
+/// exactly this schedule; the flags then fold into straight-line code.
+template <uint32_t RED, uint32_t SKIP, uint32_t LAST>
+struct FixSched {
+    const DevStage* st;
+    __device__ __forceinline__ bool red(int s) const { return (RED >> s) & 1; }
+    __device__ __forceinline__ bool skip(int s) const { return (SKIP >> s) & 1; }
+    __device__ __forceinline__ bool last(int s) const { return (LAST >> s) & 1; }
+};
+
+template <class SCH>
+__device__ __forceinline__ SF sflags(const SCH& sch, int s) {
     SF f;
-    f.tw_off = s.tw_off, f.zeta_off = s.zeta_off;
-    f.red = s.reduce_before, f.skip_ok = s.skip_ok, f.last = s.last;
+    f.tw_off = sch.st[s].tw_off, f.zeta_off = sch.st[s].zeta_off;
+    f.red = sch.red(s), f.skip_ok = sch.skip(s), f.last = sch.last(s);
     return f;
 }
 
@@ -205,14 +224,15 @@ __device__ __forceinline__ void inv_group(const Ctx& c, const SF* f, int blockK,
 /// One pass of K radix-2 stages of a factor over a padded shared-memory tile: groups of 2^K
 /// elements at distance SPAN (= 2^LOG_SPAN) inside blocks of 2^LOG_GLEN elements, 2^LOG_NB twiddle
 /// blocks per factor at the pass's reference stage (first stage forward, last stage inverse).
-template <bool INV, int K, int LOG_SPAN, int LOG_GLEN, int LOG_NB>
-__device__ __forceinline__ void r2_pass(const Ctx& c, int64_t* s, int ngroups, const DevStage* st, bool reduce_output) {
+template <bool INV, int K, int LOG_SPAN, int LOG_GLEN, int LOG_NB, class SCH>
+__device__ __forceinline__ void r2_pass(const Ctx& c, int64_t* s, int ngroups, const SCH& sch, int s0,
+                                        bool reduce_output) {
     constexpr int M = 1 << K, SPAN = 1 << LOG_SPAN;
     SF f[K];
     bool fuse[K];
 #pragma unroll
     for (int q = 0; q < K; q++) {
-        f[q] = sflags(st[q]);
+        f[q] = sflags(sch, s0 + q);
         fuse[q] = f[q].last && reduce_output;
     }
     for (int gg = threadIdx.x; gg < ngroups; gg += blockDim.x) {
@@ -243,16 +263,27 @@ __device__ __forceinline__ void line_store(const int64_t* s, int64_t* g, int len
     }
 }
 
-/// [2, 3, 8, 64] line (3072 residues): g -> g, via the padded tile s (3456 words).
-/// Forward programme: stage 0 = factor 2, 1 = factor 3, 2..4 = factor 8, 5..10 = factor 64.
-__device__ __forceinline__ void line3072(const DevPlanHeader* __restrict__ P, const Ctx& c, int64_t* s, int64_t* g,
-                                         int mode, const int64_t* mulp, int64_t me, int64_t mn, int64_t mi) {
-    const bool inv = mode & 1;
-    const DevStage* st = inv ? P->inv : P->fwd;
-    const bool reduce_output = mode == 0;
+/// Reduces every element of a register group when the stage asks for it (src/hal/ntt.rs: the
+/// reduction pass before a stage whose growth could overflow).
+template <int N>
+__device__ __forceinline__ void red_all(const Ctx& c, bool red, int64_t* x) {
+    if (red) {
+#pragma unroll
+        for (int m = 0; m < N; m++) x[m] = red1(c, x[m]);
+    }
+}
+
+/// [2, 3, 8, 64] line (3072 residues): g -> g, via the padded tile s (3456 words). MODE as the
+/// tile kernel (0 forward, 1 inverse, 2 forward + product, 3 inverse + product); the schedule
+/// SCH is that of the programme of MODE's direction. Stages: 0 = factor 2, 1 = factor 3,
+/// 2..4 = factor 8, 5..10 = factor 64.
+template <int MODE, class SCH>
+__device__ __forceinline__ void line3072(const SCH& sch, const Ctx& c, int64_t* s, int64_t* g, const int64_t* mulp,
+                                         int64_t me, int64_t mn, int64_t mi) {
+    constexpr bool inv = MODE & 1, reduce_output = MODE == 0;
     // pass 1: factors 2 (distance 1536) and 3 (distance 512), straight from global memory
     {
-        const SF f0 = sflags(st[0]), f1 = sflags(st[1]);
+        const SF f0 = sflags(sch, 0), f1 = sflags(sch, 1);
         const bool fz0 = f0.last && reduce_output, fz1 = f1.last && reduce_output;
         for (int o = threadIdx.x; o < 512; o += blockDim.x) {
             int64_t x[2][3];
@@ -260,27 +291,14 @@ __device__ __forceinline__ void line3072(const DevPlanHeader* __restrict__ P, co
             for (int b = 0; b < 2; b++)
 #pragma unroll
                 for (int a = 0; a < 3; a++) x[b][a] = g[o + 512 * a + 1536 * b];
+            red_all<6>(c, f0.red, &x[0][0]);
             if (!inv) {
-                if (f0.red)
-#pragma unroll
-                    for (int b = 0; b < 2; b++)
-#pragma unroll
-                        for (int a = 0; a < 3; a++) x[b][a] = red1(c, x[b][a]);
 #pragma unroll
                 for (int a = 0; a < 3; a++) fwd2<true>(c, f0, fz0, 0, x[0][a], x[1][a]);
-                if (f1.red)
-#pragma unroll
-                    for (int b = 0; b < 2; b++)
-#pragma unroll
-                        for (int a = 0; a < 3; a++) x[b][a] = red1(c, x[b][a]);
+                red_all<6>(c, f1.red, &x[0][0]);
 #pragma unroll
                 for (int b = 0; b < 2; b++) fwd3<true>(c, f1, fz1, 0, x[b][0], x[b][1], x[b][2]);
             } else {
-                if (f0.red)
-#pragma unroll
-                    for (int b = 0; b < 2; b++)
-#pragma unroll
-                        for (int a = 0; a < 3; a++) x[b][a] = red1(c, x[b][a]);
 #pragma unroll
                 for (int a = 0; a < 3; a++) {
                     // factor 2: one block, twiddle 1 unless fused
@@ -293,11 +311,7 @@ __device__ __forceinline__ void line3072(const DevPlanHeader* __restrict__ P, co
                         x[1][a] = dif;
                     }
                 }
-                if (f1.red)
-#pragma unroll
-                    for (int b = 0; b < 2; b++)
-#pragma unroll
-                        for (int a = 0; a < 3; a++) x[b][a] = red1(c, x[b][a]);
+                red_all<6>(c, f1.red, &x[0][0]);
 #pragma unroll
                 for (int b = 0; b < 2; b++) inv3(c, f1, 0, x[b][0], x[b][1], x[b][2]);
             }
@@ -309,53 +323,48 @@ __device__ __forceinline__ void line3072(const DevPlanHeader* __restrict__ P, co
     }
     __syncthreads();
     if (!inv) {
-        r2_pass<false, 3, 6, 9, 0>(c, s, 384, st + 2, reduce_output);  // factor 8: distances 256, 128, 64
+        r2_pass<false, 3, 6, 9, 0>(c, s, 384, sch, 2, reduce_output);  // factor 8: distances 256, 128, 64
         __syncthreads();
-        r2_pass<false, 3, 3, 6, 0>(c, s, 384, st + 5, reduce_output);  // factor 64: 32, 16, 8
+        r2_pass<false, 3, 3, 6, 0>(c, s, 384, sch, 5, reduce_output);  // factor 64: 32, 16, 8
         __syncthreads();
-        r2_pass<false, 3, 0, 3, 3>(c, s, 384, st + 8, reduce_output);  // factor 64: 4, 2, 1
+        r2_pass<false, 3, 0, 3, 3>(c, s, 384, sch, 8, reduce_output);  // factor 64: 4, 2, 1
     } else {
-        r2_pass<true, 3, 6, 9, 0>(c, s, 384, st + 2, false);  // factor 8: distances 64, 128, 256
+        r2_pass<true, 3, 6, 9, 0>(c, s, 384, sch, 2, false);  // factor 8: distances 64, 128, 256
         __syncthreads();
-        r2_pass<true, 3, 0, 3, 3>(c, s, 384, st + 5, false);  // factor 64: 1, 2, 4
+        r2_pass<true, 3, 0, 3, 3>(c, s, 384, sch, 5, false);  // factor 64: 1, 2, 4
         __syncthreads();
-        r2_pass<true, 3, 3, 6, 0>(c, s, 384, st + 8, false);  // factor 64: 8, 16, 32
+        r2_pass<true, 3, 3, 6, 0>(c, s, 384, sch, 8, false);  // factor 64: 8, 16, 32
     }
     __syncthreads();
-    line_store(s, g, 3072, mode & 2, mulp, me, mn, mi);
+    line_store(s, g, 3072, MODE & 2, mulp, me, mn, mi);
 }
 
-/// [3, 64, 64] line (12288 residues): forward programme stage 0 = factor 3 (distance 4096),
-/// 1..6 = first factor 64 (distances 2048 .. 64), 7..12 = second factor 64 (32 .. 1).
-__device__ __forceinline__ void line12288(const DevPlanHeader* __restrict__ P, const Ctx& c, int64_t* s, int64_t* g,
-                                          int mode, const int64_t* mulp, int64_t me, int64_t mn, int64_t mi) {
-    const bool inv = mode & 1;
-    const DevStage* st = inv ? P->inv : P->fwd;
-    const bool reduce_output = mode == 0;
+/// [3, 64, 64] line (12288 residues): stages 0 = factor 3 (distance 4096), 1..6 = first factor
+/// 64 (distances 2048 .. 64), 7..12 = second factor 64 (32 .. 1).
+template <int MODE, class SCH>
+__device__ __forceinline__ void line12288(const SCH& sch, const Ctx& c, int64_t* s, int64_t* g, const int64_t* mulp,
+                                          int64_t me, int64_t mn, int64_t mi) {
+    constexpr bool inv = MODE & 1, reduce_output = MODE == 0;
     // pass 1: factor 3 and three stages of the first factor 64, straight from global memory
     {
         SF f[4];
         bool fz[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            f[q] = sflags(st[q]);
+            f[q] = sflags(sch, q);
             fz[q] = f[q].last && reduce_output;
         }
+        // forward: elements o + 512 m + 4096 a (o < 512); inverse: base + 64 m + 4096 a with
+        // base = (gg >> 6) * 512 + (gg & 63)
+        constexpr int span = inv ? 64 : 512;
         for (int gg = threadIdx.x; gg < 512; gg += blockDim.x) {
-            // forward: elements o + 512 m + 4096 a (o < 512); inverse: base + 64 m + 4096 a with
-            // base = (gg >> 6) * 512 + (gg & 63)
             const int base = inv ? ((gg >> 6) << 9) + (gg & 63) : gg;
-            const int span = inv ? 64 : 512;
             int64_t x[3][8];
 #pragma unroll
             for (int a = 0; a < 3; a++)
 #pragma unroll
                 for (int m = 0; m < 8; m++) x[a][m] = g[base + span * m + 4096 * a];
-            if (f[0].red)
-#pragma unroll
-                for (int a = 0; a < 3; a++)
-#pragma unroll
-                    for (int m = 0; m < 8; m++) x[a][m] = red1(c, x[a][m]);
+            red_all<24>(c, f[0].red, &x[0][0]);
             if (!inv) {
 #pragma unroll
                 for (int m = 0; m < 8; m++) fwd3<true>(c, f[0], fz[0], 0, x[0][m], x[1][m], x[2][m]);
@@ -375,20 +384,20 @@ __device__ __forceinline__ void line12288(const DevPlanHeader* __restrict__ P, c
     }
     __syncthreads();
     if (!inv) {
-        r2_pass<false, 3, 6, 9, 3>(c, s, 1536, st + 4, reduce_output);   // factor 64 (a): 256, 128, 64
+        r2_pass<false, 3, 6, 9, 3>(c, s, 1536, sch, 4, reduce_output);   // factor 64 (a): 256, 128, 64
         __syncthreads();
-        r2_pass<false, 3, 3, 6, 0>(c, s, 1536, st + 7, reduce_output);   // factor 64 (b): 32, 16, 8
+        r2_pass<false, 3, 3, 6, 0>(c, s, 1536, sch, 7, reduce_output);   // factor 64 (b): 32, 16, 8
         __syncthreads();
-        r2_pass<false, 3, 0, 3, 3>(c, s, 1536, st + 10, reduce_output);  // factor 64 (b): 4, 2, 1
+        r2_pass<false, 3, 0, 3, 3>(c, s, 1536, sch, 10, reduce_output);  // factor 64 (b): 4, 2, 1
     } else {
-        r2_pass<true, 3, 9, 12, 0>(c, s, 1536, st + 4, false);  // factor 64 (a): 512, 1024, 2048
+        r2_pass<true, 3, 9, 12, 0>(c, s, 1536, sch, 4, false);  // factor 64 (a): 512, 1024, 2048
         __syncthreads();
-        r2_pass<true, 3, 0, 3, 3>(c, s, 1536, st + 7, false);   // factor 64 (b): 1, 2, 4
+        r2_pass<true, 3, 0, 3, 3>(c, s, 1536, sch, 7, false);   // factor 64 (b): 1, 2, 4
         __syncthreads();
-        r2_pass<true, 3, 3, 6, 0>(c, s, 1536, st + 10, false);  // factor 64 (b): 8, 16, 32
+        r2_pass<true, 3, 3, 6, 0>(c, s, 1536, sch, 10, false);  // factor 64 (b): 8, 16, 32
     }
     __syncthreads();
-    line_store(s, g, 12288, mode & 2, mulp, me, mn, mi);
+    line_store(s, g, 12288, MODE & 2, mulp, me, mn, mi);
 }
 
 // ---------------------------------------------------------------- columns

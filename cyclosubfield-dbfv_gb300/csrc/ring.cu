@@ -1602,7 +1602,7 @@ std::string crt_signature(const std::vector<CrtSlab>& v) {
 /// larger of a line and a column block; rounded to an even word count (16-byte aligned twiddles).
 size_t crt_tile_words(const CrtSlab& s, int logv) {
     size_t w = std::max<size_t>((size_t)s.dk, (size_t)s.dl << logv);
-    if ((s.shapes & 0xff) != 0) w = std::max<size_t>(w, (size_t)s.dk + (size_t)s.dk / 8);
+    if ((s.shapes & 0xff) != 0 && ((s.shapes >> 16) & 1)) w = std::max<size_t>(w, (size_t)s.dk + (size_t)s.dk / 8);
     return (w + 1) & ~(size_t)1;
 }
 
@@ -1652,7 +1652,11 @@ hc_status hc_crt_batch_create(hc_context ctx, const hc_crt_item* items, size_t n
                     s.n = tc.mods[j].n, s.ninv = tc.mods[j].neg_inv_n;
                     s.dl = (int32_t)R->dl(), s.dk = (int32_t)R->dk();
                     s.ops = ops;
-                    s.shapes = plan_shape(tc.pk[j]) | (plan_shape(tc.plp[j]) << 8);
+                    {
+                        // plan_shape: shape in bits 0..7, fixed schedule in bit 8
+                        const int32_t s3 = plan_shape(tc.pk[j]), s2 = plan_shape(tc.plp[j]);
+                        s.shapes = (s3 & 0xff) | ((s2 & 0xff) << 8) | (((s3 >> 8) & 1) << 16) | (((s2 >> 8) & 1) << 17);
+                    }
                     b->host.push_back(s);
                     b->tw_words = std::max<size_t>(b->tw_words, 2 * (size_t)(plan_ntw(tc.plp[j]) + plan_ntw(tc.pk[j])));
                 }
