@@ -40,6 +40,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=8, help="ciphertext pairs multiplied per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-crt-batch", action="store_true", help="skip the batched CRT-transform workload")
+    ap.add_argument("--roofline-only", action="store_true",
+                    help="time only the dominant NTT kernel (the launches a profile of it captures)")
     return ap.parse_args()
 
 
@@ -310,14 +312,20 @@ def e2e_steps(be, work, steps):
     return ms, 2 * nbytes, nbytes, hout
 
 
-def kernel_roofline(be, work, reps, peaks):
-    """Dominant kernel: the dimension-3 lazy NTT of the transforms (one HAL launch), timed alone on
-    the lifted-product tensor of one ct-mult [3, r + e, 12, 3072]. Algorithmic bytes per launch:
-    one read and one write of every i64 residue (16 B per residue)."""
+# DRAM bytes (read + written) of one launch of that kernel on that tensor, from an ncu capture of
+# `python bench.py --roofline-only` (profiles/ntt_line_kernel_intt_dim3_field36864_r34.md): the
+# tensor is read once; its writes stay in L2 during the launch.
+NCU_TRAFFIC_BYTES = 30239232
+
+
+def kernel_roofline(be, R, base, reps, peaks):
+    """Dominant kernel: the dimension-3 lazy NTT of the transforms (one HAL launch of the
+    specialised [2, 3, 8, 64] line kernel), timed alone on the lifted-product tensor of one
+    ct-mult [3, r + e, 12, 3072]. Algorithmic bytes per launch: one read and one write of every
+    i64 residue (16 B per residue)."""
     import halcuda
 
-    R = work.ring
-    lifted = work.base + R.extension_base(work.base)
+    lifted = base + R.extension_base(base)
     t = R.allocate(3, len(lifted))
     plans = [R_plan for R_plan in _k_plans(R, lifted)]
     ev0, ev1 = halcuda.Event(), halcuda.Event()
@@ -332,10 +340,13 @@ def kernel_roofline(be, work, reps, peaks):
     bytes_alg = 16 * 3 * len(lifted) * R.n
     achieved = bytes_alg / (ms * 1e-3) / 1e9
     peak = peaks.get("hbm_gbs")
-    return {"kernel": "ntt_tile_kernel (intt, dim 3, [3, %d, 12, 3072])" % len(lifted), "bound": "hbm",
-            "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4) if peak else None, "traffic": None,
-            "bytes_per_launch": bytes_alg, "launch_ms": round(ms, 5), "peak_source": "measured"}
+    return {"kernel": "ntt_line_kernel (inverse, dim 3, lines [2, 3, 8, 64], tensor [3, %d, 12, 3072])" % len(lifted),
+            "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4) if peak else None,
+            "traffic": NCU_TRAFFIC_BYTES if len(lifted) == 34 else None,
+            "bytes_per_launch": bytes_alg, "launch_ms": round(ms, 5),
+            "peak_source": "measured" if not peaks.get("fallback") else "fallback",
+            "note": "bit-exact lazy Barrett NTT: bound by the 32-bit integer multiply pipe, not by HBM"}
 
 
 _PLAN_CACHE = {}
@@ -451,6 +462,12 @@ def main():
 
     halcuda.lib()
     be = halcuda.CudaBackend(dist.local_rank)
+    if args.roofline_only:
+        import ringcuda
+
+        ring = ringcuda.RingContext(FIELD, LOG2_Q[0], LOG2_Q[1], T_BITS, backend=be)
+        print(json.dumps(kernel_roofline(be, ring, ring.initial_base(), max(1, args.steps), load_peaks())), flush=True)
+        return
     work = Workload(be, args.batch)
     scratch = be.hal_allocate_i64((1, 1, 1, 2 * L2_BYTES // 8))
     peaks = load_peaks()
@@ -480,7 +497,7 @@ def main():
 
     e2e_ms, h2d, d2h, _ = e2e_steps(be, work, args.steps)
     e2e_val = dist.world * work.batch * args.steps / (e2e_ms * 1e-3)
-    roof = kernel_roofline(be, work, 20, peaks)
+    roof = kernel_roofline(be, work.ring, work.base, 20, peaks)
     crt = None if args.no_crt_batch else crt_batch_bench(be, max(3, args.steps // 2), args.warmup)
 
     if dist.rank != 0:

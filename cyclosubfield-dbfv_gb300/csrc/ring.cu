@@ -899,13 +899,24 @@ struct Wide {
         step(rs, re, sb * mp2());
     }
     bool full(size_t row) const { return bound[row] > ((u128)minp << 63); }
-    void reduce_into(const hc_view& dst) {
+    /// wide[rs..re) = sum_t lhs_t * rhs_t (fresh rows only; src/ring.rs:460-485), all operands
+    /// almost reduced (bound 1)
+    void inner_product(size_t rs, size_t re, const std::vector<hc_view>& lhs, const std::vector<hc_view>& rhs) {
+        for (size_t i = rs; i < re; i++) REQUIRE(bound[i] == 0, HC_ERR_ARG, "inner product into a used row");
+        REQUIRE(!lhs.empty() && lhs.size() == rhs.size(), HC_ERR_ARG, "inner product terms");
+        CK(hc_inner_product_i64(R->ctx, vrows(data.view(), (int64_t)rs, (int64_t)re, true), lhs.data(), rhs.data(),
+                                lhs.size()));
+        step(rs, re, (u128)lhs.size() * mp2());
+    }
+    void reduce_into(const hc_view& dst) { reduce_rows_into(dst, bound.size()); }
+    /// reduces rows [0, rows) into dst (src/ring.rs:846-865)
+    void reduce_rows_into(const hc_view& dst, size_t rows) {
         std::vector<hc_modulus> m = R->mods(base);
         size_t s = 0;
-        while (s < bound.size()) {
+        while (s < rows) {
             bool f = full(s);
             size_t e = s + 1;
-            while (e < bound.size() && full(e) == f) e++;
+            while (e < rows && full(e) == f) e++;
             hc_view d = vrows(dst, (int64_t)s, (int64_t)e);
             hc_view w = vrows(data.view(), (int64_t)s, (int64_t)e, true);
             if (f) {
@@ -1774,6 +1785,366 @@ hc_status hc_crt_batch_tune(hc_crt_batch b, int reps, hc_crt_launch* chosen) {
 hc_status hc_crt_batch_destroy(hc_crt_batch b) {
     delete b;
     return HC_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------- Galois keysets
+
+/// Galois keys of one gadget split, resident in HBM up to a byte budget; the rest is kept in
+/// pinned host memory and staged into two alternating device slots right before use, the copy
+/// of the next key running on a copy stream while the current key switch computes.
+struct hc_keyset_s {
+    hc_ring R = nullptr;
+    Digits digits;
+    size_t r_key = 0, key_words = 0, budget = 0, resident_bytes = 0;
+    struct Entry {
+        DBuf dev;
+        void* host = nullptr;
+    };
+    std::map<uint64_t, Entry> keys;
+    DBuf slot[2];
+    cudaEvent_t ready[2] = {nullptr, nullptr}, freed[2] = {nullptr, nullptr};
+    cudaStream_t copy = nullptr;
+    int next_slot = 0;
+    uint64_t streamed_keys = 0, streamed_bytes = 0;
+    ~hc_keyset_s() {
+        for (auto& kv : keys)
+            if (kv.second.host) cudaFreeHost(kv.second.host);
+        for (int i = 0; i < 2; i++) {
+            if (ready[i]) cudaEventDestroy(ready[i]);
+            if (freed[i]) cudaEventDestroy(freed[i]);
+        }
+        if (copy) cudaStreamDestroy(copy);
+    }
+    size_t key_bytes() const { return key_words * 8; }
+    hc_view view_of(void* p) const {
+        hc_view v;
+        v.ptr = p;
+        v.shape[0] = 2 * (int64_t)digits.size(), v.shape[1] = (int64_t)r_key, v.shape[2] = R->dl(), v.shape[3] = R->dk();
+        v.strides[3] = 1, v.strides[2] = R->dk(), v.strides[1] = R->dl() * R->dk(), v.strides[0] = (int64_t)r_key * v.strides[1];
+        return v;
+    }
+    /// Issues the copy of a streamed key into the next slot (after that slot's last use).
+    int stage(const Entry& e) {
+        const int s = next_slot;
+        next_slot ^= 1;
+        cudaStream_t st = stream_of(R->ctx);
+        if (!slot[s].p) slot[s] = DBuf(R->ctx, key_bytes());
+        CK(cuda_check(cudaStreamWaitEvent(copy, freed[s], 0), "keyset copy wait"));
+        CK(cuda_check(cudaMemcpyAsync(slot[s].p, e.host, key_bytes(), cudaMemcpyHostToDevice, copy), "key stream copy"));
+        CK(cuda_check(cudaEventRecord(ready[s], copy), "keyset copy event"));
+        (void)st;
+        streamed_keys++;
+        streamed_bytes += key_bytes();
+        return s;
+    }
+    /// Runs fn(i, key view) for the keys of gs in order on the context stream; resident keys are
+    /// used in place, streamed keys are staged one ahead.
+    template <typename F>
+    void each(const std::vector<uint64_t>& gs, F fn) {
+        cudaStream_t st = stream_of(R->ctx);
+        std::vector<const Entry*> es;
+        for (uint64_t g : gs) {
+            auto it = keys.find(g);
+            REQUIRE(it != keys.end(), HC_ERR_ARG, "keyset: no Galois key for automorphism " + std::to_string(g));
+            es.push_back(&it->second);
+        }
+        std::vector<int> slot_of(gs.size(), -1);
+        size_t pre = 0;  // next key whose copy is not yet issued
+        auto issue_next = [&](size_t from) {
+            for (pre = std::max(pre, from); pre < es.size(); pre++)
+                if (es[pre]->host) {
+                    slot_of[pre] = stage(*es[pre]);
+                    pre++;
+                    return;
+                }
+        };
+        issue_next(0);
+        for (size_t i = 0; i < es.size(); i++) {
+            hc_view kv;
+            if (es[i]->host) {
+                const int s = slot_of[i];
+                CK(cuda_check(cudaStreamWaitEvent(st, ready[s], 0), "keyset ready wait"));
+                issue_next(i + 1);  // overlaps the key switch of key i
+                kv = view_of(slot[s].p);
+                fn(i, kv);
+                CK(cuda_check(cudaEventRecord(freed[s], st), "keyset slot event"));
+            } else {
+                kv = view_of(es[i]->dev.p);
+                fn(i, kv);
+            }
+        }
+    }
+};
+
+namespace {
+
+/// bfv_hom_gal (src/bfv.rs:783-841) with the keys of a keyset and one output view per automorphism.
+void hom_gal_keyset(hc_ring R, const hc_view& ct, const Base& b, const std::vector<uint64_t>& gs, hc_keyset ks,
+                    const std::vector<hc_view>& outs) {
+    if (gs.empty()) return;
+    const int64_t rr = (int64_t)b.size();
+    Digits dg = clip(ks->digits, b.size());
+    REQUIRE(ks->r_key >= b.size(), HC_ERR_SHAPE, "keyset keys cover fewer RNS factors than the ciphertext");
+    Tensor c1(R->ctx, 1, rr, R->dl(), R->dk());
+    CK(hc_assign(R->ctx, c1.view(), vrows(ct, 1, 2)));
+    R->transform(c1.view(), b, true);
+    Tensor parts = gadget_decompose(R, c1.view(), b, dg);
+    hc_view c0 = vrows(ct, 0, 1);
+    ks->each(gs, [&](size_t gi, const hc_view& key) {
+        PermCache& pc = R->perms(gs[gi]);
+        keyswitch(R, parts.view(), key, b, dg.size(), &c0, nullptr, outs[gi], pc.p2.as<uint32_t>(), pc.p3.as<uint32_t>());
+    });
+}
+
+/// src/dbfv.rs:97-121
+std::vector<std::vector<i128>> balanced_digits_vec(std::vector<i128> cur, i128 b, size_t max_digits) {
+    std::vector<std::vector<i128>> out;
+    for (size_t it = 0; it < max_digits; it++) {
+        bool zero = true;
+        for (i128 v : cur) zero = zero && v == 0;
+        if (zero) break;
+        std::vector<i128> rems;
+        for (i128& v : cur) {
+            i128 rem = v % b;  // cmod: the representative in (-b/2, b/2] (src/ring.rs:94-104)
+            if (rem < 0) rem += b;
+            if (rem > b / 2) rem -= b;
+            rems.push_back(rem);
+            v = (v - rem) / b;
+        }
+        out.push_back(rems);
+    }
+    return out;
+}
+
+/// src/bootstrap/homcrt.rs:335-339
+std::pair<size_t, size_t> bsgs_split(size_t len) {
+    size_t best = 1, best_cost = (size_t)-1;
+    for (size_t count = 1; count <= len; count++) {
+        size_t cost = count + 3 * ((len - 1) / count + 1);  // UNHOISTED_OVERHEAD = 3 (homcrt.rs:333)
+        if (cost < best_cost) best_cost = cost, best = count;
+    }
+    return {best, (len - 1) / best + 1};
+}
+
+uint64_t pow_mod_m(uint64_t g, size_t e, uint64_t m) {
+    uint64_t r = 1;
+    for (size_t i = 0; i < e; i++) r = (uint64_t)((u128)r * g % m);
+    return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+hc_status hc_keyset_create(hc_ring R, const size_t* digits, size_t d, size_t r_key, size_t hbm_budget_bytes,
+                           hc_keyset* out) {
+    return guard([&] {
+        REQUIRE(R && out, HC_ERR_ARG, "null argument");
+        REQUIRE(d > 0 && r_key > 0, HC_ERR_ARG, "keyset: digits and key RNS length");
+        auto ks = std::make_unique<hc_keyset_s>();
+        ks->R = R;
+        ks->digits = digits_of(digits, d);
+        ks->r_key = r_key;
+        ks->key_words = 2 * d * r_key * (size_t)R->dl() * (size_t)R->dk();
+        ks->budget = hbm_budget_bytes;
+        CK(cuda_check(cudaStreamCreateWithFlags(&ks->copy, cudaStreamNonBlocking), "keyset copy stream"));
+        for (int i = 0; i < 2; i++) {
+            CK(cuda_check(cudaEventCreateWithFlags(&ks->ready[i], cudaEventDisableTiming), "keyset event"));
+            CK(cuda_check(cudaEventCreateWithFlags(&ks->freed[i], cudaEventDisableTiming), "keyset event"));
+            CK(cuda_check(cudaEventRecord(ks->freed[i], stream_of(R->ctx)), "keyset event"));
+        }
+        *out = ks.release();
+    });
+}
+
+hc_status hc_keyset_add(hc_keyset ks, uint64_t g, hc_view key) {
+    return guard([&] {
+        REQUIRE(ks, HC_ERR_ARG, "null keyset");
+        hc_ring R = ks->R;
+        check_view(key, 2 * (int64_t)ks->digits.size(), (int64_t)ks->r_key, R->dl(), R->dk(), "Galois key");
+        REQUIRE(key.strides[2] == R->dk() && key.strides[1] == R->dl() * R->dk() &&
+                    key.strides[0] == (int64_t)ks->r_key * R->dl() * R->dk(),
+                HC_ERR_SHAPE, "Galois key must be contiguous");
+        REQUIRE(!ks->keys.count(g), HC_ERR_ARG, "keyset: automorphism already has a key");
+        hc_keyset_s::Entry e;
+        cudaStream_t st = stream_of(R->ctx);
+        if (ks->resident_bytes + ks->key_bytes() <= ks->budget) {
+            e.dev = DBuf(R->ctx, ks->key_bytes());
+            CK(cuda_check(cudaMemcpyAsync(e.dev.p, key.ptr, ks->key_bytes(), cudaMemcpyDeviceToDevice, st), "key copy"));
+            ks->resident_bytes += ks->key_bytes();
+        } else {
+            CK(cuda_check(cudaMallocHost(&e.host, ks->key_bytes()), "pinned key allocation"));
+            CK(cuda_check(cudaMemcpyAsync(e.host, key.ptr, ks->key_bytes(), cudaMemcpyDeviceToHost, st), "key copy"));
+            CK(cuda_check(cudaStreamSynchronize(st), "key copy"));
+        }
+        ks->keys[g] = std::move(e);
+    });
+}
+
+hc_status hc_keyset_stats(hc_keyset ks, size_t* resident, size_t* streamed, uint64_t* streamed_keys,
+                          uint64_t* streamed_bytes) {
+    return guard([&] {
+        REQUIRE(ks, HC_ERR_ARG, "null keyset");
+        size_t res = 0, str = 0;
+        for (auto& kv : ks->keys) (kv.second.host ? str : res)++;
+        if (resident) *resident = res;
+        if (streamed) *streamed = str;
+        if (streamed_keys) *streamed_keys = ks->streamed_keys;
+        if (streamed_bytes) *streamed_bytes = ks->streamed_bytes;
+    });
+}
+
+hc_status hc_keyset_destroy(hc_keyset ks) {
+    if (ks) cudaStreamSynchronize(stream_of(ks->R->ctx));
+    delete ks;
+    return HC_OK;
+}
+
+hc_status hc_bfv_hom_gal_keyset(hc_ring R, hc_view ct, const size_t* base, size_t r, const uint64_t* gs, size_t ngs,
+                                hc_keyset ks, hc_view out) {
+    return guard([&] {
+        REQUIRE(R && ks, HC_ERR_ARG, "null argument");
+        if (ngs == 0) return;
+        REQUIRE(gs, HC_ERR_ARG, "null automorphism list");
+        Base b = base_of(base, r);
+        check_view(ct, 2, (int64_t)r, R->dl(), R->dk(), "ciphertext");
+        check_view(out, 2 * (int64_t)ngs, (int64_t)r, R->dl(), R->dk(), "output");
+        std::vector<hc_view> outs;
+        for (size_t i = 0; i < ngs; i++) outs.push_back(vrows(out, 2 * (int64_t)i, 2 * (int64_t)i + 2));
+        hom_gal_keyset(R, ct, b, std::vector<uint64_t>(gs, gs + ngs), ks, outs);
+    });
+}
+
+hc_status hc_dbfv_hom_cyclic_transform(hc_ring R, size_t log2_b, size_t log2_t, uint64_t g, const int64_t* coeffs,
+                                       size_t len, hc_view ct, const size_t* base, size_t r, hc_keyset ks, hc_view out,
+                                       size_t* out_rows) {
+    return guard([&] {
+        REQUIRE(R && ks && out_rows, HC_ERR_ARG, "null argument");
+        REQUIRE(log2_b >= 1 && log2_t >= 1 && log2_t <= 126, HC_ERR_ARG, "t = 2^log2_t must be between 2 and 2^126");
+        REQUIRE(len == 0 || coeffs, HC_ERR_ARG, "null coefficients");
+        const size_t digits = (log2_t - 1) / log2_b + 1;
+        REQUIRE(log2_b <= 125, HC_ERR_ARG, "digit base too large");
+        const i128 bb = (i128)1 << log2_b;
+        Base b = base_of(base, r);
+        const int64_t rr = (int64_t)r, dl = R->dl(), dk = R->dk();
+        REQUIRE(ct.shape[0] % 2 == 0, HC_ERR_SHAPE, "dBFV ciphertext rows");
+        const size_t d = (size_t)ct.shape[0] / 2;
+        REQUIRE(d <= digits, HC_ERR_SHAPE, "ciphertext has more digits than the modulus");
+        check_view(ct, ct.shape[0], rr, dl, dk, "dBFV ciphertext");
+        check_view(out, 2 * (int64_t)digits, rr, dl, dk, "output");
+        *out_rows = 0;
+        if (len == 0) return;
+        // the L' coefficients' balanced digits as CRT-basis tensors [1, r, deg_L', 1]
+        // (src/ring.rs:1227-1250), all in one batch
+        std::vector<std::vector<std::vector<i128>>> bd(len);
+        std::vector<size_t> first(len, 0);
+        size_t nt = 0;
+        for (size_t i = 0; i < len; i++) {
+            std::vector<i128> c((size_t)dl);
+            for (int64_t k = 0; k < dl; k++) {
+                const int64_t* w = coeffs + 2 * (i * (size_t)dl + (size_t)k);
+                c[(size_t)k] = (i128)(((u128)(uint64_t)w[1] << 64) | (uint64_t)w[0]);
+            }
+            bd[i] = balanced_digits_vec(c, bb, digits);
+            first[i] = nt;
+            nt += bd[i].size();
+        }
+        Tensor L;
+        if (nt > 0) {
+            L = Tensor(R->ctx, (int64_t)nt, rr, dl, 1);
+            std::vector<int64_t> vals;
+            for (size_t i = 0; i < len; i++)
+                for (auto& cv : bd[i])
+                    for (size_t idx : b) {
+                        const int64_t p = R->prime(idx);
+                        for (i128 cf : cv) vals.push_back(mont_repr((int64_t)(cf % (i128)p), p));
+                    }
+            CK(hc_import(R->ctx, L.view(), vals.data(), vals.size()));
+            TransformCache& tc = R->transform_cache(b);
+            CK(hc_ntt_mul_mont64_dim(R->ctx, L.view(), tc.plp.data(), r, HC_DIM2, tc.kl.view(), tc.mods.data(), r));
+            CK(hc_intt_mont64_dim(R->ctx, L.view(), tc.plp.data(), r, HC_DIM2));
+        }
+        auto ltensor = [&](size_t i, size_t jj) { return vrows(L.view(), (int64_t)(first[i] + jj), (int64_t)(first[i] + jj + 1)); };
+        // a dBFV batch O of `od` digits in CRT basis, reduced from a fresh accumulator
+        Tensor O;
+        size_t od = 0;
+        auto finish = [&](Wide& acc, size_t used) {
+            Tensor n(R->ctx, 2 * (int64_t)used, rr, dl, dk, false, false);
+            if (used > 0) acc.reduce_rows_into(n.view(), 2 * used);
+            O = std::move(n);
+            od = used;
+        };
+        if (len == 1) {
+            // dbfv_hom_fma_element_lprime with an empty summand (src/dbfv.rs:431-453)
+            if (d == 0 || bd[0].empty()) return;
+            Wide acc(R, 2 * (int64_t)digits, b);
+            const size_t nd = std::min(digits, d + bd[0].size() - 1);
+            for (size_t i = 0; i < d; i++)
+                for (size_t j = 0; j < bd[0].size(); j++)
+                    if (i + j < nd)
+                        acc.fma(2 * (i + j), 2 * (i + j) + 2, vrows(ct, 2 * (int64_t)i, 2 * (int64_t)i + 2), 1,
+                                ltensor(0, j), 1);
+            finish(acc, nd);
+        } else {
+            const auto sp = bsgs_split(len);
+            const size_t baby = sp.first, giant_steps = sp.second;
+            const uint64_t m = R->field.m();
+            std::vector<uint64_t> baby_exps;
+            for (size_t j = 1; j < baby; j++) baby_exps.push_back(pow_mod_m(g, j, m));
+            // babys: block j (rows j 2d .. (j + 1) 2d) = sigma^j(ct)
+            Tensor B(R->ctx, (int64_t)(baby * 2 * d), rr, dl, dk, false, false);
+            if (d > 0) CK(hc_assign(R->ctx, vrows(B.view(), 0, 2 * (int64_t)d), ct));
+            for (size_t di = 0; di < d; di++) {
+                std::vector<hc_view> outs;
+                for (size_t j = 1; j < baby; j++)
+                    outs.push_back(vrows(B.view(), (int64_t)(j * 2 * d + 2 * di), (int64_t)(j * 2 * d + 2 * di + 2)));
+                hom_gal_keyset(R, vrows(B.view(), 2 * (int64_t)di, 2 * (int64_t)di + 2), b, baby_exps, ks, outs);
+            }
+            const uint64_t giant_exp = pow_mod_m(g, baby, m);
+            for (size_t giant = giant_steps; giant-- > 0;) {
+                if (giant != giant_steps - 1 && od > 0) {
+                    Tensor rot(R->ctx, 2 * (int64_t)od, rr, dl, dk, false, false);
+                    for (size_t di = 0; di < od; di++)
+                        hom_gal_keyset(R, vrows(O.view(), 2 * (int64_t)di, 2 * (int64_t)di + 2), b, {giant_exp}, ks,
+                                       {vrows(rot.view(), 2 * (int64_t)di, 2 * (int64_t)di + 2)});
+                    O = std::move(rot);
+                }
+                Wide acc(R, 2 * (int64_t)digits, b);
+                const size_t nterm = std::min(baby, len - giant * baby);
+                size_t max_new = 0;
+                for (size_t j = 0; j < nterm; j++) {
+                    const size_t nr = bd[giant * baby + j].size();
+                    if (d > 0 && nr > 0) max_new = std::max(max_new, std::min(digits, d + nr - 1));
+                }
+                // one inner product per output digit over the convolution diagonal (src/dbfv.rs:291-352)
+                for (size_t k = 0; k < max_new; k++) {
+                    std::vector<hc_view> lhs, rhs;
+                    for (size_t j = 0; j < nterm; j++) {
+                        const size_t ci = giant * baby + j, nr = bd[ci].size();
+                        if (d == 0 || nr == 0 || k >= std::min(digits, d + nr - 1)) continue;
+                        for (size_t jj = 0; jj < nr && jj <= k; jj++) {
+                            const size_t i = k - jj;
+                            if (i >= d) continue;
+                            lhs.push_back(vrows(B.view(), (int64_t)(j * 2 * d + 2 * i), (int64_t)(j * 2 * d + 2 * i + 2)));
+                            rhs.push_back(ltensor(ci, jj));
+                        }
+                    }
+                    REQUIRE(lhs.size() <= HC_MAX_TERMS, HC_ERR_UNSUPPORTED, "too many inner-product terms per digit");
+                    if (!lhs.empty()) acc.inner_product(2 * k, 2 * k + 2, lhs, rhs);
+                }
+                size_t used = max_new;
+                if (od > 0) {
+                    acc.add(0, 2 * od, O.view(), 1);
+                    used = std::max(used, od);
+                }
+                finish(acc, used);
+            }
+        }
+        if (od > 0) CK(hc_assign(R->ctx, vrows(out, 0, 2 * (int64_t)od), O.view()));
+        *out_rows = 2 * od;
+    });
 }
 
 }  // extern "C"

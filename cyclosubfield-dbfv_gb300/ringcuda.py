@@ -317,3 +317,63 @@ class CrtBatch:
             self.close()
         except Exception:
             pass
+
+
+class Keyset:
+    """hc_keyset: Galois keys of one gadget split, in HBM up to `hbm_budget_bytes`, the rest in
+    pinned host memory and streamed in before use (replaces the reference's key offloading)."""
+
+    def __init__(self, ring, digits, r_key, hbm_budget_bytes):
+        self.ring, self.digits, self.r_key = ring, list(digits), r_key
+        dg, nd = _digits(digits)
+        h = ctypes.c_void_p()
+        check(lib().hc_keyset_create(ring.h, dg, nd, ctypes.c_size_t(r_key), ctypes.c_size_t(int(hbm_budget_bytes)),
+                                     ctypes.byref(h)))
+        self.h = h
+        ring.backend.add_dependent(self)
+
+    def add(self, g, key):
+        check(lib().hc_keyset_add(self.h, ctypes.c_uint64(g), key.view()))
+
+    def stats(self):
+        res, strm = ctypes.c_size_t(), ctypes.c_size_t()
+        nk, nb = ctypes.c_uint64(), ctypes.c_uint64()
+        check(lib().hc_keyset_stats(self.h, ctypes.byref(res), ctypes.byref(strm), ctypes.byref(nk), ctypes.byref(nb)))
+        return {"resident": res.value, "streamed": strm.value, "streamed_copies": nk.value,
+                "streamed_bytes": nb.value}
+
+    def close(self):
+        if self.h and self.ring.backend.h:
+            lib().hc_keyset_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def hom_gal_keyset(ring, ct, base, gs, ks):
+    out = ring.allocate(2 * len(gs), len(base))
+    garr = (ctypes.c_uint64 * max(1, len(gs)))(*gs)
+    check(lib().hc_bfv_hom_gal_keyset(ring.h, ct.view(), _sz(base), ctypes.c_size_t(len(base)), garr,
+                                      ctypes.c_size_t(len(gs)), ks.h, out.view()))
+    return out
+
+
+def dbfv_hom_cyclic_transform(ring, log2_b, log2_t, g, coeffs, ct, base, ks):
+    """hom_cyclic_transform_dbfv on the GPU; returns a [rows, r, ...] device tensor."""
+    digits = (log2_t - 1) // log2_b + 1
+    words = np.zeros((max(1, len(coeffs)), ring.dl, 2), dtype=np.int64)
+    for i, c in enumerate(coeffs):
+        for k, v in enumerate(c):
+            w = _i128(v)
+            words[i, k, 0], words[i, k, 1] = w[0], w[1]
+    out = ring.allocate(2 * digits, len(base))
+    rows = ctypes.c_size_t(0)
+    check(lib().hc_dbfv_hom_cyclic_transform(ring.h, ctypes.c_size_t(log2_b), ctypes.c_size_t(log2_t), ctypes.c_uint64(g),
+                                             words.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(len(coeffs)),
+                                             ct.view(), _sz(base), ctypes.c_size_t(len(base)), ks.h, out.view(),
+                                             ctypes.byref(rows)))
+    return out.rows(0, rows.value)

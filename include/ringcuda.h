@@ -135,6 +135,33 @@ hc_status hc_crt_batch_get_launch(hc_crt_batch b, hc_crt_launch* out);
 size_t hc_crt_batch_num_slabs(hc_crt_batch b);
 hc_status hc_crt_batch_destroy(hc_crt_batch b);
 
+/* Galois keysets: the device-side replacement of the reference's key offloading
+ * (KeySwitchKey::offload_to_disk, src/bfv.rs:95-116, and the mmap keystore, src/keystore.rs:87-119).
+ * Keys of one gadget split (d digits over r_key factors, each [2 d, r_key, deg_L', deg_K]) stay in
+ * HBM while the resident bytes fit `hbm_budget_bytes`; further keys are moved to pinned host memory
+ * and copied into one of two device slots right before their key switch, on a separate copy
+ * stream, so that the next key's copy overlaps the current key switch. */
+typedef struct hc_keyset_s* hc_keyset;
+hc_status hc_keyset_create(hc_ring ring, const size_t* digits, size_t d, size_t r_key, size_t hbm_budget_bytes,
+                           hc_keyset* out);
+/* Adds (copies) the Galois key of automorphism g; `key` is a contiguous device tensor. */
+hc_status hc_keyset_add(hc_keyset ks, uint64_t g, hc_view key);
+hc_status hc_keyset_stats(hc_keyset ks, size_t* resident, size_t* streamed, uint64_t* streamed_keys,
+                          uint64_t* streamed_bytes);
+hc_status hc_keyset_destroy(hc_keyset ks);
+/* bfv_hom_gal (src/bfv.rs:783-841) with the keys of a keyset: ct [2, r] CRT -> out [ngs * 2, r] */
+hc_status hc_bfv_hom_gal_keyset(hc_ring ring, hc_view ct, const size_t* base, size_t r, const uint64_t* gs, size_t ngs,
+                                hc_keyset ks, hc_view out);
+/* hom_cyclic_transform_dbfv (src/bootstrap/homcrt.rs:369-429): the dBFV ciphertext ct [2 d, r]
+ * (CRT basis, almost reduced) is mapped to sum_i coeffs[i] sigma_g^i(ct) by baby-step giant-step:
+ * the baby steps share one gadget decomposition per digit, every giant step applies one unhoisted
+ * automorphism; coefficients are L' elements (len x deg_L' i128 values as (low, high) words),
+ * decomposed into balanced digits of base b = 2^log2_b, t = 2^log2_t. out has 2 * digits rows
+ * (digits = ceil(log2_t / log2_b)); *out_rows receives the rows written. */
+hc_status hc_dbfv_hom_cyclic_transform(hc_ring ring, size_t log2_b, size_t log2_t, uint64_t g, const int64_t* coeffs,
+                                       size_t len, hc_view ct, const size_t* base, size_t r, hc_keyset ks, hc_view out,
+                                       size_t* out_rows);
+
 /* No counterpart in the reference (its CPU backend allocates freely): hc_bfv_key_switch with the
  * same arguments and the same result, for callers that cannot allocate device memory - a host
  * whose HBM is handed out by its own arena or budget, or a code path where cudaMalloc / cudaFree

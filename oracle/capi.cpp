@@ -4,7 +4,7 @@
 #include <cstdio>
 #include <cstring>
 
-#include "bfv.hpp"
+#include "dbfv.hpp"
 
 using namespace oracle;
 
@@ -433,6 +433,51 @@ int or_bfv_hom_gal(void* h, const int64_t* ct, const size_t* base, size_t r, con
             els_to(e, out + off);
             off += e.data.data.size();
         }
+    });
+}
+/// lprime_element_tensor (src/ring.rs:1227-1250): deg_L' i128 coefficients (low, high words)
+/// -> out [1, r, deg_L', 1] CRT basis, Montgomery form
+int or_ring_lprime_element_tensor(void* h, const size_t* base, size_t r, const int64_t* coeffs, int64_t* out) {
+    return guarded([&] {
+        RingContext& ring = *((BfvHandle*)h)->ring;
+        std::vector<i128> c(ring.field.deg_lprime);
+        for (size_t k = 0; k < c.size(); k++)
+            c[k] = (i128)(((u128)(uint64_t)coeffs[2 * k + 1] << 64) | (uint64_t)coeffs[2 * k]);
+        Tensor<int64_t> t = ring.lprime_element_tensor(base_from(base, r), c);
+        std::memcpy(out, t.data.data(), t.data.size() * sizeof(int64_t));
+    });
+}
+/// hom_cyclic_transform_dbfv (src/bootstrap/homcrt.rs:369-429): ct [2 d_ct, r] CRT basis;
+/// coeffs: len L' elements of deg_L' i128 coefficients as (low, high) int64 words; ngk Galois
+/// keys stacked [ngk * 2 dk, r_key, ...] with their automorphisms gk_g. out receives the result
+/// (at most 2 * digits rows), *out_rows its row count.
+int or_dbfv_hom_cyclic_transform(void* h, size_t log2_b, size_t log2_t, uint64_t g, const int64_t* coeffs, size_t len,
+                                 const int64_t* ct, size_t d_ct, const size_t* base, size_t r, const int64_t* gks,
+                                 const uint64_t* gk_g, size_t ngk, const size_t* digits, size_t dk, size_t r_key,
+                                 int64_t* out, size_t* out_rows) {
+    return guarded([&] {
+        RingContext& ring = *((BfvHandle*)h)->ring;
+        Base b = base_from(base, r);
+        RingEls c = els_from(ring, ct, 2 * d_ct, b, Basis::CRTBasis);
+        std::vector<KeySwitchKey> ks;
+        size_t per = dk * 2 * r_key * ring.n();
+        for (size_t i = 0; i < ngk; i++) ks.push_back(key_from(ring, gks + i * per, dk, digits_from(digits, dk), r_key));
+        auto key_for = [&](uint64_t gg) -> const KeySwitchKey* {
+            for (size_t i = 0; i < ngk; i++)
+                if (gk_g[i] == gg) return &ks[i];
+            ORACLE_ASSERT(false, "missing galois key");
+            return nullptr;
+        };
+        const size_t dl = ring.field.deg_lprime;
+        std::vector<std::vector<i128>> cf(len, std::vector<i128>(dl));
+        for (size_t i = 0; i < len; i++)
+            for (size_t k = 0; k < dl; k++) {
+                const int64_t* w = coeffs + 2 * (i * dl + k);
+                cf[i][k] = (i128)(((u128)(uint64_t)w[1] << 64) | (uint64_t)w[0]);
+            }
+        RingEls res = hom_cyclic_transform_dbfv(ring, DBFVModulus{log2_b, log2_t}, g, cf, as_view(c), key_for);
+        els_to(res, out);
+        *out_rows = res.count();
     });
 }
 /// c0 [1, r] CRT basis, c1 [1, r] period basis -> [2, r] CRT basis

@@ -476,6 +476,37 @@ class Ring:
               ctypes.c_size_t(keys.shape[3]), _p(out))
         return out
 
+    def lprime_element_tensor(self, base, coeffs):
+        """[1, r, deg_L', 1] CRT-basis tensor of an L' element (src/ring.rs:1227-1250)."""
+        b = _sz(base)
+        words = np.ascontiguousarray(to_i128(list(coeffs)))
+        out = np.zeros((1, len(base), self.dl, 1), dtype=np.int64)
+        _call("or_ring_lprime_element_tensor", self.h, _p(b), ctypes.c_size_t(len(b)), _p(words), _p(out))
+        return out
+
+    def dbfv_hom_cyclic_transform(self, log2_b, log2_t, g, coeffs, ct, base, gks, digits):
+        """hom_cyclic_transform_dbfv (src/bootstrap/homcrt.rs:369-429): ct [2 d, r, ...] CRT basis,
+        coeffs a list of deg_L'-long integer lists, gks {automorphism: key [d_key, 2, r_key, ...]}."""
+        b = _sz(base)
+        ct = np.ascontiguousarray(ct, dtype=np.int64)
+        words = np.zeros((max(1, len(coeffs)), self.dl, 2), dtype=np.int64)
+        for i, c in enumerate(coeffs):
+            for k, v in enumerate(c):
+                w = to_i128([v])
+                words[i, k] = w[0]
+        items = sorted(gks.items())
+        keys = np.ascontiguousarray(np.stack([k for _, k in items])) if items else np.zeros((1, 1, 2, 1, 1, 1), np.int64)
+        gg = np.ascontiguousarray(np.asarray([g_ for g_, _ in items] or [0], dtype=np.uint64))
+        mod_digits = (log2_t - 1) // log2_b + 1
+        out = np.zeros((2 * mod_digits, len(base), self.dl, self.dk), dtype=np.int64)
+        rows = ctypes.c_size_t(0)
+        dg = self._digits(digits)
+        _call("or_dbfv_hom_cyclic_transform", self.h, ctypes.c_size_t(log2_b), ctypes.c_size_t(log2_t),
+              ctypes.c_uint64(g), _p(words), ctypes.c_size_t(len(coeffs)), _p(ct), ctypes.c_size_t(ct.shape[0] // 2),
+              _p(b), ctypes.c_size_t(len(b)), _p(keys), _p(gg), ctypes.c_size_t(len(items)), _p(dg),
+              ctypes.c_size_t(len(digits)), ctypes.c_size_t(keys.shape[3]), _p(out), ctypes.byref(rows))
+        return out[:rows.value]
+
     def key_switch(self, c0, c1_pb, base, keys, digits):
         b = _sz(base)
         out = self.zeros(2, len(base))
