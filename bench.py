@@ -40,6 +40,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=8, help="ciphertext pairs multiplied per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-crt-batch", action="store_true", help="skip the batched CRT-transform workload")
+    ap.add_argument("--no-homcrt", action="store_true", help="skip the homomorphic CRT transform workload")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--roofline-only", action="store_true",
                     help="time only the dominant NTT kernel (the launches a profile of it captures)")
     return ap.parse_args()
@@ -248,6 +250,87 @@ def crt_batch_bench(be, steps, warmup):
             "launches_per_batch": launches, "plain_launches_per_batch": 9 * n,
             "launch_shape": {"threads": w.launch[0], "ctas_per_sm": w.launch[1], "dim2_columns": 1 << w.launch[2]},
             "autotuned": True, "l2": "inputs 2 x %.1f GB, larger than L2" % (w.residues * 8 / 1e9)}
+
+
+def homcrt_bench(be, reps=3):
+    """Homomorphic CRT transform step (hom_cyclic_transform_dbfv) on field_49152, r = 23 factors
+    (log2 q in 1280..1310), dBFV modulus t = 2^24 in 3 digits of 8 bits: sum_{i < 64} c_i sigma^i(ct)
+    for the descriptor's order-64 generator, 13 baby steps and 5 giant steps, 13 Galois keys with
+    6 gadget digits (108 MB each). Timed with every key resident in HBM, and with an HBM key budget
+    of 8 keys, the other 5 streamed from pinned host memory for every use."""
+    import numpy as np
+
+    import halcuda
+    import ringcuda
+
+    R = ringcuda.RingContext("field_49152", 1280, 1310, 2, backend=be)
+    base = R.initial_base()
+    r = len(base)
+    log2_b, log2_t, g, length = 8, 24, 20965738, 64
+    digits = ringcuda.select_digits(math.ceil(r / 4), r)
+    la = R.log2_alpha_for_sigma(base, 3.2)
+    st = [99]
+    sk = R.gen_sk(st)
+    m = 35297665
+    baby = min(range(1, length + 1), key=lambda c: (c + 3 * ((length - 1) // c + 1), c))
+    giant = (length - 1) // baby + 1
+    gs = sorted(set([pow(g, j, m) for j in range(1, baby)] + [pow(g, baby, m)]))
+    keys = {gg: R.gen_gk(st, sk, gg, digits, la) for gg in gs}
+    t = 1 << log2_t
+    rng = np.random.default_rng(5)
+    ct = R.allocate(6, r)
+    be.hal_assign(ct.rows(0, 2), R.enc(st, base, t, [int(v) for v in rng.integers(0, t, size=R.n)], sk, la))
+    for dd in (1, 2):
+        be.hal_assign(ct.rows(2 * dd, 2 * dd + 2), R.enc(st, base, t, [0] * R.n, sk, la))
+    coeffs = [[int(v) for v in rng.integers(-t // 2, t // 2, size=R.dl)] for _ in range(length)]
+    key_bytes = 2 * len(digits) * r * R.n * 8
+    out = {"workload": "hom_cyclic_transform_dbfv field_49152 r=%d, t=2^%d (b=2^%d, 3 digits), len %d "
+                       "(%d baby x %d giant steps), %d Galois keys of %d gadget digits"
+                       % (r, log2_t, log2_b, length, baby, giant, len(gs), len(digits)),
+           "key_MB": round(key_bytes / 1e6, 1), "keys": len(gs)}
+    ev0, ev1 = halcuda.Event(), halcuda.Event()
+    for label, budget in (("resident", len(gs)), ("streamed", 8)):
+        ks = ringcuda.Keyset(R, digits, r, budget * key_bytes)
+        for gg in gs:
+            ks.add(gg, keys[gg])
+        ringcuda.dbfv_hom_cyclic_transform(R, log2_b, log2_t, g, coeffs, ct, base, ks)  # warm-up (tables)
+        be.synchronize()
+        s0 = ks.stats()
+        ev0.record(be)
+        for _ in range(reps):
+            ringcuda.dbfv_hom_cyclic_transform(R, log2_b, log2_t, g, coeffs, ct, base, ks)
+        ev1.record(be)
+        ms = ev0.elapsed_ms(ev1) / reps
+        s1 = ks.stats()
+        out[label] = {"ms_per_transform": round(ms, 3), "resident_keys": s1["resident"], "streamed_keys": s1["streamed"],
+                      "streamed_GB_per_transform": round((s1["streamed_bytes"] - s0["streamed_bytes"]) / reps / 1e9, 3)}
+        ks.close()
+    out["key_switches_per_transform"] = 3 * (baby - 1) + 3 * (giant - 1)
+    R.close()
+    return out
+
+
+def serving_bench(be, n=4000, rate=2000.0):
+    """Serving: a seeded Poisson stream of `n` requests at `rate` per second - ciphertext
+    multiplications 50 %, automorphisms 35 %, standalone CRT transforms 15 % - over field_36864
+    and field_49152 (log2 q in 1100..1140, t = 256) at RNS levels uniform in 4..20, keys resident
+    in HBM, admission by an HBM budget of 16 GB; continuously batched and plain (one request per
+    call) through the same engine."""
+    import serving
+
+    fields = {
+        "field_36864": serving.FieldState(be, "field_36864", (1100, 1140), 256, range(4, 21), 2, 3283177, seed=11),
+        "field_49152": serving.FieldState(be, "field_49152", (1100, 1140), 256, range(4, 21), 2, 20965738, seed=12),
+    }
+    out = {"workload": "%d requests, Poisson %.0f/s, mix mul/rot/crt 50/35/15, fields field_36864 + field_49152, "
+                       "levels 4..20, keys in HBM, HBM admission budget 16 GB" % (n, rate)}
+    serving.Engine(be, fields, 16 << 30).warm()  # builds the rings' tables
+    for label, batched in (("batched", True), ("plain", False)):
+        reqs = serving.make_stream(n, rate, [0.5, 0.35, 0.15], sorted(fields), (4, 20), 2, seed=7)
+        out[label] = serving.Engine(be, fields, 16 << 30).run(reqs, batched=batched)
+    for f in fields.values():
+        f.ring.close()
+    return out
 
 
 def flush_l2(be, scratch):
@@ -499,6 +582,8 @@ def main():
     e2e_val = dist.world * work.batch * args.steps / (e2e_ms * 1e-3)
     roof = kernel_roofline(be, work.ring, work.base, 20, peaks)
     crt = None if args.no_crt_batch else crt_batch_bench(be, max(3, args.steps // 2), args.warmup)
+    hcrt = None if args.no_homcrt else homcrt_bench(be)
+    srv = None if args.no_serving else serving_bench(be)
 
     if dist.rank != 0:
         return
@@ -531,6 +616,10 @@ def main():
     }
     if crt:
         line["crt_batch"] = crt
+    if hcrt:
+        line["homcrt"] = hcrt
+    if srv:
+        line["serving"] = srv
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)

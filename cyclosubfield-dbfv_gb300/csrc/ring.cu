@@ -1459,6 +1459,30 @@ hc_status hc_bfv_hom_mul(hc_ring R, const int64_t t[2], hc_view ct1, hc_view ct2
     });
 }
 
+/// B ciphertexts [2B, r] (rows 2i, 2i + 1) under one automorphism g: the gadget decomposition and
+/// the key switch each run once over the whole batch.
+hc_status hc_bfv_hom_gal_batch(hc_ring R, hc_view ct, const size_t* base, size_t r, uint64_t g, hc_view gk,
+                               const size_t* digits, size_t d, hc_view out) {
+    return guard([&] {
+        REQUIRE(R, HC_ERR_ARG, "null ring");
+        Base b = base_of(base, r);
+        const int64_t rr = (int64_t)r;
+        REQUIRE(ct.shape[0] >= 2 && ct.shape[0] % 2 == 0, HC_ERR_SHAPE, "ciphertexts must have 2 rows each");
+        const int64_t B = ct.shape[0] / 2;
+        check_view(ct, 2 * B, rr, R->dl(), R->dk(), "ciphertexts");
+        check_view(out, 2 * B, rr, R->dl(), R->dk(), "output");
+        Digits dg = clip(digits_of(digits, d), r);
+        REQUIRE(gk.shape[0] >= 2 * (int64_t)dg.size() && gk.shape[1] >= rr, HC_ERR_SHAPE, "Galois key tensor shape");
+        Tensor c1(R->ctx, B, rr, R->dl(), R->dk());
+        CK(hc_assign(R->ctx, c1.view(), vstep(ct, 1, 2, B)));
+        R->transform(c1.view(), b, true);
+        Tensor parts = gadget_decompose(R, c1.view(), b, dg);
+        hc_view c0 = vstep(ct, 0, 2, B);
+        PermCache& pc = R->perms(g);
+        keyswitch(R, parts.view(), gk, b, dg.size(), &c0, nullptr, out, pc.p2.as<uint32_t>(), pc.p3.as<uint32_t>());
+    });
+}
+
 hc_status hc_bfv_hom_gal(hc_ring R, hc_view ct, const size_t* base, size_t r, const uint64_t* gs, size_t ngs,
                          hc_view gks, const size_t* digits, size_t d, hc_view out) {
     return guard([&] {

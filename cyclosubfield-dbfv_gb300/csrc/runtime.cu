@@ -70,6 +70,17 @@ hc_status hc_event_record(hc_context ctx, hc_event ev) {
     return cuda_check(cudaEventRecord(ev->ev, stream_of(ctx)), "event record");
 }
 
+hc_status hc_event_query(hc_event ev, int* done) {
+    if (!ev || !done) return fail(HC_ERR_ARG, "null argument");
+    cudaError_t e = cudaEventQuery(ev->ev);
+    if (e == cudaErrorNotReady) {
+        *done = 0;
+        return HC_OK;
+    }
+    *done = 1;
+    return cuda_check(e, "event query");
+}
+
 hc_status hc_event_elapsed_ms(hc_event start, hc_event end, double timeout_ms, float* ms) {
     if (!start || !end || !ms) return fail(HC_ERR_ARG, "null argument");
     auto t0 = std::chrono::steady_clock::now();

@@ -400,6 +400,12 @@ class Event:
     def record(self, be):
         check(lib().hc_event_record(be.h, self.h))
 
+    def query(self):
+        """True once the work recorded before this event has completed (does not block)."""
+        done = ctypes.c_int(0)
+        check(lib().hc_event_query(self.h, ctypes.byref(done)))
+        return bool(done.value)
+
     def elapsed_ms(self, end, timeout_ms=120000.0):
         ms = ctypes.c_float()
         check(lib().hc_event_elapsed_ms(self.h, end.h, ctypes.c_double(timeout_ms), ctypes.byref(ms)))

@@ -235,6 +235,14 @@ class RingContext:
                                    rk.view(), dg, nd, ctypes.c_int(int(period_output)), out.view()))
         return out
 
+    def hom_gal_batch(self, ct, base, g, gk, digits, out=None):
+        """hc_bfv_hom_gal_batch: B ciphertexts [2B, r] under one automorphism g."""
+        out = out if out is not None else self.allocate(ct.shape[0], len(base))
+        dg, nd = _digits(digits)
+        check(lib().hc_bfv_hom_gal_batch(self.h, ct.view(), _sz(base), ctypes.c_size_t(len(base)), ctypes.c_uint64(g),
+                                         gk.view(), dg, nd, out.view()))
+        return out
+
     def hom_gal(self, ct, base, gs, gks, digits):
         out = self.allocate(2 * len(gs), len(base))
         dg, nd = _digits(digits)

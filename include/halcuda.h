@@ -180,6 +180,8 @@ hc_status hc_memset_async(hc_context ctx, void* dst, int value, size_t bytes);
 hc_status hc_event_create(hc_event* out);
 hc_status hc_event_destroy(hc_event ev);
 hc_status hc_event_record(hc_context ctx, hc_event ev);
+/* Non-blocking: *done = 1 once all work recorded before the event has completed, else 0. */
+hc_status hc_event_query(hc_event ev, int* done);
 /* Milliseconds between two recorded events; waits for `end` (bounded by `timeout_ms`, then
  * HC_ERR_TIMEOUT; timeout_ms <= 0 waits without bound). */
 hc_status hc_event_elapsed_ms(hc_event start, hc_event end, double timeout_ms, float* ms);

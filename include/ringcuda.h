@@ -99,6 +99,11 @@ hc_status hc_bfv_hom_mul(hc_ring ring, const int64_t t[2], hc_view ct1, hc_view 
 hc_status hc_bfv_hom_gal(hc_ring ring, hc_view ct, const size_t* base, size_t r, const uint64_t* gs, size_t ngs,
                          hc_view gks, const size_t* digits, size_t d, hc_view out);
 
+/* bfv_hom_gal of B ciphertexts ct [2B, r] (CRT basis) under one automorphism g with its key
+ * gk [2 d, r_key, ...] -> out [2B, r]; the batched form of hc_bfv_hom_gal with one element. */
+hc_status hc_bfv_hom_gal_batch(hc_ring ring, hc_view ct, const size_t* base, size_t r, uint64_t g, hc_view gk,
+                               const size_t* digits, size_t d, hc_view out);
+
 /* Batched CRT transforms of many ring elements of different fields and RNS lengths in one
  * persistent launch. Each item is a tensor of elements of one ring over one base; per element
  * and factor ("slab") the batch runs, as `ops` says, pb_to_crt (src/ring.rs:1118-1138), a

@@ -246,6 +246,26 @@ def test_hom_gal(rings, name, po):
         assert dec == [ptxt[int(perm[i])] for i in range(o.n)]
 
 
+@pytest.mark.parametrize("name", ["field_18", "field_36864"])
+def test_hom_gal_batch_matches_oracle(rings, name, po):
+    """B ciphertexts under one automorphism in one call: each equals the oracle's hom_gal."""
+    o, d = rings(name)
+    base = o.initial_base()
+    la = o.log2_alpha_for_sigma(base, 3.2)
+    st = [8]
+    sk = o.gen_sk(st)
+    digits = po_digits(len(base) if len(base) < 8 else len(base) // 4, len(base))
+    g = list(o.info["gens"])[0]
+    gk = o.gen_gk(st, sk, g, digits, la)
+    B = 3
+    cts = [o.enc(st, base, 16, [(i * (b + 2)) % 16 for i in range(o.n)], sk, la) for b in range(B)]
+    got = d.hom_gal_batch(d.tensor(np.concatenate(cts)), base, g, d.tensor(gk.reshape((-1,) + gk.shape[2:])),
+                          digits).to_numpy()
+    for b in range(B):
+        exp = o.hom_gal(cts[b], base, [g], gk[None], digits)[0]
+        assert (got[2 * b:2 * b + 2] == exp).all(), b
+
+
 def test_hom_mul_batched_matches_single(po, be):
     """B ciphertext pairs stacked along dimension 0 in one call give the per-pair results."""
     import ringcuda
