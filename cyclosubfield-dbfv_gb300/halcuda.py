@@ -31,6 +31,16 @@ class HcModulus(ctypes.Structure):
 _lib = None
 
 
+def lib_path():
+    """Path of libhalcuda.so, built first if it is missing or stale (nothing is loaded)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("_halcuda_build", os.path.join(HERE, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build()
+
+
 def lib():
     """Loads libhalcuda.so (building it first if it is missing or stale)."""
     global _lib
