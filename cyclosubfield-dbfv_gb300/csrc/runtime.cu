@@ -70,6 +70,20 @@ hc_status hc_event_record(hc_context ctx, hc_event ev) {
     return cuda_check(cudaEventRecord(ev->ev, stream_of(ctx)), "event record");
 }
 
+hc_status hc_stream_create(void** out) {
+    if (!out) return fail(HC_ERR_ARG, "null argument");
+    cudaStream_t s = nullptr;
+    hc_status st = cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream creation");
+    *out = st ? nullptr : (void*)s;
+    return st;
+}
+
+hc_status hc_stream_destroy(void* stream) {
+    if (!stream) return HC_OK;
+    cudaStreamSynchronize((cudaStream_t)stream);
+    return cuda_check(cudaStreamDestroy((cudaStream_t)stream), "stream destroy");
+}
+
 hc_status hc_event_query(hc_event ev, int* done) {
     if (!ev || !done) return fail(HC_ERR_ARG, "null argument");
     cudaError_t e = cudaEventQuery(ev->ev);

@@ -206,6 +206,22 @@ class CudaBackend:
     def synchronize(self):
         check(lib().hc_synchronize(self.h))
 
+    def set_stream(self, stream):
+        """Routes subsequent calls to `stream` (a Stream), or back to the context's own stream (None)."""
+        check(lib().hc_context_set_stream(self.h, stream.h if stream is not None else None))
+
+    def on(self, stream):
+        be = self
+
+        class _Use:
+            def __enter__(self):
+                be.set_stream(stream)
+
+            def __exit__(self, *exc):
+                be.set_stream(None)
+
+        return _Use()
+
     def launch_count(self):
         return int(lib().hc_launch_count(self.h))
 
@@ -399,6 +415,26 @@ def memcpy_async(be, dst_ptr, src_ptr, nbytes, kind):
 
 def memset_async(be, dst_ptr, value, nbytes):
     check(lib().hc_memset_async(be.h, ctypes.c_void_p(dst_ptr), ctypes.c_int(value), ctypes.c_size_t(nbytes)))
+
+
+class Stream:
+    """An extra CUDA stream; `with be.on(stream):` routes the calls inside to it."""
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        check(lib().hc_stream_create(ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().hc_stream_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Event:

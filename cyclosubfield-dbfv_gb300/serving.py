@@ -15,9 +15,12 @@ The engine runs one host loop:
     submission rounds are queued on it at a time, and requests that arrive meanwhile gather on
     the host, to be admitted and submitted together as soon as a round finishes - the device
     queue stays full while batches grow with the load;
+  * the batches of a round go round-robin to `streams` CUDA streams, so that independent batches
+    (small levels fill only part of the GPU) run concurrently;
   * completion is detected by polling one event per batch; the latency of a request is the time
     from its arrival to the completion of its batch.
-The plain form submits every request alone, in arrival order, through the same loop.
+The plain form submits every request alone, in arrival order, on one stream, through the same
+loop.
 """
 import collections
 import math
@@ -101,12 +104,24 @@ def make_stream(n, rate, mix, fields, levels, pool_size, seed):
 
 
 class Engine:
-    def __init__(self, be, fields, hbm_budget_bytes, max_batch=64, max_rounds=2):
+    def __init__(self, be, fields, hbm_budget_bytes, max_batch=64, max_rounds=2, streams=4):
         self.be = be
         self.fields = fields
         self.budget = int(hbm_budget_bytes)
         self.max_batch = max_batch
         self.max_rounds = max_rounds
+        self.streams = [halcuda.Stream() for _ in range(max(0, streams))]
+        self.next_stream = 0
+
+    def submit_on_stream(self, reqs, use_streams):
+        """submit() on the next extra stream (round robin) or on the context's own stream; the
+        batch's temporaries are released on the stream they were used on."""
+        if not use_streams or not self.streams:
+            return self.submit(reqs)
+        s = self.streams[self.next_stream % len(self.streams)]
+        self.next_stream += 1
+        with self.be.on(s):
+            return self.submit(reqs)
 
     def warm(self):
         """Runs one request of every (operation, field, level) once, so that the rings' tables
@@ -215,7 +230,7 @@ class Engine:
                     else:
                         units = [[x] for x in admitted]
                     for u in units:
-                        ev = self.submit([q for q, _ in u])
+                        ev = self.submit_on_stream([q for q, _ in u], batched)
                         inflight.append((ev, [q for q, _ in u], sum(nb for _, nb in u), rnd))
                         batches += 1
                     rnd += 1

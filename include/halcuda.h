@@ -180,6 +180,10 @@ hc_status hc_memset_async(hc_context ctx, void* dst, int value, size_t bytes);
 hc_status hc_event_create(hc_event* out);
 hc_status hc_event_destroy(hc_event ev);
 hc_status hc_event_record(hc_context ctx, hc_event ev);
+/* Extra streams for concurrent work on one context: create, select with hc_context_set_stream
+ * (NULL selects the context's own stream again), destroy after their work is done. */
+hc_status hc_stream_create(void** out);
+hc_status hc_stream_destroy(void* stream);
 /* Non-blocking: *done = 1 once all work recorded before the event has completed, else 0. */
 hc_status hc_event_query(hc_event ev, int* done);
 /* Milliseconds between two recorded events; waits for `end` (bounded by `timeout_ms`, then
