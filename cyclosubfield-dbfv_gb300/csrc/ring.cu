@@ -898,6 +898,11 @@ struct Wide {
         accumulate(rs, re, src, R->scalar_tensor(base, 1).view());
         step(rs, re, sb * mp2());
     }
+    /// lhs any i64 tensor, rhs bounded by max_p (src/ring.rs:488-493)
+    void fma_unbounded(size_t rs, size_t re, const hc_view& l, const hc_view& r) {
+        accumulate(rs, re, l, r);
+        step(rs, re, (u128)maxp << 63);
+    }
     bool full(size_t row) const { return bound[row] > ((u128)minp << 63); }
     /// wide[rs..re) = sum_t lhs_t * rhs_t (fresh rows only; src/ring.rs:460-485), all operands
     /// almost reduced (bound 1)
@@ -2168,6 +2173,295 @@ hc_status hc_dbfv_hom_cyclic_transform(hc_ring R, size_t log2_b, size_t log2_t, 
         }
         if (od > 0) CK(hc_assign(R->ctx, vrows(out, 0, 2 * (int64_t)od), O.view()));
         *out_rows = 2 * od;
+    });
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------- dBFV reduction path
+// split_overflow, dbfv_reduce, dbfv_enc, dbfv_mul_convolve / dbfv_hom_mul (src/dbfv.rs:661-1143).
+// The big-integer constants are evaluated modulo 2^128 (wrapping products of the primes) and
+// modulo each prime.
+
+namespace {
+
+/// src/dbfv.rs:762-768
+i128 inv_mod_2_128(i128 q) {
+    u128 x = (u128)q, qq = (u128)q;
+    for (int i = 0; i < 6; i++) x = x * (2 - qq * x);
+    return (i128)x;
+}
+
+u128 q_mod_2_128(hc_ring R, const Base& b) {
+    u128 q = 1;
+    for (size_t i : b) q *= (u128)R->prime(i);
+    return q;
+}
+
+/// round(Q / 2^k) modulo p (Q odd: no ties)
+std::function<int64_t(int64_t)> delta_pow2(hc_ring R, const Base& b, size_t k) {
+    const u128 c = q_mod_2_128(R, b) & (((u128)1 << k) - 1);
+    const int64_t extra = c >= ((u128)1 << (k - 1)) ? 1 : 0;
+    return [c, k, extra](int64_t p) {
+        int64_t cp = (int64_t)(c % (u128)p), two = 1;
+        for (size_t i = 0; i < k; i++) two = mulm(two, 2, p);
+        return emod(mulm(emod(-cp, p), invm(two, p), p) + extra, p);
+    };
+}
+
+int64_t pow2_mod(size_t e, int64_t p) {
+    int64_t v = 1;
+    for (size_t i = 0; i < e; i++) v = mulm(v, 2, p);
+    return v;
+}
+
+/// [1, r, 1, 1] tensor of mont(mont(smallest lift)) (src/ring.rs:907-920)
+Tensor scalar_tensor_big_mont2(hc_ring R, const Base& b, const std::function<int64_t(int64_t)>& res) {
+    std::vector<int64_t> v;
+    for (size_t i : b) {
+        const int64_t p = R->prime(i);
+        v.push_back(mont_repr(mont_repr(centred(res(p), p), p), p));
+    }
+    Tensor t(R->ctx, 1, (int64_t)b.size(), 1, 1);
+    CK(hc_import(R->ctx, t.view(), v.data(), v.size()));
+    return t;
+}
+
+/// rows [s, e) of dimension 1
+hc_view dim1(hc_view v, int64_t s, int64_t e) {
+    v.ptr = (char*)v.ptr + s * v.strides[1] * 8;
+    v.shape[1] = e - s;
+    return v;
+}
+
+/// SplitOverflowData (src/dbfv.rs:735-849)
+struct SplitData {
+    size_t log2_r = 0, log2_gamma = 0;
+    i128 q_mod_r = 0, neg_q_inv_mod_r = 0;
+    Tensor rqinv, matrix;
+    std::vector<Tensor> neg_b_delta_mont2;
+    size_t limbs() const { return log2_r <= 62 ? 1 : 2; }
+    SplitData(hc_ring R, size_t log2_b, size_t log2_t, const Base& b) {
+        log2_r = log2_t - log2_b;
+        REQUIRE(log2_r >= 1 && log2_r <= 126, HC_ERR_ARG, "t/b must be between 2 and 2^126");
+        const size_t L = limbs();
+        const u128 rmask = ((u128)1 << log2_r) - 1;
+        const int64_t mx = R->max_p(b), mn = R->min_p(b);
+        log2_gamma = std::max<size_t>(64, bitlen_u128(4 * (u128)b.size() * (u128)mx + 1));
+        REQUIRE(log2_gamma <= 126, HC_ERR_UNSUPPORTED, "split overflow precision");
+        const i128 gamma = (i128)1 << log2_gamma;
+        REQUIRE((gamma / mn + 1) <= I128MAX / ((i128)mx * (i128)b.size()), HC_ERR_ARG, "split overflow matrix range");
+        std::vector<i128> qpr;
+        for (size_t i : b) {
+            u128 q = 1;
+            for (size_t j : b)
+                if (j != i) q *= (u128)R->prime(j);
+            qpr.push_back((i128)(q & rmask));
+        }
+        std::vector<int64_t> mat;
+        for (i128 c : qpr) mat.push_back((int64_t)c);  // split_i128_limbs(c).0 (src/hal/mod.rs:71-76)
+        if (L == 2)
+            for (i128 c : qpr) mat.push_back((int64_t)((c - (i128)(int64_t)c) >> 64));
+        for (size_t i : b) {
+            const i128 p = R->prime(i);
+            mat.push_back((int64_t)((gamma + p / 2) / p));
+        }
+        matrix = Tensor(R->ctx, 1, (int64_t)L + 1, (int64_t)b.size(), 1);
+        CK(hc_import(R->ctx, matrix.view(), mat.data(), mat.size()));
+        q_mod_r = (i128)(q_mod_2_128(R, b) & rmask);
+        neg_q_inv_mod_r = (i128)((u128)(-inv_mod_2_128(q_mod_r)) & rmask);
+        // smallest lifts of R (Q/p)^-1 mod p (src/ring.rs:1029-1043)
+        std::vector<int64_t> qv;
+        for (size_t i : b) {
+            const int64_t p = R->prime(i);
+            int64_t qo = 1;
+            for (size_t j : b)
+                if (j != i) qo = mulm(qo, R->prime(j) % p, p);
+            qv.push_back(centred(mulm(invm(qo, p), pow2_mod(log2_r, p), p), p));
+        }
+        rqinv = Tensor(R->ctx, 1, (int64_t)b.size(), 1, 1);
+        CK(hc_import(R->ctx, rqinv.view(), qv.data(), qv.size()));
+        auto delta = delta_pow2(R, b, log2_t);
+        for (size_t k = 0; k < L; k++)
+            neg_b_delta_mont2.push_back(scalar_tensor_big_mont2(R, b, [&](int64_t p) {
+                return emod(-mulm(mulm(delta(p), pow2_mod(log2_b, p), p), pow2_mod(64 * k, p), p), p);
+            }));
+    }
+};
+
+/// src/dbfv.rs:891-950: x <- x_lo in place; returns the overflow limbs [count, limbs, ...]
+Tensor split_overflow(hc_ring R, const SplitData& D, const hc_view& x, u128 x_bound, const Base& b) {
+    const int64_t count = x.shape[0], r = (int64_t)b.size(), L = (int64_t)D.limbs();
+    std::vector<hc_modulus> m = R->mods(b);
+    Tensor lifts(R->ctx, count, r, R->dl(), R->dk(), false, false);
+    CK(hc_assign(R->ctx, lifts.view(), x));
+    CK(hc_mul_mont64(R->ctx, lifts.view(), D.rqinv.view(), m.data(), m.size()));
+    Tensor sums(R->ctx, count, L + 1, R->dl(), R->dk(), true, false);
+    CK(hc_matmul_i64(R->ctx, sums.view(), D.matrix.view(), lifts.view()));
+    Tensor overflow(R->ctx, count, L, R->dl(), R->dk(), false, false);
+    if (L == 1) {
+        CK(hc_bconv_correct_pow2(R->ctx, overflow.view(), sums.view(), (int64_t)D.q_mod_r, (int64_t)D.neg_q_inv_mod_r,
+                                 D.log2_gamma, D.log2_r));
+    } else {
+        const int64_t f0[2] = {(int64_t)(uint64_t)D.q_mod_r, (int64_t)(D.q_mod_r >> 64)};
+        const int64_t f1[2] = {(int64_t)(uint64_t)D.neg_q_inv_mod_r, (int64_t)(D.neg_q_inv_mod_r >> 64)};
+        CK(hc_bconv_correct_pow2_wide(R->ctx, overflow.view(), sums.view(), f0, f1, D.log2_gamma, D.log2_r));
+    }
+    Wide acc(R, count, b);
+    for (int64_t k = 0; k < L; k++) acc.fma_unbounded(0, (size_t)count, dim1(overflow.view(), k, k + 1), D.neg_b_delta_mont2[(size_t)k].view());
+    acc.add(0, (size_t)count, x, x_bound);
+    acc.reduce_into(x);
+    return overflow;
+}
+
+/// src/dbfv.rs:968-1032, period basis in and out; returns the [2 digits, r] result
+Tensor dbfv_reduce(hc_ring R, size_t log2_b, size_t log2_t, const hc_view& ct, u128 bound, const Base& b,
+                   size_t* rows_out) {
+    const size_t digits = (log2_t - 1) / log2_b + 1, d = (size_t)ct.shape[0] / 2;
+    REQUIRE(d <= digits, HC_ERR_SHAPE, "ciphertext has more digits than the modulus");
+    const int64_t rr = (int64_t)b.size();
+    if (digits == 1 || d == 0) {
+        Tensor out(R->ctx, 2 * (int64_t)d, rr, R->dl(), R->dk(), false, false);
+        if (d) CK(hc_assign(R->ctx, out.view(), ct));
+        *rows_out = 2 * d;
+        return out;
+    }
+    SplitData D(R, log2_b, log2_t, b);
+    auto delta = delta_pow2(R, b, log2_t);
+    std::vector<Tensor> delta_mont2;
+    for (size_t k = 0; k < D.limbs(); k++)
+        delta_mont2.push_back(scalar_tensor_big_mont2(R, b, [&](int64_t p) { return mulm(delta(p), pow2_mod(64 * k, p), p); }));
+    Tensor result(R->ctx, 2 * (int64_t)digits, rr, R->dl(), R->dk());
+    CK(hc_assign(R->ctx, vrows(result.view(), 0, 2 * (int64_t)d), ct));
+    Tensor carry;
+    bool have = false;
+    for (size_t i = 0; i < digits; i++) {
+        const u128 in_bound = i < d ? bound : 1;
+        hc_view rows = vrows(result.view(), 2 * (int64_t)i, 2 * (int64_t)i + 2);
+        if (have) {
+            Wide acc(R, 2, b);
+            for (size_t k = 0; k < delta_mont2.size(); k++)
+                acc.fma_unbounded(0, 2, dim1(carry.view(), (int64_t)k, (int64_t)k + 1), delta_mont2[k].view());
+            acc.add(0, 2, rows, in_bound);
+            acc.reduce_into(rows);
+        }
+        carry = split_overflow(R, D, rows, have ? 1 : in_bound, b);
+        have = true;
+    }
+    *rows_out = 2 * digits;
+    return result;
+}
+
+}  // namespace
+
+extern "C" {
+
+hc_status hc_dbfv_reduce(hc_ring R, size_t log2_b, size_t log2_t, hc_view ct, const size_t* base, size_t r,
+                         uint64_t bound, hc_view out, size_t* out_rows) {
+    return guard([&] {
+        REQUIRE(R && out_rows, HC_ERR_ARG, "null argument");
+        REQUIRE(log2_b >= 1 && log2_t >= 1 && log2_t <= 126, HC_ERR_ARG, "t = 2^log2_t must be between 2 and 2^126");
+        Base b = base_of(base, r);
+        REQUIRE(ct.shape[0] % 2 == 0, HC_ERR_SHAPE, "dBFV ciphertext rows");
+        check_view(ct, ct.shape[0], (int64_t)r, R->dl(), R->dk(), "dBFV ciphertext");
+        size_t rows = 0;
+        Tensor res = dbfv_reduce(R, log2_b, log2_t, ct, bound, b, &rows);
+        REQUIRE(out.shape[0] >= (int64_t)rows, HC_ERR_SHAPE, "output has too few rows");
+        check_view(out, out.shape[0], (int64_t)r, R->dl(), R->dk(), "output");
+        if (rows) CK(hc_assign(R->ctx, vrows(out, 0, (int64_t)rows), res.view()));
+        *out_rows = rows;
+    });
+}
+
+hc_status hc_dbfv_enc(hc_ring R, uint64_t* st, size_t log2_b, size_t log2_t, const size_t* base, size_t r,
+                      const int64_t* ptxt, hc_view sk, double log2_alpha, hc_view out) {
+    return guard([&] {
+        REQUIRE(R && st && ptxt, HC_ERR_ARG, "null argument");
+        REQUIRE(log2_b >= 1 && log2_t >= 1 && log2_t <= 126, HC_ERR_ARG, "t = 2^log2_t must be between 2 and 2^126");
+        const size_t digits = (log2_t - 1) / log2_b + 1;
+        Base b = base_of(base, r);
+        const int64_t rr = (int64_t)r;
+        check_view(out, 2 * (int64_t)digits, rr, R->dl(), R->dk(), "dBFV ciphertext");
+        const double la = log2_alpha + (double)(log2_b * (digits - 1));  // src/dbfv.rs:602-604
+        const i128 t = (i128)1 << log2_t;
+        const int64_t tw[2] = {(int64_t)(uint64_t)t, (int64_t)(t >> 64)};
+        CK(hc_bfv_enc(R, st, base, r, tw, ptxt, sk, la, vrows(out, 0, 2)));
+        if (digits == 1) return;
+        for (size_t i = 1; i < digits; i++) enc_zero(R, b, sk, st, la, vrows(out, 2 * (int64_t)i, 2 * (int64_t)i + 2));
+        Tensor pb(R->ctx, 2 * (int64_t)digits, rr, R->dl(), R->dk(), false, false);
+        CK(hc_assign(R->ctx, pb.view(), out));
+        R->transform(pb.view(), b, true);
+        size_t rows = 0;
+        Tensor red = dbfv_reduce(R, log2_b, log2_t, pb.view(), 1, b, &rows);
+        R->transform(red.view(), b, false);
+        CK(hc_assign(R->ctx, out, red.view()));
+        CK(hc_synchronize(R->ctx));
+    });
+}
+
+hc_status hc_dbfv_hom_mul(hc_ring R, size_t log2_b, size_t log2_t, hc_view lhs, hc_view rhs, const size_t* base, size_t r,
+                          hc_view rk, const size_t* digits, size_t d, int period_output, hc_view out, size_t* out_rows) {
+    return guard([&] {
+        REQUIRE(R && out_rows, HC_ERR_ARG, "null argument");
+        REQUIRE(log2_b >= 1 && log2_t >= 1 && log2_t <= 126, HC_ERR_ARG, "t = 2^log2_t must be between 2 and 2^126");
+        const size_t mdig = (log2_t - 1) / log2_b + 1;
+        Base b = base_of(base, r);
+        const int64_t rr = (int64_t)r;
+        REQUIRE(lhs.shape[0] % 2 == 0 && rhs.shape[0] % 2 == 0, HC_ERR_SHAPE, "dBFV ciphertext rows");
+        check_view(lhs, lhs.shape[0], rr, R->dl(), R->dk(), "lhs");
+        check_view(rhs, rhs.shape[0], rr, R->dl(), R->dk(), "rhs");
+        size_t r1 = 0, r2 = 0;
+        Tensor l = dbfv_reduce(R, log2_b, log2_t, lhs, 1, b, &r1), rt = dbfv_reduce(R, log2_b, log2_t, rhs, 1, b, &r2);
+        *out_rows = 0;
+        if (r1 == 0 || r2 == 0) return;
+        const size_t d1 = r1 / 2, d2 = r2 / 2, d_out = std::min(mdig, d1 + d2 - 1);
+        check_view(out, out.shape[0], rr, R->dl(), R->dk(), "output");
+        REQUIRE(out.shape[0] >= 2 * (int64_t)d_out, HC_ERR_SHAPE, "output has too few rows");
+        Tensor ll = lift_to_extended(R, vrows(l.view(), 0, (int64_t)r1), nullptr, b);
+        Tensor rl = lift_to_extended(R, vrows(rt.view(), 0, (int64_t)r2), nullptr, b);
+        Base lifted = b;
+        for (int64_t i = rr; i < ll.shape[1]; i++) lifted.push_back(R->initial_len + (size_t)(i - rr));
+        // all 3-component digit products, rows 3k .. 3k + 3 for output digit k (src/dbfv.rs:1081-1126)
+        Wide acc(R, 3 * (int64_t)d_out, lifted);
+        auto row = [](const Tensor& t, size_t i) { return vrows(t.view(), (int64_t)i, (int64_t)i + 1); };
+        for (size_t k = 0; k < d_out; k++) {
+            std::vector<hc_view> a0, b0, a1, b1, a2, b2;
+            const size_t jlo = k >= d2 - 1 ? k - (d2 - 1) : 0, jhi = std::min(k, d1 - 1);
+            for (size_t j = jlo; j <= jhi; j++) {
+                a0.push_back(row(ll, 2 * j)), b0.push_back(row(rl, 2 * (k - j)));
+                a1.push_back(row(ll, 2 * j)), b1.push_back(row(rl, 2 * (k - j) + 1));
+                a1.push_back(row(ll, 2 * j + 1)), b1.push_back(row(rl, 2 * (k - j)));
+                a2.push_back(row(ll, 2 * j + 1)), b2.push_back(row(rl, 2 * (k - j) + 1));
+            }
+            acc.inner_product(3 * k, 3 * k + 1, a0, b0);
+            acc.inner_product(3 * k + 1, 3 * k + 2, a1, b1);
+            acc.inner_product(3 * k + 2, 3 * k + 3, a2, b2);
+        }
+        Tensor prod(R->ctx, 3 * (int64_t)d_out, (int64_t)lifted.size(), R->dl(), R->dk(), false, false);
+        acc.reduce_into(prod.view());
+        R->transform(prod.view(), lifted, true);
+        const i128 t = (i128)1 << log2_t;
+        Tensor resc = rescale_to_base(R, prod.view(), lifted, r, t);
+        // relinearisation of every output digit at once (src/bfv.rs:699-741)
+        const int64_t D = (int64_t)d_out;
+        Digits dg = clip(digits_of(digits, d), r);
+        REQUIRE(rk.shape[0] >= 2 * (int64_t)dg.size() && rk.shape[1] >= rr, HC_ERR_SHAPE, "relinearisation key shape");
+        Tensor c2(R->ctx, D, rr, R->dl(), R->dk(), false, false);
+        CK(hc_assign(R->ctx, c2.view(), vstep(resc.view(), 2, 3, D)));
+        Tensor parts = gadget_decompose(R, c2.view(), b, dg);
+        hc_view c0 = vstep(resc.view(), 0, 3, D), c1 = vstep(resc.view(), 1, 3, D);
+        hc_view o = vrows(out, 0, 2 * D);
+        if (!period_output) {
+            R->transform(c0, b, false);
+            R->transform(c1, b, false);
+            keyswitch(R, parts.view(), rk, b, dg.size(), &c0, &c1, o);
+        } else {
+            keyswitch(R, parts.view(), rk, b, dg.size(), nullptr, nullptr, o);
+            R->transform(o, b, true);
+            CK(hc_add_i64(R->ctx, vstep(o, 0, 2, D), c0));
+            CK(hc_add_i64(R->ctx, vstep(o, 1, 2, D), c1));
+        }
+        *out_rows = 2 * d_out;
     });
 }
 

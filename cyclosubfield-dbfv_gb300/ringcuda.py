@@ -385,3 +385,40 @@ def dbfv_hom_cyclic_transform(ring, log2_b, log2_t, g, coeffs, ct, base, ks):
                                              ct.view(), _sz(base), ctypes.c_size_t(len(base)), ks.h, out.view(),
                                              ctypes.byref(rows)))
     return out.rows(0, rows.value)
+
+
+def dbfv_digits(log2_b, log2_t):
+    return (log2_t - 1) // log2_b + 1
+
+
+def dbfv_enc(ring, state, log2_b, log2_t, base, ptxt, sk, log2_alpha):
+    """hc_dbfv_enc: [2 digits, r] CRT-basis dBFV ciphertext"""
+    st = (ctypes.c_uint64 * 1)(state[0])
+    words = np.zeros((ring.n, 2), dtype=np.int64)
+    for i, v in enumerate(ptxt):
+        w = _i128(v)
+        words[i, 0], words[i, 1] = w[0], w[1]
+    out = ring.allocate(2 * dbfv_digits(log2_b, log2_t), len(base))
+    check(lib().hc_dbfv_enc(ring.h, st, ctypes.c_size_t(log2_b), ctypes.c_size_t(log2_t), _sz(base),
+                            ctypes.c_size_t(len(base)), words.ctypes.data_as(ctypes.c_void_p), sk.view(),
+                            ctypes.c_double(log2_alpha), out.view()))
+    state[0] = int(st[0])
+    return out
+
+
+def dbfv_reduce(ring, log2_b, log2_t, ct_pb, base, bound=1):
+    out = ring.allocate(max(2 * dbfv_digits(log2_b, log2_t), ct_pb.shape[0]), len(base))
+    rows = ctypes.c_size_t(0)
+    check(lib().hc_dbfv_reduce(ring.h, ctypes.c_size_t(log2_b), ctypes.c_size_t(log2_t), ct_pb.view(), _sz(base),
+                               ctypes.c_size_t(len(base)), ctypes.c_uint64(bound), out.view(), ctypes.byref(rows)))
+    return out.rows(0, rows.value)
+
+
+def dbfv_hom_mul(ring, log2_b, log2_t, lhs_pb, rhs_pb, base, rk, digits, period_output=False):
+    out = ring.allocate(2 * dbfv_digits(log2_b, log2_t), len(base))
+    rows = ctypes.c_size_t(0)
+    dg, nd = _digits(digits)
+    check(lib().hc_dbfv_hom_mul(ring.h, ctypes.c_size_t(log2_b), ctypes.c_size_t(log2_t), lhs_pb.view(), rhs_pb.view(),
+                                _sz(base), ctypes.c_size_t(len(base)), rk.view(), dg, nd,
+                                ctypes.c_int(int(period_output)), out.view(), ctypes.byref(rows)))
+    return out.rows(0, rows.value)

@@ -167,6 +167,21 @@ hc_status hc_dbfv_hom_cyclic_transform(hc_ring ring, size_t log2_b, size_t log2_
                                        size_t len, hc_view ct, const size_t* base, size_t r, hc_keyset ks, hc_view out,
                                        size_t* out_rows);
 
+/* dBFV reduction path (src/dbfv.rs:661-1143): t = 2^log2_t in digits of b = 2^log2_b.
+ * dbfv_reduce (:968-1032): ct [2 d, r] period basis with entries bounded by `bound` p -> out (at
+ * least 2 digits rows; *out_rows written), every digit reduced modulo b Delta with its overflow
+ * carried into the next digit (split_overflow, :891-950). */
+hc_status hc_dbfv_reduce(hc_ring ring, size_t log2_b, size_t log2_t, hc_view ct, const size_t* base, size_t r,
+                         uint64_t bound, hc_view out, size_t* out_rows);
+/* dbfv_enc (:661-689): n i128 plaintext coefficients -> out [2 digits, r] CRT basis */
+hc_status hc_dbfv_enc(hc_ring ring, uint64_t* rng_state, size_t log2_b, size_t log2_t, const size_t* base, size_t r,
+                      const int64_t* ptxt, hc_view sk, double log2_alpha, hc_view out);
+/* dbfv_hom_mul (:1034-1059, digit convolution :1081-1143): lhs [2 d1, r], rhs [2 d2, r] period
+ * basis -> out (CRT basis, or period basis when period_output), *out_rows = 2 min(digits, d1 + d2 - 1) */
+hc_status hc_dbfv_hom_mul(hc_ring ring, size_t log2_b, size_t log2_t, hc_view lhs, hc_view rhs, const size_t* base,
+                          size_t r, hc_view rk, const size_t* digits, size_t d, int period_output, hc_view out,
+                          size_t* out_rows);
+
 /* No counterpart in the reference (its CPU backend allocates freely): hc_bfv_key_switch with the
  * same arguments and the same result, for callers that cannot allocate device memory - a host
  * whose HBM is handed out by its own arena or budget, or a code path where cudaMalloc / cudaFree

@@ -435,6 +435,49 @@ int or_bfv_hom_gal(void* h, const int64_t* ct, const size_t* base, size_t r, con
         }
     });
 }
+/// dbfv_enc (src/dbfv.rs:661-689): out [2 digits, r] CRT basis
+int or_dbfv_enc(void* h, uint64_t* state, size_t log2_b, size_t log2_t, const size_t* base, size_t r,
+                const int64_t* ptxt, const int64_t* sk, double log2_alpha, int64_t* out) {
+    return guarded([&] {
+        RingContext& ring = *((BfvHandle*)h)->ring;
+        Bfv bfv(ring, state);
+        RingEls s = els_from(ring, sk, 1, ring.initial_rns_base(), Basis::CRTBasis);
+        std::vector<i128> m(ring.n());
+        for (size_t i = 0; i < m.size(); i++) m[i] = (i128)(((u128)(uint64_t)ptxt[2 * i + 1] << 64) | (uint64_t)ptxt[2 * i]);
+        els_to(dbfv_enc(ring, bfv, DBFVModulus{log2_b, log2_t}, base_from(base, r), m, s, log2_alpha), out);
+    });
+}
+/// dbfv_reduce (src/dbfv.rs:968-1032): ct [2 d, r] period basis with entries bounded by
+/// `bound` p -> out [2 digits, r] period basis (*out_rows rows)
+int or_dbfv_reduce(void* h, size_t log2_b, size_t log2_t, const int64_t* ct, size_t d, const size_t* base, size_t r,
+                   uint64_t bound, int64_t* out, size_t* out_rows) {
+    return guarded([&] {
+        RingContext& ring = *((BfvHandle*)h)->ring;
+        RingEls c = els_from(ring, ct, 2 * d, base_from(base, r), Basis::PeriodBasis);
+        c.bound = bound;
+        RingEls res = dbfv_reduce(ring, DBFVModulus{log2_b, log2_t}, as_view(c));
+        els_to(res, out);
+        *out_rows = res.count();
+    });
+}
+/// dbfv_hom_mul (src/dbfv.rs:1034-1059): lhs [2 d1, r], rhs [2 d2, r] period basis -> out
+/// (CRT basis, or period basis when period_output) with *out_rows rows
+int or_dbfv_hom_mul(void* h, size_t log2_b, size_t log2_t, const int64_t* lhs, size_t d1, const int64_t* rhs, size_t d2,
+                    const size_t* base, size_t r, const int64_t* rk, const size_t* digits, size_t dk, size_t r_key,
+                    int period_output, int64_t* out, size_t* out_rows) {
+    return guarded([&] {
+        RingContext& ring = *((BfvHandle*)h)->ring;
+        uint64_t st = 0;
+        Bfv bfv(ring, &st);
+        Base b = base_from(base, r);
+        RingEls l = els_from(ring, lhs, 2 * d1, b, Basis::PeriodBasis), rr = els_from(ring, rhs, 2 * d2, b, Basis::PeriodBasis);
+        KeySwitchKey k = key_from(ring, rk, dk, digits_from(digits, dk), r_key);
+        RingEls res = dbfv_hom_mul(ring, bfv, DBFVModulus{log2_b, log2_t}, as_view(l), as_view(rr), k,
+                                   period_output ? Basis::PeriodBasis : Basis::CRTBasis);
+        els_to(res, out);
+        *out_rows = res.count();
+    });
+}
 /// lprime_element_tensor (src/ring.rs:1227-1250): deg_L' i128 coefficients (low, high words)
 /// -> out [1, r, deg_L', 1] CRT basis, Montgomery form
 int or_ring_lprime_element_tensor(void* h, const size_t* base, size_t r, const int64_t* coeffs, int64_t* out) {

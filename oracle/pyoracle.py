@@ -476,6 +476,56 @@ class Ring:
               ctypes.c_size_t(keys.shape[3]), _p(out))
         return out
 
+    def dbfv_enc(self, state, log2_b, log2_t, base, ptxt, sk, log2_alpha):
+        """dbfv_enc (src/dbfv.rs:661-689): [2 digits, r, ...] CRT basis"""
+        st = np.array([state[0]], dtype=np.uint64)
+        digits = (log2_t - 1) // log2_b + 1
+        m = to_i128(ptxt)
+        b = _sz(base)
+        out = self.zeros(2 * digits, len(base))
+        _call("or_dbfv_enc", self.h, _p(st), ctypes.c_size_t(log2_b), ctypes.c_size_t(log2_t), _p(b),
+              ctypes.c_size_t(len(b)), _p(m), _p(np.ascontiguousarray(sk)), ctypes.c_double(log2_alpha), _p(out))
+        state[0] = int(st[0])
+        return out
+
+    def dbfv_reduce(self, log2_b, log2_t, ct_pb, base, bound=1):
+        """dbfv_reduce (src/dbfv.rs:968-1032), period basis in and out"""
+        ct = np.ascontiguousarray(ct_pb, dtype=np.int64)
+        digits = (log2_t - 1) // log2_b + 1
+        out = self.zeros(max(2 * digits, ct.shape[0]), len(base))
+        rows = ctypes.c_size_t(0)
+        b = _sz(base)
+        _call("or_dbfv_reduce", self.h, ctypes.c_size_t(log2_b), ctypes.c_size_t(log2_t), _p(ct),
+              ctypes.c_size_t(ct.shape[0] // 2), _p(b), ctypes.c_size_t(len(b)), ctypes.c_uint64(bound), _p(out),
+              ctypes.byref(rows))
+        return out[:rows.value]
+
+    def dbfv_hom_mul(self, log2_b, log2_t, lhs_pb, rhs_pb, base, rk, digits, period_output=False):
+        """dbfv_hom_mul (src/dbfv.rs:1034-1059): period-basis operands"""
+        l = np.ascontiguousarray(lhs_pb, dtype=np.int64)
+        r = np.ascontiguousarray(rhs_pb, dtype=np.int64)
+        md = (log2_t - 1) // log2_b + 1
+        out = self.zeros(2 * md, len(base))
+        rows = ctypes.c_size_t(0)
+        b = _sz(base)
+        dg = self._digits(digits)
+        _call("or_dbfv_hom_mul", self.h, ctypes.c_size_t(log2_b), ctypes.c_size_t(log2_t), _p(l),
+              ctypes.c_size_t(l.shape[0] // 2), _p(r), ctypes.c_size_t(r.shape[0] // 2), _p(b), ctypes.c_size_t(len(b)),
+              _p(np.ascontiguousarray(rk)), _p(dg), ctypes.c_size_t(len(digits)), ctypes.c_size_t(rk.shape[2]),
+              ctypes.c_int(int(period_output)), _p(out), ctypes.byref(rows))
+        return out[:rows.value]
+
+    def dbfv_decrypt(self, ct_crt, base, sk, log2_b, log2_t):
+        """dbfv_dec (src/dbfv.rs:699-722) on a CRT-basis ciphertext: centred plaintext coefficients"""
+        t = 1 << log2_t
+        res = [0] * self.n
+        for i in range(ct_crt.shape[0] // 2):
+            part = self.decrypt(ct_crt[2 * i:2 * i + 2], base, sk, t)
+            mod_i = 1 << (log2_t - i * log2_b)
+            for j in range(self.n):
+                res[j] += cmod(part[j], mod_i) << (i * log2_b)
+        return [cmod(v, t) for v in res]
+
     def lprime_element_tensor(self, base, coeffs):
         """[1, r, deg_L', 1] CRT-basis tensor of an L' element (src/ring.rs:1227-1250)."""
         b = _sz(base)

@@ -82,3 +82,48 @@ def test_hom_cyclic_transform_decrypts_to_plain_transform(po, length, log2_b, lo
     plain = np.concatenate([acc, np.zeros_like(acc)], axis=0)
     exp = [cmod(v, t) for v in o.decrypt(plain, base, sk, t)]
     assert got == exp
+
+
+# ---- the dBFV reduction path (src/dbfv.rs:735-1143), pinned by decryption ----
+
+DBFV_CASES = [("field_192", 200, 220, 4, 8), ("field_192", 300, 320, 8, 24), ("field_18", 400, 420, 16, 64),
+              ("field_18", 520, 540, 32, 96)]
+
+
+def _dbfv_setup(po, field, lo, hi, seed):
+    o = po.Ring(field, lo, hi, 4)
+    base = o.initial_base()
+    la = o.log2_alpha_for_sigma(base, 3.2)
+    st = [seed]
+    sk = o.gen_sk(st)
+    return o, base, la, st, sk
+
+
+@pytest.mark.parametrize("field,lo,hi,log2_b,log2_t", DBFV_CASES)
+def test_dbfv_enc_dec_and_reduce(po, field, lo, hi, log2_b, log2_t):
+    o, base, la, st, sk = _dbfv_setup(po, field, lo, hi, 31)
+    t = 1 << log2_t
+    rng = np.random.default_rng(log2_t)
+    msg = [int(v) for v in rng.integers(0, 1 << min(62, log2_t), size=o.n)]
+    if log2_t > 62:
+        msg = [(v << (log2_t - 62)) + 12345 for v in msg]
+    ct = o.dbfv_enc(st, log2_b, log2_t, base, msg, sk, la)
+    assert ct.shape[0] == 2 * ((log2_t - 1) // log2_b + 1)
+    assert o.dbfv_decrypt(ct, base, sk, log2_b, log2_t) == [cmod(v, t) for v in msg]
+    # reducing again (from period basis) keeps the plaintext
+    red = o.dbfv_reduce(log2_b, log2_t, o.crt_to_pb(ct, base), base)
+    assert o.dbfv_decrypt(o.pb_to_crt(red, base), base, sk, log2_b, log2_t) == [cmod(v, t) for v in msg]
+
+
+@pytest.mark.parametrize("field,lo,hi,log2_b,log2_t", DBFV_CASES)
+def test_dbfv_hom_mul_decrypts_to_the_product(po, field, lo, hi, log2_b, log2_t):
+    o, base, la, st, sk = _dbfv_setup(po, field, lo, hi, 32)
+    t = 1 << log2_t
+    digits = po.select_digits(len(base), len(base))
+    rk = o.gen_rk(st, sk, digits, la)
+    a, b = 5 + (1 << (log2_t // 2)), 7 + (1 << (log2_t // 3))
+    c1 = o.crt_to_pb(o.dbfv_enc(st, log2_b, log2_t, base, o.encode_scalar(a), sk, la), base)
+    c2 = o.crt_to_pb(o.dbfv_enc(st, log2_b, log2_t, base, o.encode_scalar(b), sk, la), base)
+    res = o.dbfv_hom_mul(log2_b, log2_t, c1, c2, base, rk, digits)
+    dec = o.dbfv_decrypt(res, base, sk, log2_b, log2_t)
+    assert o.decode_scalar(t, dec) == cmod(a * b, t)
