@@ -14,6 +14,8 @@
 #include <cstring>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 
 namespace {
@@ -575,6 +577,40 @@ __global__ void __launch_bounds__(THREADS, MINB) ntt_line_kernel(KView t, PlanPt
     run_line<SHAPE, MODE, FIX>(P, c, smem, g, mulp, me, mn, mi);
 }
 
+/// [3, 64, 64] lines along dimension 3 as 3-CTA clusters: CTA `blk` of a cluster computes block
+/// blk (4096 residues) of one line.
+template <int MODE, bool FIX>
+__global__ void __cluster_dims__(3, 1, 1) __launch_bounds__(128, 5)
+    ntt_line3_kernel(KView t, PlanPtrs plans, KView mul, KMods mods) {
+    extern __shared__ int64_t smem[];
+    const int64_t tile = blockIdx.x / 3;
+    const int blk = (int)(blockIdx.x % 3);
+    const int64_t k = tile % t.n2, r = tile / t.n2;
+    const int64_t j = r % t.n1, i = r / t.n1;
+    const DevPlanHeader* P = plans.p[j];
+    int64_t* tws = smem + 4608;
+    stage_twiddles(P, tws);
+    __syncthreads();
+    const fast::Ctx c = make_ctx(P, tws);
+    int64_t* g = reinterpret_cast<int64_t*>(t.p) + i * t.s0 + j * t.s1 + k * t.s2;
+    const int64_t* mulp = nullptr;
+    int64_t me = 0, mn = 0, mi = 0;
+    if (MODE == 2) {
+        mulp = kat<int64_t>(mul, i, j, k, 0);
+        me = mul.b3 ? 0 : 1;
+        mn = mods.n[j], mi = mods.ninv[j];
+    }
+    auto csync = [] { cooperative_groups::this_cluster().sync(); };
+    const DevStage* st = (MODE & 1) ? P->inv : P->fwd;
+    if constexpr (FIX) {
+        const FixedSched<HC_SHAPE_L12288, (MODE & 1) != 0> sch{st};
+        fast::line12288_block<MODE>(sch, c, smem, g, blk, mulp, me, mn, mi, csync);
+    } else {
+        const fast::DynSched sch{st};
+        fast::line12288_block<MODE>(sch, c, smem, g, blk, mulp, me, mn, mi, csync);
+    }
+}
+
 /// One specialised column (global element stride ge) of shape SHAPE, in registers.
 template <int SHAPE, int MODE, bool FIX>
 __device__ __forceinline__ void run_column(const DevPlanHeader* P, const fast::Ctx& c, int64_t* g, int64_t ge,
@@ -653,7 +689,15 @@ __global__ void __launch_bounds__(HC_COL_THREADS, SHAPE == HC_SHAPE_C12 ? 2 : 4)
 template <int SHAPE, int MODE, bool FIX>
 hc_status launch_special(hc_context ctx, const KView& t, const PlanPtrs& pp, const KView& mul, const KMods& mods,
                          size_t smem, int64_t tiles, int ncb) {
-    if constexpr (SHAPE == HC_SHAPE_L3072 || SHAPE == HC_SHAPE_L12288) {
+    if constexpr (SHAPE == HC_SHAPE_L12288) {
+        // one 3-CTA cluster per line: padded 4096-residue block + twiddles per CTA
+        const size_t smem3 = smem - ((size_t)line_tile_words(SHAPE) - 4608) * 8;
+        auto kern = ntt_line3_kernel<MODE, FIX>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3);
+        if (e != cudaSuccess) return hc::cuda_check(e, "ntt smem attribute");
+        if (tiles * 3 > 0x7fffffff) return hc::fail(HC_ERR_UNSUPPORTED, "too many NTT lines in one call");
+        kern<<<(unsigned)(tiles * 3), 128, smem3, hc::stream_of(ctx)>>>(t, pp, mul, mods);
+    } else if constexpr (SHAPE == HC_SHAPE_L3072) {
         constexpr int TH = SHAPE == HC_SHAPE_L3072 ? 128 : 256, MB = SHAPE == HC_SHAPE_L3072 ? 6 : 2;
         auto kern = ntt_line_kernel<SHAPE, MODE, FIX, TH, MB>;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

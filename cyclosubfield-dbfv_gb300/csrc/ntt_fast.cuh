@@ -400,6 +400,103 @@ __device__ __forceinline__ void line12288(const SCH& sch, const Ctx& c, int64_t*
     line_store(s, g, 12288, MODE & 2, mulp, me, mn, mi);
 }
 
+/// One of the three 4096-residue blocks of a [3, 64, 64] line, computed by one CTA of a 3-CTA
+/// cluster: the factor-3 stage couples the blocks, but each output of a radix-3 butterfly needs
+/// only its own two twiddle products, so the CTA of block `blk` reads all three inputs of its
+/// positions and computes just its output; the remaining 12 stages act within the block. The
+/// line is transformed in place, so no CTA may store before all three have read their inputs:
+/// `cluster_sync` (a cluster-wide barrier) separates the first pass from the stores.
+template <int MODE, class SCH, class SYNC>
+__device__ __forceinline__ void line12288_block(const SCH& sch, const Ctx& c, int64_t* s, int64_t* g, int blk,
+                                                const int64_t* mulp, int64_t me, int64_t mn, int64_t mi,
+                                                SYNC cluster_sync) {
+    constexpr bool inv = MODE & 1, reduce_output = MODE == 0;
+    {
+        SF f[4];
+        bool fz[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            f[q] = sflags(sch, q);
+            fz[q] = f[q].last && reduce_output;
+        }
+        // twiddles of the factor-3 stage (one block)
+        int64_t wz0, wu0, wz1, wu1, wz2, wu2, wz3, wu3;  // forward: the two products of output blk
+        if (!inv) {
+            const int i0 = blk == 0 ? 0 : (blk == 1 ? 1 : 2), i1 = blk == 0 ? 3 : (blk == 1 ? 5 : 4);
+            twl(c, f[0].tw_off + i0, wz0, wu0);
+            twl(c, f[0].tw_off + i1, wz1, wu1);
+            wz2 = wu2 = wz3 = wu3 = 0;
+        } else {
+            twl(c, f[0].zeta_off, wz0, wu0);       // zeta
+            twl(c, f[0].zeta_off + 1, wz1, wu1);   // zeta^2
+            twl(c, f[0].tw_off + (blk == 2 ? 1 : 0), wz2, wu2);  // block twiddle of output blk (1, 2)
+            twl(c, f[0].tw_off, wz3, wu3);                       // its first entry decides the skip
+            (void)wu3;
+        }
+        constexpr int span = inv ? 64 : 512;
+        for (int gg = threadIdx.x; gg < 512; gg += blockDim.x) {
+            const int base = inv ? ((gg >> 6) << 9) + (gg & 63) : gg;
+            int64_t x[8];
+#pragma unroll
+            for (int m = 0; m < 8; m++) {
+                const int p = base + span * m;
+                int64_t a = g[p], b = g[p + 4096], d = g[p + 8192];
+                if (f[0].red) {
+                    a = red1(c, a);
+                    b = red1(c, b);
+                    d = red1(c, d);
+                }
+                int64_t o;
+                if (!inv) {
+                    // src/hal/ntt.rs:386-406, output blk of the butterfly
+                    int64_t tb, tc;
+                    if (blk == 0 && f[0].skip_ok) {
+                        tb = b;
+                        tc = d;
+                    } else {
+                        tb = bmul(wz0, wu0, b, c.n);
+                        tc = bmul(wz1, wu1, d, c.n);
+                    }
+                    o = wadd(wadd(a, tb), tc);
+                    if (fz[0]) o = red1(c, o);
+                } else {
+                    // src/hal/ntt.rs:511-530, output blk of the butterfly
+                    if (blk == 0) {
+                        o = wadd(wadd(a, b), d);
+                    } else if (blk == 1) {
+                        o = wadd(wadd(a, bmul(wz1, wu1, b, c.n)), bmul(wz0, wu0, d, c.n));
+                    } else {
+                        o = wadd(wadd(a, bmul(wz0, wu0, b, c.n)), bmul(wz1, wu1, d, c.n));
+                    }
+                    if (f[0].last) o = bmul(c.il_z, c.il_u, o, c.n);
+                    else if (blk != 0 && wz3 != 1) o = bmul(wz2, wu2, o, c.n);
+                }
+                x[m] = o;
+            }
+            if (!inv) fwd_group<3, true>(c, f + 1, fz + 1, 0, x);
+            else inv_group<3, false>(c, f + 1, gg >> 6, x);
+#pragma unroll
+            for (int m = 0; m < 8; m++) s[pad8(base + span * m)] = x[m];
+        }
+    }
+    cluster_sync();  // also a barrier of this CTA
+    if (!inv) {
+        r2_pass<false, 3, 6, 9, 3>(c, s, 512, sch, 4, reduce_output);   // factor 64 (a): 256, 128, 64
+        __syncthreads();
+        r2_pass<false, 3, 3, 6, 0>(c, s, 512, sch, 7, reduce_output);   // factor 64 (b): 32, 16, 8
+        __syncthreads();
+        r2_pass<false, 3, 0, 3, 3>(c, s, 512, sch, 10, reduce_output);  // factor 64 (b): 4, 2, 1
+    } else {
+        r2_pass<true, 3, 9, 12, 0>(c, s, 512, sch, 4, false);  // factor 64 (a): 512, 1024, 2048
+        __syncthreads();
+        r2_pass<true, 3, 0, 3, 3>(c, s, 512, sch, 7, false);   // factor 64 (b): 1, 2, 4
+        __syncthreads();
+        r2_pass<true, 3, 3, 6, 0>(c, s, 512, sch, 10, false);  // factor 64 (b): 8, 16, 32
+    }
+    __syncthreads();
+    line_store(s, g + 4096 * blk, 4096, MODE & 2, mulp + (me ? 4096 * blk : 0), me, mn, mi);
+}
+
 // ---------------------------------------------------------------- columns
 
 /// [4, 3] column (12 residues at element stride ge): factor 4 (distance 3) then factor 3
