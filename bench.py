@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--no-crt-batch", action="store_true", help="skip the batched CRT-transform workload")
     ap.add_argument("--no-homcrt", action="store_true", help="skip the homomorphic CRT transform workload")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
+    ap.add_argument("--only", choices=["crt_batch", "homcrt", "serving"],
+                    help="run just this workload and print its result (for profiling it alone)")
     ap.add_argument("--roofline-only", action="store_true",
                     help="time only the dominant NTT kernel (the launches a profile of it captures)")
     return ap.parse_args()
@@ -545,6 +547,12 @@ def main():
 
     halcuda.lib()
     be = halcuda.CudaBackend(dist.local_rank)
+    if args.only:
+        fn = {"crt_batch": lambda: crt_batch_bench(be, max(3, args.steps // 2), args.warmup),
+              "homcrt": lambda: homcrt_bench(be, reps=max(1, args.steps // 3)),
+              "serving": lambda: serving_bench(be)}[args.only]
+        print(json.dumps({args.only: fn()}), flush=True)
+        return
     if args.roofline_only:
         import ringcuda
 

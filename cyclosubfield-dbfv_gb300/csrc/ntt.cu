@@ -521,14 +521,15 @@ __device__ __forceinline__ fast::Ctx make_ctx(const DevPlanHeader* P, const int6
     return c;
 }
 
-/// The reduction / skip / fused-final schedule that the plans of primes just below 2^57 have
-/// (the primes the rings sample), per shape and direction: bit s = the flag of stage s.
+/// The reduction / skip / fused-final schedule that the plans of the rings' primes have, per shape
+/// and direction (bit s = the flag of stage s): field_36864 samples primes just below 2^57,
+/// field_49152 primes just below 2^56.
 struct SchedMasks {
     uint32_t fred, fskip, flast, ired, ilast;
 };
 __host__ __device__ constexpr SchedMasks fixed_masks(int shape) {
     return shape == HC_SHAPE_L3072    ? SchedMasks{0u, 0xFu, 1u << 10, 0x410u, 1u << 10}
-           : shape == HC_SHAPE_L12288 ? SchedMasks{0u, 0xFu, 1u << 12, 0x410u, 1u << 12}
+           : shape == HC_SHAPE_L12288 ? SchedMasks{0u, 0x1Fu, 1u << 12, 0x1020u, 1u << 12}
            : shape == HC_SHAPE_C12    ? SchedMasks{0u, 0x7u, 1u << 2, 0u, 1u << 2}
            : shape == HC_SHAPE_C4     ? SchedMasks{0u, 0x3u, 1u << 1, 0u, 1u << 1}
                                       : SchedMasks{0u, 0u, 0u, 0u, 0u};
