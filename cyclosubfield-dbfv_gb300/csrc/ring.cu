@@ -33,6 +33,8 @@ hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys
                            const int64_t* one_dev, const uint32_t* p2, const uint32_t* p3);
 hc_status launch_tensor(hc_context ctx, const KView& d, const KView& lhs, const KView& rhs, const KMods& m, int f0,
                         int f1, int f2);
+hc_status launch_giant(hc_context ctx, const KView* lhs, const KView* rhs, int nterms, const KView* add, int full,
+                       const KView& dst, const KMods& m, const int64_t* one_dev);
 }  // namespace hc
 
 using namespace hc;
@@ -2140,35 +2142,43 @@ hc_status hc_dbfv_hom_cyclic_transform(hc_ring R, size_t log2_b, size_t log2_t, 
                                        {vrows(rot.view(), 2 * (int64_t)di, 2 * (int64_t)di + 2)});
                     O = std::move(rot);
                 }
-                Wide acc(R, 2 * (int64_t)digits, b);
                 const size_t nterm = std::min(baby, len - giant * baby);
                 size_t max_new = 0;
                 for (size_t j = 0; j < nterm; j++) {
                     const size_t nr = bd[giant * baby + j].size();
                     if (d > 0 && nr > 0) max_new = std::max(max_new, std::min(digits, d + nr - 1));
                 }
-                // one inner product per output digit over the convolution diagonal (src/dbfv.rs:291-352)
-                for (size_t k = 0; k < max_new; k++) {
-                    std::vector<hc_view> lhs, rhs;
-                    for (size_t j = 0; j < nterm; j++) {
+                // one fused launch per output digit: the inner product over the convolution
+                // diagonal (src/dbfv.rs:291-352), the carried digit through mont(1) and the
+                // reduction the accumulator's bound asks for (src/ring.rs:365, :846-865)
+                const size_t used = std::max(max_new, od);
+                Tensor n(R->ctx, 2 * (int64_t)used, rr, dl, dk, false, false);
+                const u128 mp2 = (u128)R->max_p(b) * (u128)R->max_p(b);
+                const int64_t minp = R->min_p(b);
+                const KMods km = R->kmods(b);
+                const int64_t* one = R->one_dev(b);
+                for (size_t k = 0; k < used; k++) {
+                    std::vector<KView> lhs, rhs;
+                    for (size_t j = 0; j < nterm && k < max_new; j++) {
                         const size_t ci = giant * baby + j, nr = bd[ci].size();
                         if (d == 0 || nr == 0 || k >= std::min(digits, d + nr - 1)) continue;
                         for (size_t jj = 0; jj < nr && jj <= k; jj++) {
                             const size_t i = k - jj;
                             if (i >= d) continue;
-                            lhs.push_back(vrows(B.view(), (int64_t)(j * 2 * d + 2 * i), (int64_t)(j * 2 * d + 2 * i + 2)));
-                            rhs.push_back(ltensor(ci, jj));
+                            lhs.push_back(kv(vrows(B.view(), (int64_t)(j * 2 * d + 2 * i), (int64_t)(j * 2 * d + 2 * i + 2))));
+                            rhs.push_back(kv(ltensor(ci, jj)));
                         }
                     }
                     REQUIRE(lhs.size() <= HC_MAX_TERMS, HC_ERR_UNSUPPORTED, "too many inner-product terms per digit");
-                    if (!lhs.empty()) acc.inner_product(2 * k, 2 * k + 2, lhs, rhs);
+                    const bool has_add = k < od;
+                    const u128 bound = (u128)lhs.size() * mp2 + (has_add ? mp2 : 0);
+                    KView addv = has_add ? kv(vrows(O.view(), 2 * (int64_t)k, 2 * (int64_t)k + 2)) : KView();
+                    CK(launch_giant(R->ctx, lhs.data(), rhs.data(), (int)lhs.size(), has_add ? &addv : nullptr,
+                                    needs_full(bound, minp), kv(vrows(n.view(), 2 * (int64_t)k, 2 * (int64_t)k + 2)), km,
+                                    one));
                 }
-                size_t used = max_new;
-                if (od > 0) {
-                    acc.add(0, 2 * od, O.view(), 1);
-                    used = std::max(used, od);
-                }
-                finish(acc, used);
+                O = std::move(n);
+                od = used;
             }
         }
         if (od > 0) CK(hc_assign(R->ctx, vrows(out, 0, 2 * (int64_t)od), O.view()));

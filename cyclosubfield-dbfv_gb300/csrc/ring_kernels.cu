@@ -9,6 +9,10 @@
 //  - keyswitch_kernel: the key-switch inner product, the addition of c0 / c1 through mont(1)
 //    and reduce_wide (src/bfv.rs:498-556, src/ring.rs:460-485, :503-509, :846-865).
 //  - tensor_kernel: hom_mul_raw_acc + reduce_wide (src/bfv.rs:667-683).
+//  - giant_kernel: one giant step of the homomorphic CRT transform for one output digit: the
+//    baby-step inner product over the digit convolution (dbfv_acc_inner_product_element_lprime,
+//    src/dbfv.rs:291-399), the addition of the carried result (dbfv_acc_add, :153-163) and the
+//    reduction (dbfv_finish_accumulator, :401-404), without the wide accumulator in HBM.
 #include "common.cuh"
 
 namespace {
@@ -158,6 +162,40 @@ __global__ void __launch_bounds__(256) tensor_kernel(KView d, KView lhs, KView r
     }
 }
 
+struct GiantArgs {
+    KView lhs[HC_MAX_TERMS];  // [2, r, dl, dk]: c0 / c1 rows of one digit of a baby step
+    KView rhs[HC_MAX_TERMS];  // [1, r, dl, 1]: one balanced digit of an L' coefficient (CRT basis)
+    int nterms;
+    KView add;                // [2, r, dl, dk]: the carried digit, through mont(1) (has_add)
+    int has_add;
+    int full;                 // the rows need the full double reduction
+    KView dst;                // [2, r, dl, dk]
+};
+
+__global__ void __launch_bounds__(256) giant_kernel(GiantArgs a, KMods m, const int64_t* one, int64_t lines,
+                                                    int chunks) {
+    const int64_t tiles = lines * chunks;
+    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        int64_t line = tile / chunks;  // (j, k)
+        int64_t l = (tile - line * chunks) * blockDim.x + threadIdx.x;
+        if (l >= a.dst.n3) continue;
+        int64_t k = line % a.dst.n2, j = line / a.dst.n2;
+        i128 acc0 = 0, acc1 = 0;
+        for (int t = 0; t < a.nterms; t++) {
+            const int64_t f = *kat<int64_t>(a.rhs[t], 0, j, k, 0);
+            acc0 = (i128)((u128)acc0 + (u128)((i128)*kat<int64_t>(a.lhs[t], 0, j, k, l) * (i128)f));
+            acc1 = (i128)((u128)acc1 + (u128)((i128)*kat<int64_t>(a.lhs[t], 1, j, k, l) * (i128)f));
+        }
+        if (a.has_add) {
+            const int64_t o = one[j];
+            acc0 = (i128)((u128)acc0 + (u128)((i128)*kat<int64_t>(a.add, 0, j, k, l) * (i128)o));
+            acc1 = (i128)((u128)acc1 + (u128)((i128)*kat<int64_t>(a.add, 1, j, k, l) * (i128)o));
+        }
+        *kat<int64_t>(a.dst, 0, j, k, l) = finish_wide(acc0, a.full, m, (int)j);
+        *kat<int64_t>(a.dst, 1, j, k, l) = finish_wide(acc1, a.full, m, (int)j);
+    }
+}
+
 void grid_lines(hc_context ctx, int64_t n3, int64_t lines, int* chunks, unsigned* blocks) {
     *chunks = (int)((n3 + 255) / 256);
     int64_t tiles = lines * *chunks;
@@ -226,6 +264,30 @@ hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys
     keyswitch_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(a, m, one_dev, lines, chunks);
     count_launch(ctx);
     return cuda_check(cudaGetLastError(), "keyswitch kernel launch");
+}
+
+hc_status launch_giant(hc_context ctx, const KView* lhs, const KView* rhs, int nterms, const KView* add, int full,
+                       const KView& dst, const KMods& m, const int64_t* one_dev) {
+    if (nterms > HC_MAX_TERMS) return fail(HC_ERR_UNSUPPORTED, "too many inner-product terms per digit");
+    GiantArgs a;
+    for (int t = 0; t < nterms; t++) {
+        a.lhs[t] = lhs[t];
+        a.rhs[t] = rhs[t];
+        a.rhs[t].b3 = 1;  // broadcast along dimension 3
+    }
+    a.nterms = nterms;
+    a.has_add = add != nullptr;
+    if (add) a.add = *add;
+    a.full = full;
+    a.dst = dst;
+    int64_t lines = dst.n1 * dst.n2;
+    if (lines == 0 || dst.n3 == 0) return HC_OK;
+    int chunks;
+    unsigned blocks;
+    grid_lines(ctx, dst.n3, lines, &chunks, &blocks);
+    giant_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(a, m, one_dev, lines, chunks);
+    count_launch(ctx);
+    return cuda_check(cudaGetLastError(), "giant-step kernel launch");
 }
 
 hc_status launch_tensor(hc_context ctx, const KView& d, const KView& lhs, const KView& rhs, const KMods& m, int f0,
