@@ -49,31 +49,51 @@ __global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a,
     }
     if (!live) return;
     const i128 half = (i128)1 << (a.shift - 1);
+    const int64_t* xcol = xs + threadIdx.x;  // this thread's lifts, stride BCONV_THREADS
     for (int b = 0; b < a.nb; b++) {
         const int u0 = a.ucol[2 * b], u1 = a.ucol[2 * b + 1];
-        const int64_t* mb = a.mat + (int64_t)b * (a.rd + 1) * a.r;
+        const int64_t* __restrict__ mb = a.mat + (int64_t)b * (a.rd + 1) * a.r;
         i128 corr = 0;
-        for (int u = u0; u < u1; u++)
-            corr = (i128)((u128)corr + (u128)((i128)mb[(int64_t)a.rd * a.r + u] * (i128)xs[u * BCONV_THREADS + threadIdx.x]));
+        {
+            const int64_t* mq = mb + (int64_t)a.rd * a.r;
+#pragma unroll 4
+            for (int u = u0; u < u1; u++)
+                corr = (i128)((u128)corr + (u128)((i128)__ldg(mq + u) * (i128)xcol[u * BCONV_THREADS]));
+        }
         const int64_t q = (int64_t)((i128)((u128)corr + (u128)half) >> a.shift);
-        for (int j = 0; j < a.rd; j++) {
-            const int64_t* mj = mb + (int64_t)j * a.r;
-            int64_t val = 0;
+        // two output rows per pass over the lifts (each lift is read once for both); the
+        // reference's chunked matmul (src/ring.rs:1678-1691) splits the columns into chunks of
+        // `chunk` (one chunk whenever r <= chunk, which holds for all 57-bit bases up to 8192
+        // factors) and double-reduces each chunk's sum
+        for (int j = 0; j < a.rd; j += 2) {
+            const bool two = j + 1 < a.rd;
+            const int64_t* __restrict__ m0 = mb + (int64_t)j * a.r;
+            const int64_t* __restrict__ m1 = two ? m0 + a.r : m0;
+            int64_t v0 = 0, v1 = 0;
             bool first = true;
-            // chunks of the reference's matmul (src/ring.rs:1678-1691), restricted to the
-            // columns the matrix does not zero
             for (int c0 = 0; c0 < a.r; c0 += a.chunk) {
-                int c1 = min(c0 + a.chunk, a.r);
-                int lo = max(c0, u0), hi = min(c1, u1);
-                i128 acc = 0;
-                for (int u = lo; u < hi; u++)
-                    acc = (i128)((u128)acc + (u128)((i128)mj[u] * (i128)xs[u * BCONV_THREADS + threadIdx.x]));
-                int64_t red = double_red128(acc, dm.n[j], dm.ninv[j]);
-                val = first ? red : wadd(val, red);
+                const int lo = max(c0, u0), hi = min(min(c0 + a.chunk, a.r), u1);
+                i128 s0 = 0, s1 = 0;
+#pragma unroll 4
+                for (int u = lo; u < hi; u++) {
+                    const i128 x = (i128)xcol[u * BCONV_THREADS];
+                    s0 = (i128)((u128)s0 + (u128)((i128)__ldg(m0 + u) * x));
+                    s1 = (i128)((u128)s1 + (u128)((i128)__ldg(m1 + u) * x));
+                }
+                const int64_t r0 = double_red128(s0, dm.n[j], dm.ninv[j]);
+                v0 = first ? r0 : wadd(v0, r0);
+                if (two) {
+                    const int64_t r1 = double_red128(s1, dm.n[j + 1], dm.ninv[j + 1]);
+                    v1 = first ? r1 : wadd(v1, r1);
+                }
                 first = false;
             }
-            val = wadd(val, mul_mont(q, a.qmodp[(int64_t)b * a.rd + j], dm.n[j], dm.ninv[j]));
-            *kat<int64_t>(a.dst, i * a.nb + b, j, k, l) = to_mont64(val, dm.n[j], dm.ninv[j], dm.r2[j]);
+            v0 = wadd(v0, mul_mont(q, a.qmodp[(int64_t)b * a.rd + j], dm.n[j], dm.ninv[j]));
+            *kat<int64_t>(a.dst, i * a.nb + b, j, k, l) = to_mont64(v0, dm.n[j], dm.ninv[j], dm.r2[j]);
+            if (two) {
+                v1 = wadd(v1, mul_mont(q, a.qmodp[(int64_t)b * a.rd + j + 1], dm.n[j + 1], dm.ninv[j + 1]));
+                *kat<int64_t>(a.dst, i * a.nb + b, j + 1, k, l) = to_mont64(v1, dm.n[j + 1], dm.ninv[j + 1], dm.r2[j + 1]);
+            }
         }
     }
 }
