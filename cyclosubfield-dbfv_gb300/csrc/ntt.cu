@@ -659,11 +659,14 @@ __device__ __forceinline__ void run_column(const DevPlanHeader* P, const fast::C
 }
 
 #define HC_COL_THREADS 256
+#ifndef HC_COL12_MIN_BLOCKS
+#define HC_COL12_MIN_BLOCKS 4  // resident CTAs per SM the [4, 3] column kernel's registers must allow
+#endif
 #define HC_COL_TW 128  // twiddle words a column plan may have (checked at dispatch)
 
 /// Specialised dimension-2 NTT: one thread per column (i, j, l), CTAs over (i, j, column block).
 template <int SHAPE, int MODE, bool FIX>
-__global__ void __launch_bounds__(HC_COL_THREADS, SHAPE == HC_SHAPE_C12 ? 2 : 4) ntt_col_kernel(KView t, PlanPtrs plans, KView mul, KMods mods,
+__global__ void __launch_bounds__(HC_COL_THREADS, SHAPE == HC_SHAPE_C12 ? HC_COL12_MIN_BLOCKS : 4) ntt_col_kernel(KView t, PlanPtrs plans, KView mul, KMods mods,
                                                                     int ncb) {
     __shared__ __align__(16) int64_t tws[HC_COL_TW];
     const int64_t tile = blockIdx.x;
