@@ -402,12 +402,25 @@ static hc_status ntt_call(hc_context ctx, hc_view dst, const hc_ntt_plan* plans,
     if (st) return st;
     KView t = kview(dst), m = t;
     KMods km;
-    if (mode == 2) {
+    if (mode & 2) {
         if ((st = bview(*mul, dst.shape, "mul", &m))) return st;
         if ((st = kmods(mods, nmods, dst.shape[1], &km))) return st;
     }
     return launch_ntt(ctx, t, plans, nplans, (int)dim, mode, m, km);
 }
+
+}  // extern "C"
+
+namespace hc {
+/// Inverse transform followed by a Montgomery product with `mul` in the epilogue of the last pass
+/// (the same integers as hc_intt_mont64_dim followed by hc_mul_mont64); used by the ring layer.
+hc_status intt_mul_mont64_dim(hc_context ctx, hc_view dst, const hc_ntt_plan* plans, size_t nplans, hc_data_dim dim,
+                              hc_view mul, const hc_modulus* mods, size_t nmods) {
+    return ntt_call(ctx, dst, plans, nplans, dim, 3, &mul, mods, nmods);
+}
+}  // namespace hc
+
+extern "C" {
 
 hc_status hc_ntt_mont64_dim(hc_context ctx, hc_view dst, const hc_ntt_plan* plans, size_t nplans, hc_data_dim dim) {
     return ntt_call(ctx, dst, plans, nplans, dim, 0, nullptr, nullptr, 0);

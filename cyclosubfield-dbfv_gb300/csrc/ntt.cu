@@ -570,7 +570,7 @@ __global__ void __launch_bounds__(THREADS, MINB) ntt_line_kernel(KView t, PlanPt
     int64_t* g = reinterpret_cast<int64_t*>(t.p) + i * t.s0 + j * t.s1 + k * t.s2;
     const int64_t* mulp = nullptr;
     int64_t me = 0, mn = 0, mi = 0;
-    if (MODE == 2) {
+    if (MODE & 2) {
         mulp = kat<int64_t>(mul, i, j, k, 0);
         me = mul.b3 ? 0 : 1;
         mn = mods.n[j], mi = mods.ninv[j];
@@ -596,7 +596,7 @@ __global__ void __cluster_dims__(3, 1, 1) __launch_bounds__(128, 5)
     int64_t* g = reinterpret_cast<int64_t*>(t.p) + i * t.s0 + j * t.s1 + k * t.s2;
     const int64_t* mulp = nullptr;
     int64_t me = 0, mn = 0, mi = 0;
-    if (MODE == 2) {
+    if (MODE & 2) {
         mulp = kat<int64_t>(mul, i, j, k, 0);
         me = mul.b3 ? 0 : 1;
         mn = mods.n[j], mi = mods.ninv[j];
@@ -681,7 +681,7 @@ __global__ void __launch_bounds__(HC_COL_THREADS, SHAPE == HC_SHAPE_C12 ? HC_COL
     int64_t* g = reinterpret_cast<int64_t*>(t.p) + i * t.s0 + j * t.s1 + l;
     const int64_t* mulp = nullptr;
     int64_t ms = 0, mn = 0, mi = 0;
-    if (MODE == 2) {
+    if (MODE & 2) {
         mulp = kat<int64_t>(mul, i, j, 0, l);
         ms = mul.s2;
         mn = mods.n[j], mi = mods.ninv[j];
@@ -720,11 +720,13 @@ hc_status launch_special_mode(hc_context ctx, int mode, bool fix, const KView& t
     if (fix) {
         if (mode == 0) return launch_special<SHAPE, 0, true>(ctx, t, pp, mul, mods, smem, tiles, ncb);
         if (mode == 1) return launch_special<SHAPE, 1, true>(ctx, t, pp, mul, mods, smem, tiles, ncb);
-        return launch_special<SHAPE, 2, true>(ctx, t, pp, mul, mods, smem, tiles, ncb);
+        if (mode == 2) return launch_special<SHAPE, 2, true>(ctx, t, pp, mul, mods, smem, tiles, ncb);
+        return launch_special<SHAPE, 3, true>(ctx, t, pp, mul, mods, smem, tiles, ncb);
     }
     if (mode == 0) return launch_special<SHAPE, 0, false>(ctx, t, pp, mul, mods, smem, tiles, ncb);
     if (mode == 1) return launch_special<SHAPE, 1, false>(ctx, t, pp, mul, mods, smem, tiles, ncb);
-    return launch_special<SHAPE, 2, false>(ctx, t, pp, mul, mods, smem, tiles, ncb);
+    if (mode == 2) return launch_special<SHAPE, 2, false>(ctx, t, pp, mul, mods, smem, tiles, ncb);
+    return launch_special<SHAPE, 3, false>(ctx, t, pp, mul, mods, smem, tiles, ncb);
 }
 
 /// mode 0: forward (reduced), 1: inverse, 2: forward unreduced + Montgomery multiplication by `mul`.
@@ -757,7 +759,7 @@ __global__ void __launch_bounds__(256, HC_NTT_MIN_BLOCKS) ntt_tile_kernel(KView 
     io.ge = dim == 3 ? 1 : t.s2;
     io.ncol = dim == 3 ? 1 : t.n3 - cb * V;
     io.mulp = nullptr, io.me = io.mv = 0, io.mn = io.mi = 0;
-    if (mode == 2) {
+    if (mode & 2) {
         io.mulp = kat<int64_t>(mul, i, j, dim == 3 ? k : 0, dim == 3 ? 0 : cb * V);
         io.me = dim == 3 ? (mul.b3 ? 0 : 1) : mul.s2;
         io.mv = dim == 3 ? 0 : (mul.b3 ? 0 : 1);

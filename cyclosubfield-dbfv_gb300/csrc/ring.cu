@@ -26,7 +26,8 @@
 namespace hc {
 hc_status launch_bconv_fused(hc_context ctx, const KView& src, const KView& dst, const int64_t* qinv,
                              const int64_t* mat, const int64_t* qmodp, const int32_t* ucol, int r, int rd, int nb,
-                             int shift, int chunk, const KMods& sm, const KMods& dm, int64_t ns);
+                             int shift, int chunk, const KMods& sm, const KMods& dm, int64_t ns,
+                             const int64_t* sub_mul);
 hc_status launch_galois(hc_context ctx, const KView& d, const KView& s, const uint32_t* p2, const uint32_t* p3);
 hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys, int nterms, const KView* add0,
                            const KView* add1, int full0, int full1, const KView& dst, const KMods& m,
@@ -635,7 +636,9 @@ struct hc_ring_s {
     }
 
     // ---------------------------------------------------------------- transforms
-    void transform(const hc_view& v, const Base& b, bool inverse) {
+    /// pb_to_crt / crt_to_pb (src/ring.rs:1118-1161); `post_mul`: a Montgomery product applied to
+    /// the result in the epilogue of the last pass (the caller's next hal_mul_mont64, fused)
+    void transform(const hc_view& v, const Base& b, bool inverse, const hc_view* post_mul = nullptr) {
         REQUIRE(v.shape[1] == (int64_t)b.size() && v.shape[2] == dl() && v.shape[3] == dk(), HC_ERR_SHAPE,
                 "transform: tensor shape does not match the ring and base");
         TransformCache& c = transform_cache(b);
@@ -645,7 +648,8 @@ struct hc_ring_s {
         CK(hc_ntt_mul_mont64_dim(ctx, v, c.pk.data(), r, HC_DIM3, inverse ? c.ikk.view() : c.kk.view(),
                                  c.mods.data(), r));
         CK(hc_intt_mont64_dim(ctx, v, c.plp.data(), r, HC_DIM2));
-        CK(hc_intt_mont64_dim(ctx, v, c.pk.data(), r, HC_DIM3));
+        if (post_mul) CK(intt_mul_mont64_dim(ctx, v, c.pk.data(), r, HC_DIM3, *post_mul, c.mods.data(), r));
+        else CK(hc_intt_mont64_dim(ctx, v, c.pk.data(), r, HC_DIM3));
     }
 
     // ---------------------------------------------------------------- base conversion
@@ -695,13 +699,17 @@ struct hc_ring_s {
         return *bcache.back();
     }
 
-    void bconv(const hc_view& dst, const Base& db, const hc_view& src, const Base& sb) {
+    /// `sub_mul` (optional, one Montgomery factor per destination prime): instead of writing the
+    /// conversion v, dst <- mul_mont(dst - v, sub_mul) (the caller's hal_sub_i64 and hal_mul_mont64,
+    /// fused into the store)
+    void bconv(const hc_view& dst, const Base& db, const hc_view& src, const Base& sb,
+               const int64_t* sub_mul = nullptr) {
         check_view(src, src.shape[0], (int64_t)sb.size(), src.shape[2], src.shape[3], "bconv src");
         check_view(dst, src.shape[0], (int64_t)db.size(), src.shape[2], src.shape[3], "bconv dst");
         BconvCache& c = bconv_cache(sb, db);
         CK(launch_bconv_fused(ctx, kv(src), kv(dst), c.qinv.as<int64_t>(), c.mat.as<int64_t>(),
                               c.qmodp.as<int64_t>(), c.ucol.as<int32_t>(), (int)sb.size(), (int)db.size(), 1,
-                              c.shift, c.chunk, kmods(sb), kmods(db), src.shape[0]));
+                              c.shift, c.chunk, kmods(sb), kmods(db), src.shape[0], sub_mul));
     }
 
     GadgetCache& gadget_cache(const Base& b, const Digits& digits) {
@@ -770,7 +778,7 @@ struct hc_ring_s {
         KMods km = kmods(b);
         CK(launch_bconv_fused(ctx, kv(src), kv(dst), c.dinv.as<int64_t>(), c.mat.as<int64_t>(), c.dmodp.as<int64_t>(),
                               c.ucol.as<int32_t>(), (int)b.size(), (int)b.size(), (int)digits.size(), c.shift, c.chunk,
-                              km, km, src.shape[0]));
+                              km, km, src.shape[0], nullptr));
     }
 
     // ---------------------------------------------------------------- Galois
@@ -1136,17 +1144,18 @@ Tensor lift_to_extended(hc_ring R, const hc_view& pb, const hc_view* crt, const 
     return res;
 }
 
-Tensor rescale_to_base(hc_ring R, const hc_view& x, const Base& lifted, size_t base_len, i128 t) {
+/// rescale_to_base (src/bfv.rs:601-622); `pre_scaled`: x was already multiplied by t (fused into
+/// the epilogue of the transform that produced it)
+Tensor rescale_to_base(hc_ring R, const hc_view& x, const Base& lifted, size_t base_len, i128 t,
+                       bool pre_scaled = false) {
     const int64_t count = x.shape[0];
     Base base(lifted.begin(), lifted.begin() + base_len), ext(lifted.begin() + base_len, lifted.end());
-    std::vector<hc_modulus> ml = R->mods(lifted), me = R->mods(ext);
-    CK(hc_mul_mont64(R->ctx, x, R->scalar_tensor(lifted, t).view(), ml.data(), ml.size()));
-    Tensor tmp = temp(R->ctx, count, (int64_t)ext.size(), R->dl(), R->dk());
+    std::vector<hc_modulus> ml = R->mods(lifted);
+    if (!pre_scaled) CK(hc_mul_mont64(R->ctx, x, R->scalar_tensor(lifted, t).view(), ml.data(), ml.size()));
     hc_view xlo = vbase(x, 0, (int64_t)base_len), xhi = vbase(x, (int64_t)base_len, (int64_t)lifted.size());
-    R->bconv(tmp.view(), ext, xlo, base);
-    CK(hc_sub_i64(R->ctx, xhi, tmp.view()));
+    // xhi <- (xhi - bconv(xlo)) * (Q_base^-1 mod p), the subtraction and product in the conversion's store
     const Tensor& qinv = R->inv_modulus_tensor(ext, base);
-    CK(hc_mul_mont64(R->ctx, xhi, qinv.view(), me.data(), me.size()));
+    R->bconv(xhi, ext, xlo, base, (const int64_t*)qinv.view().ptr);
     Tensor out = temp(R->ctx, count, (int64_t)base_len, R->dl(), R->dk());
     R->bconv(out.view(), base, xhi, ext);
     return out;
@@ -1447,8 +1456,10 @@ hc_status hc_bfv_hom_mul(hc_ring R, const int64_t t[2], hc_view ct1, hc_view ct2
             CK(launch_tensor(R->ctx, kv(prod.view()), kv(l.view()), kv(rt.view()), R->kmods(lifted), needs_full(s1, mn),
                              needs_full(2 * s1, mn), needs_full(s1, mn)));
         }
-        R->transform(prod.view(), lifted, true);
-        Tensor resc = rescale_to_base(R, prod.view(), lifted, r, words(t));
+        const Tensor& tscale = R->scalar_tensor(lifted, words(t));
+        const hc_view tsv = tscale.view();
+        R->transform(prod.view(), lifted, true, &tsv);
+        Tensor resc = rescale_to_base(R, prod.view(), lifted, r, words(t), true);
         // relinearisation (src/bfv.rs:699-741)
         Digits dg = clip(digits_of(digits, d), r);
         REQUIRE(rk.shape[0] >= 2 * (int64_t)dg.size() && rk.shape[1] >= rr, HC_ERR_SHAPE, "relinearisation key shape");

@@ -30,6 +30,7 @@ struct BconvArgs {
     int shift;
     int chunk;  // acc_before_reduce of the reference
     int64_t npos;
+    const int64_t* sub_mul;  // optional [rd]: store mul_mont(dst - v, sub_mul[j]) instead of v
 };
 
 __global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a, KMods sm, KMods dm) {
@@ -89,10 +90,16 @@ __global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a,
                 first = false;
             }
             v0 = wadd(v0, mul_mont(q, a.qmodp[(int64_t)b * a.rd + j], dm.n[j], dm.ninv[j]));
-            *kat<int64_t>(a.dst, i * a.nb + b, j, k, l) = to_mont64(v0, dm.n[j], dm.ninv[j], dm.r2[j]);
+            {
+                int64_t* p = kat<int64_t>(a.dst, i * a.nb + b, j, k, l);
+                const int64_t y = to_mont64(v0, dm.n[j], dm.ninv[j], dm.r2[j]);
+                *p = a.sub_mul ? mul_mont(wsub(*p, y), a.sub_mul[j], dm.n[j], dm.ninv[j]) : y;
+            }
             if (two) {
                 v1 = wadd(v1, mul_mont(q, a.qmodp[(int64_t)b * a.rd + j + 1], dm.n[j + 1], dm.ninv[j + 1]));
-                *kat<int64_t>(a.dst, i * a.nb + b, j + 1, k, l) = to_mont64(v1, dm.n[j + 1], dm.ninv[j + 1], dm.r2[j + 1]);
+                int64_t* p = kat<int64_t>(a.dst, i * a.nb + b, j + 1, k, l);
+                const int64_t y = to_mont64(v1, dm.n[j + 1], dm.ninv[j + 1], dm.r2[j + 1]);
+                *p = a.sub_mul ? mul_mont(wsub(*p, y), a.sub_mul[j + 1], dm.n[j + 1], dm.ninv[j + 1]) : y;
             }
         }
     }
@@ -229,8 +236,10 @@ namespace hc {
 
 hc_status launch_bconv_fused(hc_context ctx, const KView& src, const KView& dst, const int64_t* qinv,
                              const int64_t* mat, const int64_t* qmodp, const int32_t* ucol, int r, int rd, int nb,
-                             int shift, int chunk, const KMods& sm, const KMods& dm, int64_t ns) {
+                             int shift, int chunk, const KMods& sm, const KMods& dm, int64_t ns,
+                             const int64_t* sub_mul) {
     BconvArgs a;
+    a.sub_mul = sub_mul;
     a.src = src;
     a.dst = dst;
     a.qinv = qinv, a.mat = mat, a.qmodp = qmodp, a.ucol = ucol;
