@@ -27,7 +27,7 @@ namespace hc {
 hc_status launch_bconv_fused(hc_context ctx, const KView& src, const KView& dst, const int64_t* qinv,
                              const int64_t* mat, const int64_t* qmodp, const int32_t* ucol, int r, int rd, int nb,
                              int shift, int chunk, const KMods& sm, const KMods& dm, int64_t ns,
-                             const int64_t* sub_mul);
+                             const int64_t* sub_mul, const int32_t* mat2);
 hc_status launch_galois(hc_context ctx, const KView& d, const KView& s, const uint32_t* p2, const uint32_t* p3);
 hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys, int nterms, const KView* add0,
                            const KView* add1, int full0, int full1, const KView& dst, const KMods& m,
@@ -443,11 +443,35 @@ struct TransformCache {
     Tensor kl, kk, ikl, ikk;
 };
 
+/// The base conversion kernel's limb form of a conversion matrix [nb][rd + 1][r] (the last row of
+/// each block is the correction row, kept in full width): the pairs (m mod 2^29, m >> 29) of the
+/// rows 0..rd-1, as [nb][rd][r] int2. The kernel multiplies them with the lifts split the same way
+/// and accumulates the three partial-product columns in int64 over groups of 16 terms, which is
+/// exact when |m| < 2^56 and the lifts satisfy |x| < 2^57, i.e. every source prime is below 2^57
+/// (which the ring's RNS factor size rule guarantees; checked here all the same).
+DBuf limb_matrix(hc_context ctx, const std::vector<int64_t>& mat, size_t nb, size_t rd, size_t r,
+                 int64_t max_src_p) {
+    REQUIRE(max_src_p < ((int64_t)1 << 57), HC_ERR_UNSUPPORTED, "base conversion: source prime above 2^57");
+    std::vector<int32_t> m2(nb * rd * r * 2);
+    for (size_t b = 0; b < nb; b++)
+        for (size_t j = 0; j < rd; j++)
+            for (size_t u = 0; u < r; u++) {
+                const int64_t m = mat[(b * (rd + 1) + j) * r + u];
+                REQUIRE(m < ((int64_t)1 << 56) && m > -((int64_t)1 << 56), HC_ERR_UNSUPPORTED,
+                        "base conversion: matrix entry above 2^56");
+                const size_t o = ((b * rd + j) * r + u) * 2;
+                m2[o] = (int32_t)(m & ((1 << 29) - 1));
+                m2[o + 1] = (int32_t)(m >> 29);
+            }
+    return DBuf(ctx, m2.data(), m2.size() * 4);
+}
+
 struct BconvCache {
     Base src, dst;
     int shift;
     int chunk;
     DBuf qinv, mat, qmodp, ucol;
+    DBuf mat2;  // limb form of mat (limb_matrix)
 };
 
 struct GadgetCache {
@@ -456,6 +480,7 @@ struct GadgetCache {
     int shift;
     int chunk;
     DBuf dinv, mat, dmodp, ucol;
+    DBuf mat2;  // as BconvCache::mat2
 };
 
 struct PermCache {
@@ -693,6 +718,7 @@ struct hc_ring_s {
         int32_t uc[2] = {0, (int32_t)r};
         c->qinv = DBuf(ctx, qinv.data(), qinv.size() * 8);
         c->mat = DBuf(ctx, mat.data(), mat.size() * 8);
+        c->mat2 = limb_matrix(ctx, mat, 1, rd, r, max_p(src));
         c->qmodp = DBuf(ctx, qm.data(), qm.size() * 8);
         c->ucol = DBuf(ctx, uc, sizeof(uc));
         bcache.push_back(std::move(c));
@@ -709,7 +735,7 @@ struct hc_ring_s {
         BconvCache& c = bconv_cache(sb, db);
         CK(launch_bconv_fused(ctx, kv(src), kv(dst), c.qinv.as<int64_t>(), c.mat.as<int64_t>(),
                               c.qmodp.as<int64_t>(), c.ucol.as<int32_t>(), (int)sb.size(), (int)db.size(), 1,
-                              c.shift, c.chunk, kmods(sb), kmods(db), src.shape[0], sub_mul));
+                              c.shift, c.chunk, kmods(sb), kmods(db), src.shape[0], sub_mul, c.mat2.as<int32_t>()));
     }
 
     GadgetCache& gadget_cache(const Base& b, const Digits& digits) {
@@ -763,6 +789,7 @@ struct hc_ring_s {
         }
         c->dinv = DBuf(ctx, dinv.data(), dinv.size() * 8);
         c->mat = DBuf(ctx, mat.data(), mat.size() * 8);
+        c->mat2 = limb_matrix(ctx, mat, d, r, r, mx);
         c->dmodp = DBuf(ctx, dm.data(), dm.size() * 8);
         c->ucol = DBuf(ctx, uc.data(), uc.size() * 4);
         gcache.push_back(std::move(c));
@@ -778,7 +805,7 @@ struct hc_ring_s {
         KMods km = kmods(b);
         CK(launch_bconv_fused(ctx, kv(src), kv(dst), c.dinv.as<int64_t>(), c.mat.as<int64_t>(), c.dmodp.as<int64_t>(),
                               c.ucol.as<int32_t>(), (int)b.size(), (int)b.size(), (int)digits.size(), c.shift, c.chunk,
-                              km, km, src.shape[0], nullptr));
+                              km, km, src.shape[0], nullptr, c.mat2.as<int32_t>()));
     }
 
     // ---------------------------------------------------------------- Galois

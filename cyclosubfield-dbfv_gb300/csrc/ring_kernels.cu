@@ -31,10 +31,43 @@ struct BconvArgs {
     int chunk;  // acc_before_reduce of the reference
     int64_t npos;
     const int64_t* sub_mul;  // optional [rd]: store mul_mont(dst - v, sub_mul[j]) instead of v
+    const int2* mat2;        // limb form of the rows 0..rd-1 of mat, [nb][rd][r] (see limb_mac2)
 };
 
+constexpr int LIMB_BITS = 29;
+constexpr int LIMB_GROUP = 16;  // terms per int64 partial-sum group (sums stay below 2^62)
+
+/// One output pair's multiply-accumulate over the lifts u in [lo, hi): exact sum_u m_u x_u as i128.
+/// The operands are split as v = v1 2^29 + v0 with 0 <= v0 < 2^29; with |x| < 2^57 and |m| < 2^56
+/// every partial product x0 m0, x0 m1 + x1 m0, x1 m1 is below 2^58 in magnitude, so 16 of them add
+/// up in int64 without overflow; each group is then folded into the 128-bit sum.
+__device__ __forceinline__ void limb_mac2(const int2* __restrict__ xcol, const int2* __restrict__ m0,
+                                          const int2* __restrict__ m1, int lo, int hi, i128& s0, i128& s1) {
+    for (int g0 = lo; g0 < hi; g0 += LIMB_GROUP) {
+        const int g1 = min(g0 + LIMB_GROUP, hi);
+        int64_t a00 = 0, a01 = 0, a11 = 0, b00 = 0, b01 = 0, b11 = 0;
+#pragma unroll 4
+        for (int u = g0; u < g1; u++) {
+            const int2 x = xcol[u * BCONV_THREADS];
+            const int2 p = __ldg(m0 + u), q = __ldg(m1 + u);
+            a00 += (int64_t)x.x * p.x;
+            a01 += (int64_t)x.x * p.y;
+            a01 += (int64_t)x.y * p.x;
+            a11 += (int64_t)x.y * p.y;
+            b00 += (int64_t)x.x * q.x;
+            b01 += (int64_t)x.x * q.y;
+            b01 += (int64_t)x.y * q.x;
+            b11 += (int64_t)x.y * q.y;
+        }
+        s0 = (i128)((u128)s0 + (u128)(i128)a00 + ((u128)(i128)a01 << LIMB_BITS) + ((u128)(i128)a11 << (2 * LIMB_BITS)));
+        s1 = (i128)((u128)s1 + (u128)(i128)b00 + ((u128)(i128)b01 << LIMB_BITS) + ((u128)(i128)b11 << (2 * LIMB_BITS)));
+    }
+}
+
+/// The products with the conversion matrix use its limb form (BconvArgs::mat2): the shared array
+/// holds each lift as its limb pair (x mod 2^29, x >> 29).
 __global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a, KMods sm, KMods dm) {
-    extern __shared__ int64_t xs[];  // [r][BCONV_THREADS]
+    extern __shared__ int2 xs[];  // [r][BCONV_THREADS]
     const int64_t i = blockIdx.y;
     const int64_t pos = (int64_t)blockIdx.x * BCONV_THREADS + threadIdx.x;
     const bool live = pos < a.npos;
@@ -46,11 +79,16 @@ __global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a,
     // the source is multiplied by (Q/p)^-1 in Montgomery form, giving plain lifts in (-p, p)
     for (int u = 0; u < a.r; u++) {
         int64_t x = live ? *kat<int64_t>(a.src, i, u, k, l) : 0;
-        xs[u * BCONV_THREADS + threadIdx.x] = live ? mul_mont(x, a.qinv[u], sm.n[u], sm.ninv[u]) : 0;
+        x = live ? mul_mont(x, a.qinv[u], sm.n[u], sm.ninv[u]) : 0;
+        xs[u * BCONV_THREADS + threadIdx.x] = make_int2((int)(x & ((1 << LIMB_BITS) - 1)), (int)(x >> LIMB_BITS));
     }
     if (!live) return;
     const i128 half = (i128)1 << (a.shift - 1);
-    const int64_t* xcol = xs + threadIdx.x;  // this thread's lifts, stride BCONV_THREADS
+    const int2* xcol = xs + threadIdx.x;  // this thread's lifts, stride BCONV_THREADS
+    auto lift = [&](int u) -> int64_t {
+        const int2 v = xcol[u * BCONV_THREADS];
+        return (int64_t)v.y * ((int64_t)1 << LIMB_BITS) + v.x;
+    };
     for (int b = 0; b < a.nb; b++) {
         const int u0 = a.ucol[2 * b], u1 = a.ucol[2 * b + 1];
         const int64_t* __restrict__ mb = a.mat + (int64_t)b * (a.rd + 1) * a.r;
@@ -59,7 +97,7 @@ __global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a,
             const int64_t* mq = mb + (int64_t)a.rd * a.r;
 #pragma unroll 4
             for (int u = u0; u < u1; u++)
-                corr = (i128)((u128)corr + (u128)((i128)__ldg(mq + u) * (i128)xcol[u * BCONV_THREADS]));
+                corr = (i128)((u128)corr + (u128)((i128)__ldg(mq + u) * (i128)lift(u)));
         }
         const int64_t q = (int64_t)((i128)((u128)corr + (u128)half) >> a.shift);
         // two output rows per pass over the lifts (each lift is read once for both); the
@@ -68,19 +106,14 @@ __global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a,
         // factors) and double-reduces each chunk's sum
         for (int j = 0; j < a.rd; j += 2) {
             const bool two = j + 1 < a.rd;
-            const int64_t* __restrict__ m0 = mb + (int64_t)j * a.r;
-            const int64_t* __restrict__ m1 = two ? m0 + a.r : m0;
+            const int2* __restrict__ m0 = a.mat2 + ((int64_t)b * a.rd + j) * a.r;
+            const int2* __restrict__ m1 = two ? m0 + a.r : m0;
             int64_t v0 = 0, v1 = 0;
             bool first = true;
             for (int c0 = 0; c0 < a.r; c0 += a.chunk) {
                 const int lo = max(c0, u0), hi = min(min(c0 + a.chunk, a.r), u1);
                 i128 s0 = 0, s1 = 0;
-#pragma unroll 4
-                for (int u = lo; u < hi; u++) {
-                    const i128 x = (i128)xcol[u * BCONV_THREADS];
-                    s0 = (i128)((u128)s0 + (u128)((i128)__ldg(m0 + u) * x));
-                    s1 = (i128)((u128)s1 + (u128)((i128)__ldg(m1 + u) * x));
-                }
+                limb_mac2(xcol, m0, m1, lo, hi, s0, s1);
                 const int64_t r0 = double_red128(s0, dm.n[j], dm.ninv[j]);
                 v0 = first ? r0 : wadd(v0, r0);
                 if (two) {
@@ -237,9 +270,10 @@ namespace hc {
 hc_status launch_bconv_fused(hc_context ctx, const KView& src, const KView& dst, const int64_t* qinv,
                              const int64_t* mat, const int64_t* qmodp, const int32_t* ucol, int r, int rd, int nb,
                              int shift, int chunk, const KMods& sm, const KMods& dm, int64_t ns,
-                             const int64_t* sub_mul) {
+                             const int64_t* sub_mul, const int32_t* mat2) {
     BconvArgs a;
     a.sub_mul = sub_mul;
+    a.mat2 = reinterpret_cast<const int2*>(mat2);
     a.src = src;
     a.dst = dst;
     a.qinv = qinv, a.mat = mat, a.qmodp = qmodp, a.ucol = ucol;
