@@ -70,6 +70,11 @@ hc_status hc_event_record(hc_context ctx, hc_event ev) {
     return cuda_check(cudaEventRecord(ev->ev, stream_of(ctx)), "event record");
 }
 
+hc_status hc_stream_wait_event(hc_context ctx, hc_event ev) {
+    if (!ctx || !ev) return fail(HC_ERR_ARG, "null argument");
+    return cuda_check(cudaStreamWaitEvent(stream_of(ctx), ev->ev, 0), "stream wait");
+}
+
 hc_status hc_stream_create(void** out) {
     if (!out) return fail(HC_ERR_ARG, "null argument");
     cudaStream_t s = nullptr;

@@ -446,6 +446,10 @@ class Event:
     def record(self, be):
         check(lib().hc_event_record(be.h, self.h))
 
+    def wait(self, be):
+        """Makes the backend's current stream wait (on the device) for the work before this event."""
+        check(lib().hc_stream_wait_event(be.h, self.h))
+
     def query(self):
         """True once the work recorded before this event has completed (does not block)."""
         done = ctypes.c_int(0)

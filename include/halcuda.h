@@ -180,6 +180,9 @@ hc_status hc_memset_async(hc_context ctx, void* dst, int value, size_t bytes);
 hc_status hc_event_create(hc_event* out);
 hc_status hc_event_destroy(hc_event ev);
 hc_status hc_event_record(hc_context ctx, hc_event ev);
+/* Work issued to the context's current stream after this call starts only once the work recorded
+ * before `ev` has completed (a device-side dependency; the host does not block). */
+hc_status hc_stream_wait_event(hc_context ctx, hc_event ev);
 /* Extra streams for concurrent work on one context: create, select with hc_context_set_stream
  * (NULL selects the context's own stream again), destroy after their work is done. */
 hc_status hc_stream_create(void** out);
