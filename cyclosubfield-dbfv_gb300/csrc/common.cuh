@@ -40,6 +40,22 @@ __device__ __forceinline__ T* kat(const KView& v, int64_t i, int64_t j, int64_t 
     return reinterpret_cast<T*>(v.p) + i * v.s0 + j * v.s1 + k * v.s2 + (v.b3 ? 0 : l);
 }
 
+/// Device tables of one base conversion (built by the ring layer; bconv_fused_kernel reads them).
+struct BconvConsts {
+    const int64_t* qinv;   // [r] plain lifts of (Q_b / p_u)^-1 mod p_u, Montgomery factors
+    const int64_t* qinvp;  // [r] qinv[u] * (-p_u^-1) mod 2^64
+    const int64_t* mat;    // [nb][rd + 1][r] conversion matrix; row rd of each block: correction row
+    const int4* mat3;      // [nb][rd][r] rows 0..rd-1 as limbs (m mod 2^29, m >> 29, their sum, 0)
+    const int64_t* qmodp;  // [nb][rd]
+    const int64_t* qtab;   // [nb][rd][2 qhalf + 1] mul_mont(q, qmodp) for |q| <= qhalf
+    const int64_t* r2p;    // [rd] (R^2 mod p_j) * (-p_j^-1) mod 2^64
+    const int32_t* ucol;   // [nb][2] source column range of output block b
+    int qhalf;
+    int corr_limb;         // the correction row fits the limb products
+    int shift;             // log2 of the correction's fixed-point scale
+    int chunk;             // acc_before_reduce of the reference
+};
+
 /// Montgomery moduli of one call, by value in the kernel's parameter space.
 struct KMods {
     int64_t n[HC_MAX_MODS];
@@ -114,6 +130,22 @@ __device__ __forceinline__ int64_t to_mont64(int64_t x, int64_t n, int64_t ninv,
 }
 __device__ __forceinline__ int64_t to_mont128(i128 x, int64_t n, int64_t ninv, int64_t r3) {
     return mul_mont(red128(x, n, ninv), r3, n, ninv);
+}
+
+/// mul_mont(a, b) for a constant b with bp = b * ninv mod 2^64: the Montgomery quotient
+/// m = lo(a b) ninv equals a bp mod 2^64, and lo(a b) != 0 exactly when m != 0 (ninv is odd), so
+/// the low word of a b is never formed. The same integers as mul_mont(a, b, n, ninv).
+__device__ __forceinline__ int64_t mul_mont_c(int64_t a, int64_t b, int64_t bp, int64_t n) {
+    const int64_t m = (int64_t)((uint64_t)a * (uint64_t)bp);
+    return (int64_t)((uint64_t)__mul64hi(a, b) + (uint64_t)__mul64hi(m, n) + (uint64_t)(m != 0));
+}
+
+/// double_red128 of the 128-bit value hi:lo: the first reduction's carry out of the low word is
+/// (lo != 0) (the low words of x and m n cancel), so the low word of m n is never formed.
+__device__ __forceinline__ int64_t double_red_words(uint64_t lo, int64_t hi, int64_t n, int64_t ninv) {
+    const int64_t m = (int64_t)(lo * (uint64_t)ninv);
+    const i128 r1 = (i128)hi + (i128)__mul64hi(m, n) + (i128)(lo != 0);
+    return red128((uint64_t)r1, (int64_t)(r1 >> 64), n, ninv);
 }
 
 __device__ __forceinline__ i128 ld128(const void* p) {

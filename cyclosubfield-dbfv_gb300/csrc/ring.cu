@@ -24,10 +24,8 @@
 #include "common.cuh"
 
 namespace hc {
-hc_status launch_bconv_fused(hc_context ctx, const KView& src, const KView& dst, const int64_t* qinv,
-                             const int64_t* mat, const int64_t* qmodp, const int32_t* ucol, int r, int rd, int nb,
-                             int shift, int chunk, const KMods& sm, const KMods& dm, int64_t ns,
-                             const int64_t* sub_mul, const int32_t* mat2);
+hc_status launch_bconv_fused(hc_context ctx, const KView& src, const KView& dst, const BconvConsts& c, int r, int rd,
+                             int nb, const KMods& sm, const KMods& dm, int64_t ns, const int64_t* sub_mul);
 hc_status launch_galois(hc_context ctx, const KView& d, const KView& s, const uint32_t* p2, const uint32_t* p3);
 hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys, int nterms, const KView* add0,
                            const KView* add1, int full0, int full1, const KView& dst, const KMods& m,
@@ -443,44 +441,92 @@ struct TransformCache {
     Tensor kl, kk, ikl, ikk;
 };
 
-/// The base conversion kernel's limb form of a conversion matrix [nb][rd + 1][r] (the last row of
-/// each block is the correction row, kept in full width): the pairs (m mod 2^29, m >> 29) of the
-/// rows 0..rd-1, as [nb][rd][r] int2. The kernel multiplies them with the lifts split the same way
-/// and accumulates the three partial-product columns in int64 over groups of 16 terms, which is
-/// exact when |m| < 2^56 and the lifts satisfy |x| < 2^57, i.e. every source prime is below 2^57
-/// (which the ring's RNS factor size rule guarantees; checked here all the same).
-DBuf limb_matrix(hc_context ctx, const std::vector<int64_t>& mat, size_t nb, size_t rd, size_t r,
-                 int64_t max_src_p) {
-    REQUIRE(max_src_p < ((int64_t)1 << 57), HC_ERR_UNSUPPORTED, "base conversion: source prime above 2^57");
-    std::vector<int32_t> m2(nb * rd * r * 2);
-    for (size_t b = 0; b < nb; b++)
+/// Host mirror of the device Montgomery product mul_mont (the same integers).
+int64_t mul_mont_host(int64_t a, int64_t b, int64_t n, int64_t ninv) {
+    const i128 p = (i128)a * b;
+    const uint64_t lo = (uint64_t)p;
+    const int64_t m = (int64_t)(lo * (uint64_t)ninv);
+    const int64_t thi = (int64_t)(((i128)m * n) >> 64);
+    return (int64_t)((uint64_t)(int64_t)(p >> 64) + (uint64_t)thi + (uint64_t)(lo != 0));
+}
+
+/// Device tables of one base conversion in blocks (nb blocks of rd outputs over the source columns
+/// ucol[b]), as bconv_fused_kernel reads them (BconvConsts):
+///  - qinv / mat / qmodp / ucol: the reference's factors (the conversion matrix [nb][rd + 1][r] with
+///    the correction row last in each block);
+///  - mat3: the matrix rows 0..rd-1 as 29-bit limbs (m mod 2^29, m >> 29, their sum), for the
+///    kernel's exact int64 multiply-accumulate; it needs |m| < 2^56 and lifts |x| < 2^57, i.e.
+///    source primes below 2^57 (the ring's RNS factor size rule; checked here all the same);
+///  - qinvp, r2p: the Montgomery factors qinv[u] and R^2 mod p_j times -p^-1 mod 2^64, so that the
+///    kernel's products with them skip one 64-bit multiplication (mul_mont_c);
+///  - qtab: mul_mont(q, qmodp) for every correction q in [-qhalf, qhalf] (|q| is at most the
+///    block's source count, because 2^shift exceeds 4 r max(p)); larger q would be computed;
+///  - corr_limb: whether the correction row (round(2^shift / p_u)) is small enough for the limb
+///    products too.
+struct BconvTables {
+    DBuf qinv, qinvp, mat, mat3, qmodp, qtab, r2p, ucol;
+    BconvConsts c{};
+};
+
+void build_bconv_tables(hc_context ctx, BconvTables& t, const std::vector<int64_t>& qinv,
+                        const std::vector<hc_modulus>& sm, const std::vector<int64_t>& mat,
+                        const std::vector<int64_t>& qm, const std::vector<hc_modulus>& dm,
+                        const std::vector<int32_t>& uc, int shift, int chunk) {
+    const size_t r = sm.size(), rd = dm.size(), nb = uc.size() / 2;
+    int64_t maxsrc = 0;
+    for (auto& m : sm) maxsrc = std::max(maxsrc, m.n);
+    REQUIRE(maxsrc < ((int64_t)1 << 57), HC_ERR_UNSUPPORTED, "base conversion: source prime above 2^57");
+    size_t maxlen = 0;
+    for (size_t b = 0; b < nb; b++) maxlen = std::max(maxlen, (size_t)(uc[2 * b + 1] - uc[2 * b]));
+    std::vector<int32_t> m3(nb * rd * r * 4, 0);
+    std::vector<int64_t> qinvp(r), r2p(rd), qtab;
+    int64_t maxmq = 0;
+    for (size_t b = 0; b < nb; b++) {
         for (size_t j = 0; j < rd; j++)
             for (size_t u = 0; u < r; u++) {
                 const int64_t m = mat[(b * (rd + 1) + j) * r + u];
                 REQUIRE(m < ((int64_t)1 << 56) && m > -((int64_t)1 << 56), HC_ERR_UNSUPPORTED,
                         "base conversion: matrix entry above 2^56");
-                const size_t o = ((b * rd + j) * r + u) * 2;
-                m2[o] = (int32_t)(m & ((1 << 29) - 1));
-                m2[o + 1] = (int32_t)(m >> 29);
+                const size_t o = ((b * rd + j) * r + u) * 4;
+                m3[o] = (int32_t)(m & ((1 << 29) - 1));
+                m3[o + 1] = (int32_t)(m >> 29);
+                m3[o + 2] = m3[o] + m3[o + 1];
             }
-    return DBuf(ctx, m2.data(), m2.size() * 4);
+        for (size_t u = 0; u < r; u++) maxmq = std::max(maxmq, std::abs(mat[(b * (rd + 1) + rd) * r + u]));
+    }
+    for (size_t u = 0; u < r; u++) qinvp[u] = (int64_t)((uint64_t)qinv[u] * (uint64_t)sm[u].neg_inv_n);
+    for (size_t j = 0; j < rd; j++) r2p[j] = (int64_t)((uint64_t)dm[j].r2_mod_n * (uint64_t)dm[j].neg_inv_n);
+    const int qhalf = (int)maxlen;
+    for (size_t b = 0; b < nb; b++)
+        for (size_t j = 0; j < rd; j++)
+            for (int q = -qhalf; q <= qhalf; q++)
+                qtab.push_back(mul_mont_host(q, qm[b * rd + j], dm[j].n, dm[j].neg_inv_n));
+    t.qinv = DBuf(ctx, qinv.data(), r * 8);
+    t.qinvp = DBuf(ctx, qinvp.data(), r * 8);
+    t.mat = DBuf(ctx, mat.data(), mat.size() * 8);
+    t.mat3 = DBuf(ctx, m3.data(), m3.size() * 4);
+    t.qmodp = DBuf(ctx, qm.data(), qm.size() * 8);
+    t.qtab = DBuf(ctx, qtab.data(), qtab.size() * 8);
+    t.r2p = DBuf(ctx, r2p.data(), rd * 8);
+    t.ucol = DBuf(ctx, uc.data(), uc.size() * 4);
+    BconvConsts& c = t.c;
+    c.qinv = t.qinv.as<int64_t>(), c.qinvp = t.qinvp.as<int64_t>(), c.mat = t.mat.as<int64_t>();
+    c.mat3 = t.mat3.as<int4>(), c.qmodp = t.qmodp.as<int64_t>(), c.qtab = t.qtab.as<int64_t>();
+    c.r2p = t.r2p.as<int64_t>(), c.ucol = t.ucol.as<int32_t>();
+    c.qhalf = qhalf, c.shift = shift, c.chunk = chunk;
+    // the correction row's limb products x0 mq, x1 mq summed over a block stay below 2^63
+    c.corr_limb = maxmq < ((int64_t)1 << 30) && (i128)maxmq * ((i128)1 << 29) * (i128)maxlen < ((i128)1 << 63);
 }
 
 struct BconvCache {
     Base src, dst;
-    int shift;
-    int chunk;
-    DBuf qinv, mat, qmodp, ucol;
-    DBuf mat2;  // limb form of mat (limb_matrix)
+    BconvTables t;
 };
 
 struct GadgetCache {
     Base base;
     Digits digits;
-    int shift;
-    int chunk;
-    DBuf dinv, mat, dmodp, ucol;
-    DBuf mat2;  // as BconvCache::mat2
+    BconvTables t;
 };
 
 struct PermCache {
@@ -502,6 +548,7 @@ struct hc_ring_s {
     std::map<Base, std::unique_ptr<DBuf>> one_cache;
     std::map<std::pair<Base, i128>, std::unique_ptr<Tensor>> scalar_cache;
     std::map<std::pair<Base, Base>, std::unique_ptr<Tensor>> qinv_cache;
+    std::map<std::pair<Base, Base>, std::unique_ptr<DBuf>> qinv_pair_cache;
 
     ~hc_ring_s() {
         cudaStreamSynchronize(stream_of(ctx));
@@ -688,11 +735,11 @@ struct hc_ring_s {
         c->src = src, c->dst = dst;
         const size_t r = src.size(), rd = dst.size();
         int64_t mx = std::max(max_p(src), max_p(dst)), mn = min_p(src);
-        c->shift = (int)std::max<size_t>(64, bitlen_u128((u128)(4 * (i128)r * mx + 1)));
-        REQUIRE(c->shift <= 126, HC_ERR_UNSUPPORTED, "base conversion precision");
-        const i128 qt = (i128)1 << c->shift;
+        const int shift = (int)std::max<size_t>(64, bitlen_u128((u128)(4 * (i128)r * mx + 1)));
+        REQUIRE(shift <= 126, HC_ERR_UNSUPPORTED, "base conversion precision");
+        const i128 qt = (i128)1 << shift;
         REQUIRE((qt - 1) / mn + 1 <= INT64_MAX, HC_ERR_ARG, "correction vector coefficients don't fit into an i64");
-        c->chunk = (int)std::min<i128>(I128MAX / ((i128)mx * mx), 1 << 30);
+        const int chunk = (int)std::min<i128>(I128MAX / ((i128)mx * mx), 1 << 30);
         std::vector<int64_t> qinv(r), mat((rd + 1) * r), qm(rd);
         for (size_t u = 0; u < r; u++) {
             int64_t pu = prime(src[u]), qo = 1;
@@ -715,27 +762,21 @@ struct hc_ring_s {
             i128 a = qt, bp = prime(src[u]);
             mat[rd * r + u] = (int64_t)((a + bp / 2) / bp);
         }
-        int32_t uc[2] = {0, (int32_t)r};
-        c->qinv = DBuf(ctx, qinv.data(), qinv.size() * 8);
-        c->mat = DBuf(ctx, mat.data(), mat.size() * 8);
-        c->mat2 = limb_matrix(ctx, mat, 1, rd, r, max_p(src));
-        c->qmodp = DBuf(ctx, qm.data(), qm.size() * 8);
-        c->ucol = DBuf(ctx, uc, sizeof(uc));
+        build_bconv_tables(ctx, c->t, qinv, mods(src), mat, qm, mods(dst), {0, (int32_t)r}, shift, chunk);
         bcache.push_back(std::move(c));
         return *bcache.back();
     }
 
-    /// `sub_mul` (optional, one Montgomery factor per destination prime): instead of writing the
-    /// conversion v, dst <- mul_mont(dst - v, sub_mul) (the caller's hal_sub_i64 and hal_mul_mont64,
-    /// fused into the store)
+    /// `sub_mul` (optional, [2][rd]: one Montgomery factor b per destination prime, then b times
+    /// -p^-1 mod 2^64): instead of writing the conversion v, dst <- mul_mont(dst - v, b) (the
+    /// caller's hal_sub_i64 and hal_mul_mont64, fused into the store)
     void bconv(const hc_view& dst, const Base& db, const hc_view& src, const Base& sb,
                const int64_t* sub_mul = nullptr) {
         check_view(src, src.shape[0], (int64_t)sb.size(), src.shape[2], src.shape[3], "bconv src");
         check_view(dst, src.shape[0], (int64_t)db.size(), src.shape[2], src.shape[3], "bconv dst");
         BconvCache& c = bconv_cache(sb, db);
-        CK(launch_bconv_fused(ctx, kv(src), kv(dst), c.qinv.as<int64_t>(), c.mat.as<int64_t>(),
-                              c.qmodp.as<int64_t>(), c.ucol.as<int32_t>(), (int)sb.size(), (int)db.size(), 1,
-                              c.shift, c.chunk, kmods(sb), kmods(db), src.shape[0], sub_mul, c.mat2.as<int32_t>()));
+        CK(launch_bconv_fused(ctx, kv(src), kv(dst), c.t.c, (int)sb.size(), (int)db.size(), 1, kmods(sb), kmods(db),
+                              src.shape[0], sub_mul));
     }
 
     GadgetCache& gadget_cache(const Base& b, const Digits& digits) {
@@ -754,10 +795,10 @@ struct hc_ring_s {
         int64_t mx = max_p(b), mn = min_p(b);
         size_t maxlen = 0;
         for (auto& dg : digits) maxlen = std::max(maxlen, dg.second - dg.first);
-        c->shift = (int)std::max<size_t>(64, bitlen_u128((u128)(4 * (i128)maxlen * mx + 1)));
-        const i128 qt = (i128)1 << c->shift;
+        const int shift = (int)std::max<size_t>(64, bitlen_u128((u128)(4 * (i128)maxlen * mx + 1)));
+        const i128 qt = (i128)1 << shift;
         REQUIRE((qt - 1) / mn + 1 <= INT64_MAX, HC_ERR_ARG, "correction vector coefficients don't fit into an i64");
-        c->chunk = (int)std::min<i128>(I128MAX / ((i128)mx * mx), 1 << 30);
+        const int chunk = (int)std::min<i128>(I128MAX / ((i128)mx * mx), 1 << 30);
         auto dover = [&](size_t di, size_t u, int64_t q) {
             int64_t v = 1;
             for (size_t l = digits[di].first; l < digits[di].second; l++)
@@ -787,11 +828,7 @@ struct hc_ring_s {
                 mat[(di * (r + 1) + r) * r + u] = (int64_t)((qt + bp / 2) / bp);
             }
         }
-        c->dinv = DBuf(ctx, dinv.data(), dinv.size() * 8);
-        c->mat = DBuf(ctx, mat.data(), mat.size() * 8);
-        c->mat2 = limb_matrix(ctx, mat, d, r, r, mx);
-        c->dmodp = DBuf(ctx, dm.data(), dm.size() * 8);
-        c->ucol = DBuf(ctx, uc.data(), uc.size() * 4);
+        build_bconv_tables(ctx, c->t, dinv, mods(b), mat, dm, mods(b), uc, shift, chunk);
         gcache.push_back(std::move(c));
         return *gcache.back();
     }
@@ -803,9 +840,8 @@ struct hc_ring_s {
                    "gadget dst");
         GadgetCache& c = gadget_cache(b, digits);
         KMods km = kmods(b);
-        CK(launch_bconv_fused(ctx, kv(src), kv(dst), c.dinv.as<int64_t>(), c.mat.as<int64_t>(), c.dmodp.as<int64_t>(),
-                              c.ucol.as<int32_t>(), (int)b.size(), (int)b.size(), (int)digits.size(), c.shift, c.chunk,
-                              km, km, src.shape[0], nullptr, c.mat2.as<int32_t>()));
+        CK(launch_bconv_fused(ctx, kv(src), kv(dst), c.t.c, (int)b.size(), (int)b.size(), (int)digits.size(), km, km,
+                              src.shape[0], nullptr));
     }
 
     // ---------------------------------------------------------------- Galois
@@ -878,6 +914,23 @@ struct hc_ring_s {
         auto t = std::make_unique<Tensor>(scalar_tensor_big(of, [&](int64_t p) { return invm(q_mod(div, p), p); }));
         auto& ref = *t;
         qinv_cache[key] = std::move(t);
+        return ref;
+    }
+    /// The factors of inv_modulus_tensor(of, div) as the base conversion's `sub_mul` pairs:
+    /// [2][|of|] = (b_j, b_j * (-p_j^-1) mod 2^64), cached
+    const DBuf& inv_modulus_pairs(const Base& of, const Base& div) {
+        auto key = std::make_pair(of, div);
+        auto it = qinv_pair_cache.find(key);
+        if (it != qinv_pair_cache.end()) return *it->second;
+        std::vector<int64_t> v(2 * of.size());
+        for (size_t j = 0; j < of.size(); j++) {
+            const int64_t p = prime(of[j]);
+            v[j] = mont_repr(centred(invm(q_mod(div, p), p), p), p);
+            v[of.size() + j] = (int64_t)((uint64_t)v[j] * (uint64_t)factors[of[j]].mod.neg_inv_n);
+        }
+        auto t = std::make_unique<DBuf>(ctx, v.data(), v.size() * 8);
+        auto& ref = *t;
+        qinv_pair_cache[key] = std::move(t);
         return ref;
     }
     /// [1, r, 1, 1] tensor holding mont(smallest_lift(residue(p))) (src/ring.rs:890-902)
@@ -1181,8 +1234,7 @@ Tensor rescale_to_base(hc_ring R, const hc_view& x, const Base& lifted, size_t b
     if (!pre_scaled) CK(hc_mul_mont64(R->ctx, x, R->scalar_tensor(lifted, t).view(), ml.data(), ml.size()));
     hc_view xlo = vbase(x, 0, (int64_t)base_len), xhi = vbase(x, (int64_t)base_len, (int64_t)lifted.size());
     // xhi <- (xhi - bconv(xlo)) * (Q_base^-1 mod p), the subtraction and product in the conversion's store
-    const Tensor& qinv = R->inv_modulus_tensor(ext, base);
-    R->bconv(xhi, ext, xlo, base, (const int64_t*)qinv.view().ptr);
+    R->bconv(xhi, ext, xlo, base, R->inv_modulus_pairs(ext, base).as<int64_t>());
     Tensor out = temp(R->ctx, count, (int64_t)base_len, R->dl(), R->dk());
     R->bconv(out.view(), base, xhi, ext);
     return out;

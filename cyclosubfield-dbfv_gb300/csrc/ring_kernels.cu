@@ -22,50 +22,66 @@ constexpr int BCONV_THREADS = 128;
 struct BconvArgs {
     KView src;  // [ns, r, dl, dk]
     KView dst;  // [ns * nb, rd, dl, dk]
-    const int64_t* qinv;   // [r] plain lifts of (Q_b / p_u)^-1 mod p_u
-    const int64_t* mat;    // [nb][rd + 1][r]
-    const int64_t* qmodp;  // [nb][rd]
-    const int32_t* ucol;   // [nb][2] source column range of output block b
+    BconvConsts c;
     int r, rd, nb;
-    int shift;
-    int chunk;  // acc_before_reduce of the reference
     int64_t npos;
-    const int64_t* sub_mul;  // optional [rd]: store mul_mont(dst - v, sub_mul[j]) instead of v
-    const int2* mat2;        // limb form of the rows 0..rd-1 of mat, [nb][rd][r] (see limb_mac2)
+    const int64_t* sub_mul;  // optional [2][rd]: store mul_mont(dst - v, b_j) instead of v (b_j, b_j ninv)
 };
 
 constexpr int LIMB_BITS = 29;
-constexpr int LIMB_GROUP = 16;  // terms per int64 partial-sum group (sums stay below 2^62)
+constexpr int LIMB_GROUP = 16;  // terms per int64 partial-sum group
 
-/// One output pair's multiply-accumulate over the lifts u in [lo, hi): exact sum_u m_u x_u as i128.
-/// The operands are split as v = v1 2^29 + v0 with 0 <= v0 < 2^29; with |x| < 2^57 and |m| < 2^56
-/// every partial product x0 m0, x0 m1 + x1 m0, x1 m1 is below 2^58 in magnitude, so 16 of them add
-/// up in int64 without overflow; each group is then folded into the 128-bit sum.
-__device__ __forceinline__ void limb_mac2(const int2* __restrict__ xcol, const int2* __restrict__ m0,
-                                          const int2* __restrict__ m1, int lo, int hi, i128& s0, i128& s1) {
+/// hi:lo += a00 + a01 2^29 + a11 2^58 (a00 >= 0).
+__device__ __forceinline__ void fold_limbs(uint64_t& lo, int64_t& hi, int64_t a00, int64_t a01, int64_t a11) {
+    const u128 s = (u128)lo + (uint64_t)a00 + ((uint64_t)a01 << LIMB_BITS) + ((uint64_t)a11 << (2 * LIMB_BITS));
+    lo = (uint64_t)s;
+    hi = (int64_t)((uint64_t)hi + (uint64_t)(a01 >> (64 - LIMB_BITS)) + (uint64_t)(a11 >> (64 - 2 * LIMB_BITS)) +
+                   (uint64_t)(s >> 64));
+}
+
+/// One output pair's multiply-accumulate over the lifts u in [lo, hi): the exact sums
+/// sum_u m_u x_u as 128-bit words. Operands are split as v = v1 2^29 + v0 with 0 <= v0 < 2^29;
+/// with |x| < 2^57 and |m| < 2^56 (so |x1| <= 2^28, |m1| <= 2^27) the products x0 m0 < 2^58,
+/// |x1 m1| <= 2^55 and |(x0 + x1)(m0 + m1)| < 2^58.91 add up over 16 terms in int64 without
+/// overflow; the middle column x0 m1 + x1 m0 is the Karatsuba difference of the three sums.
+__device__ __forceinline__ void limb_mac2(const int2* __restrict__ xcol, const int4* __restrict__ m0,
+                                          const int4* __restrict__ m1, int lo, int hi, uint64_t& l0, int64_t& h0,
+                                          uint64_t& l1, int64_t& h1) {
     for (int g0 = lo; g0 < hi; g0 += LIMB_GROUP) {
         const int g1 = min(g0 + LIMB_GROUP, hi);
-        int64_t a00 = 0, a01 = 0, a11 = 0, b00 = 0, b01 = 0, b11 = 0;
+        int64_t a00 = 0, am = 0, a11 = 0, b00 = 0, bm = 0, b11 = 0;
 #pragma unroll 4
         for (int u = g0; u < g1; u++) {
             const int2 x = xcol[u * BCONV_THREADS];
-            const int2 p = __ldg(m0 + u), q = __ldg(m1 + u);
+            const int xs = x.x + x.y;
+            const int4 p = __ldg(m0 + u), q = __ldg(m1 + u);
             a00 += (int64_t)x.x * p.x;
-            a01 += (int64_t)x.x * p.y;
-            a01 += (int64_t)x.y * p.x;
             a11 += (int64_t)x.y * p.y;
+            am += (int64_t)xs * p.z;
             b00 += (int64_t)x.x * q.x;
-            b01 += (int64_t)x.x * q.y;
-            b01 += (int64_t)x.y * q.x;
             b11 += (int64_t)x.y * q.y;
+            bm += (int64_t)xs * q.z;
         }
-        s0 = (i128)((u128)s0 + (u128)(i128)a00 + ((u128)(i128)a01 << LIMB_BITS) + ((u128)(i128)a11 << (2 * LIMB_BITS)));
-        s1 = (i128)((u128)s1 + (u128)(i128)b00 + ((u128)(i128)b01 << LIMB_BITS) + ((u128)(i128)b11 << (2 * LIMB_BITS)));
+        fold_limbs(l0, h0, a00, am - a00 - a11, a11);
+        fold_limbs(l1, h1, b00, bm - b00 - b11, b11);
     }
 }
 
-/// The products with the conversion matrix use its limb form (BconvArgs::mat2): the shared array
-/// holds each lift as its limb pair (x mod 2^29, x >> 29).
+/// The conversion's epilogue for output j of block b: v (the double-reduced sums) plus the
+/// correction mul_mont(q, qmodp), to Montgomery form, optionally dst <- mul_mont(dst - y, b_j).
+__device__ __forceinline__ void bconv_store(const BconvArgs& a, const KMods& dm, int b, int j, int64_t q, int64_t v,
+                                            int64_t* p) {
+    const int64_t n = dm.n[j], ninv = dm.ninv[j];
+    const int64_t* qt = a.c.qtab + ((int64_t)b * a.rd + j) * (2 * a.c.qhalf + 1) + a.c.qhalf;
+    const int64_t qm = (q >= -a.c.qhalf && q <= a.c.qhalf) ? __ldg(qt + q)
+                                                            : mul_mont(q, a.c.qmodp[(int64_t)b * a.rd + j], n, ninv);
+    const int64_t y = mul_mont_c(wadd(v, qm), dm.r2[j], __ldg(a.c.r2p + j), n);  // to_mont64
+    *p = a.sub_mul ? mul_mont_c(wsub(*p, y), __ldg(a.sub_mul + j), __ldg(a.sub_mul + a.rd + j), n) : y;
+}
+
+/// BEHZ base conversion of one position per thread (BConvCache::bconv, src/ring.rs:1660-1702,
+/// and the gadget form of :1800-1852). The products with the conversion matrix use its limb form:
+/// the shared array holds each lift as its limb pair (x mod 2^29, x >> 29).
 __global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a, KMods sm, KMods dm) {
     extern __shared__ int2 xs[];  // [r][BCONV_THREADS]
     const int64_t i = blockIdx.y;
@@ -79,61 +95,61 @@ __global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a,
     // the source is multiplied by (Q/p)^-1 in Montgomery form, giving plain lifts in (-p, p)
     for (int u = 0; u < a.r; u++) {
         int64_t x = live ? *kat<int64_t>(a.src, i, u, k, l) : 0;
-        x = live ? mul_mont(x, a.qinv[u], sm.n[u], sm.ninv[u]) : 0;
+        x = live ? mul_mont_c(x, __ldg(a.c.qinv + u), __ldg(a.c.qinvp + u), sm.n[u]) : 0;
         xs[u * BCONV_THREADS + threadIdx.x] = make_int2((int)(x & ((1 << LIMB_BITS) - 1)), (int)(x >> LIMB_BITS));
     }
     if (!live) return;
-    const i128 half = (i128)1 << (a.shift - 1);
+    const i128 half = (i128)1 << (a.c.shift - 1);
     const int2* xcol = xs + threadIdx.x;  // this thread's lifts, stride BCONV_THREADS
-    auto lift = [&](int u) -> int64_t {
-        const int2 v = xcol[u * BCONV_THREADS];
-        return (int64_t)v.y * ((int64_t)1 << LIMB_BITS) + v.x;
-    };
     for (int b = 0; b < a.nb; b++) {
-        const int u0 = a.ucol[2 * b], u1 = a.ucol[2 * b + 1];
-        const int64_t* __restrict__ mb = a.mat + (int64_t)b * (a.rd + 1) * a.r;
-        i128 corr = 0;
-        {
-            const int64_t* mq = mb + (int64_t)a.rd * a.r;
+        const int u0 = a.c.ucol[2 * b], u1 = a.c.ucol[2 * b + 1];
+        const int64_t* __restrict__ mq = a.c.mat + ((int64_t)b * (a.rd + 1) + a.rd) * a.r;
+        // the correction q = round(sum_u x_u round(2^shift / p_u) / 2^shift)
+        i128 corr;
+        if (a.c.corr_limb) {
+            int64_t c0 = 0, c1 = 0;
 #pragma unroll 4
-            for (int u = u0; u < u1; u++)
-                corr = (i128)((u128)corr + (u128)((i128)__ldg(mq + u) * (i128)lift(u)));
+            for (int u = u0; u < u1; u++) {
+                const int2 x = xcol[u * BCONV_THREADS];
+                const int m = (int)__ldg(mq + u);
+                c0 += (int64_t)x.x * m;
+                c1 += (int64_t)x.y * m;
+            }
+            corr = (i128)c0 + (i128)((u128)(i128)c1 << LIMB_BITS);
+        } else {
+            corr = 0;
+            for (int u = u0; u < u1; u++) {
+                const int2 x = xcol[u * BCONV_THREADS];
+                const int64_t lift = (int64_t)x.y * ((int64_t)1 << LIMB_BITS) + x.x;
+                corr = (i128)((u128)corr + (u128)((i128)__ldg(mq + u) * (i128)lift));
+            }
         }
-        const int64_t q = (int64_t)((i128)((u128)corr + (u128)half) >> a.shift);
+        const int64_t q = (int64_t)((i128)((u128)corr + (u128)half) >> a.c.shift);
         // two output rows per pass over the lifts (each lift is read once for both); the
         // reference's chunked matmul (src/ring.rs:1678-1691) splits the columns into chunks of
         // `chunk` (one chunk whenever r <= chunk, which holds for all 57-bit bases up to 8192
         // factors) and double-reduces each chunk's sum
         for (int j = 0; j < a.rd; j += 2) {
             const bool two = j + 1 < a.rd;
-            const int2* __restrict__ m0 = a.mat2 + ((int64_t)b * a.rd + j) * a.r;
-            const int2* __restrict__ m1 = two ? m0 + a.r : m0;
+            const int4* __restrict__ m0 = a.c.mat3 + ((int64_t)b * a.rd + j) * a.r;
+            const int4* __restrict__ m1 = two ? m0 + a.r : m0;
             int64_t v0 = 0, v1 = 0;
             bool first = true;
-            for (int c0 = 0; c0 < a.r; c0 += a.chunk) {
-                const int lo = max(c0, u0), hi = min(min(c0 + a.chunk, a.r), u1);
-                i128 s0 = 0, s1 = 0;
-                limb_mac2(xcol, m0, m1, lo, hi, s0, s1);
-                const int64_t r0 = double_red128(s0, dm.n[j], dm.ninv[j]);
+            for (int c0 = 0; c0 < a.r; c0 += a.c.chunk) {
+                const int lo = max(c0, u0), hi = min(min(c0 + a.c.chunk, a.r), u1);
+                uint64_t l0 = 0, l1 = 0;
+                int64_t h0 = 0, h1 = 0;
+                limb_mac2(xcol, m0, m1, lo, hi, l0, h0, l1, h1);
+                const int64_t r0 = double_red_words(l0, h0, dm.n[j], dm.ninv[j]);
                 v0 = first ? r0 : wadd(v0, r0);
                 if (two) {
-                    const int64_t r1 = double_red128(s1, dm.n[j + 1], dm.ninv[j + 1]);
+                    const int64_t r1 = double_red_words(l1, h1, dm.n[j + 1], dm.ninv[j + 1]);
                     v1 = first ? r1 : wadd(v1, r1);
                 }
                 first = false;
             }
-            v0 = wadd(v0, mul_mont(q, a.qmodp[(int64_t)b * a.rd + j], dm.n[j], dm.ninv[j]));
-            {
-                int64_t* p = kat<int64_t>(a.dst, i * a.nb + b, j, k, l);
-                const int64_t y = to_mont64(v0, dm.n[j], dm.ninv[j], dm.r2[j]);
-                *p = a.sub_mul ? mul_mont(wsub(*p, y), a.sub_mul[j], dm.n[j], dm.ninv[j]) : y;
-            }
-            if (two) {
-                v1 = wadd(v1, mul_mont(q, a.qmodp[(int64_t)b * a.rd + j + 1], dm.n[j + 1], dm.ninv[j + 1]));
-                int64_t* p = kat<int64_t>(a.dst, i * a.nb + b, j + 1, k, l);
-                const int64_t y = to_mont64(v1, dm.n[j + 1], dm.ninv[j + 1], dm.r2[j + 1]);
-                *p = a.sub_mul ? mul_mont(wsub(*p, y), a.sub_mul[j + 1], dm.n[j + 1], dm.ninv[j + 1]) : y;
-            }
+            bconv_store(a, dm, b, j, q, v0, kat<int64_t>(a.dst, i * a.nb + b, j, k, l));
+            if (two) bconv_store(a, dm, b, j + 1, q, v1, kat<int64_t>(a.dst, i * a.nb + b, j + 1, k, l));
         }
     }
 }
@@ -267,17 +283,14 @@ void grid_lines(hc_context ctx, int64_t n3, int64_t lines, int* chunks, unsigned
 
 namespace hc {
 
-hc_status launch_bconv_fused(hc_context ctx, const KView& src, const KView& dst, const int64_t* qinv,
-                             const int64_t* mat, const int64_t* qmodp, const int32_t* ucol, int r, int rd, int nb,
-                             int shift, int chunk, const KMods& sm, const KMods& dm, int64_t ns,
-                             const int64_t* sub_mul, const int32_t* mat2) {
+hc_status launch_bconv_fused(hc_context ctx, const KView& src, const KView& dst, const BconvConsts& c, int r, int rd,
+                             int nb, const KMods& sm, const KMods& dm, int64_t ns, const int64_t* sub_mul) {
     BconvArgs a;
-    a.sub_mul = sub_mul;
-    a.mat2 = reinterpret_cast<const int2*>(mat2);
     a.src = src;
     a.dst = dst;
-    a.qinv = qinv, a.mat = mat, a.qmodp = qmodp, a.ucol = ucol;
-    a.r = r, a.rd = rd, a.nb = nb, a.shift = shift, a.chunk = chunk;
+    a.c = c;
+    a.r = r, a.rd = rd, a.nb = nb;
+    a.sub_mul = sub_mul;
     a.npos = src.n2 * src.n3;
     if (a.npos == 0 || ns == 0 || rd == 0) return HC_OK;
     size_t smem = (size_t)r * BCONV_THREADS * 8;
