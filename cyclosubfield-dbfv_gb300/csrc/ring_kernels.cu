@@ -13,6 +13,8 @@
 //    baby-step inner product over the digit convolution (dbfv_acc_inner_product_element_lprime,
 //    src/dbfv.rs:291-399), the addition of the carried result (dbfv_acc_add, :153-163) and the
 //    reduction (dbfv_finish_accumulator, :401-404), without the wide accumulator in HBM.
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace {
@@ -24,6 +26,7 @@ struct BconvArgs {
     KView dst;  // [ns * nb, rd, dl, dk]
     BconvConsts c;
     int r, rd, nb;
+    int ochunk;  // outputs per CTA (even): blockIdx.z selects the outputs [z ochunk, (z + 1) ochunk)
     int64_t npos;
     const int64_t* sub_mul;  // optional [2][rd]: store mul_mont(dst - v, b_j) instead of v (b_j, b_j ninv)
 };
@@ -80,77 +83,74 @@ __device__ __forceinline__ void bconv_store(const BconvArgs& a, const KMods& dm,
 }
 
 /// BEHZ base conversion of one position per thread (BConvCache::bconv, src/ring.rs:1660-1702,
-/// and the gadget form of :1800-1852). The products with the conversion matrix use its limb form:
-/// the shared array holds each lift as its limb pair (x mod 2^29, x >> 29).
+/// and the gadget form of :1800-1852). CTA (x, y, z): 128 positions of source row y / nb, output
+/// block y % nb (a gadget digit), outputs [z ochunk, (z + 1) ochunk) of the block; only the
+/// block's own source columns are lifted. The products with the conversion matrix use its limb
+/// form: the shared array holds each lift as its limb pair (x mod 2^29, x >> 29).
 __global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a, KMods sm, KMods dm) {
     extern __shared__ int2 xs[];  // [r][BCONV_THREADS]
-    const int64_t i = blockIdx.y;
+    const int b = (int)(blockIdx.y % (unsigned)a.nb);
+    const int64_t i = blockIdx.y / (unsigned)a.nb;
+    const int jbeg = (int)blockIdx.z * a.ochunk, jend = min(a.rd, jbeg + a.ochunk);
+    const int u0 = a.c.ucol[2 * b], u1 = a.c.ucol[2 * b + 1];
     const int64_t pos = (int64_t)blockIdx.x * BCONV_THREADS + threadIdx.x;
-    const bool live = pos < a.npos;
-    int64_t k = 0, l = 0;
-    if (live) {
-        k = pos / a.src.n3;
-        l = pos - k * a.src.n3;
-    }
+    if (pos >= a.npos) return;
+    const int64_t k = pos / a.src.n3, l = pos - k * a.src.n3;
     // the source is multiplied by (Q/p)^-1 in Montgomery form, giving plain lifts in (-p, p)
-    for (int u = 0; u < a.r; u++) {
-        int64_t x = live ? *kat<int64_t>(a.src, i, u, k, l) : 0;
-        x = live ? mul_mont_c(x, __ldg(a.c.qinv + u), __ldg(a.c.qinvp + u), sm.n[u]) : 0;
+    for (int u = u0; u < u1; u++) {
+        int64_t x = *kat<int64_t>(a.src, i, u, k, l);
+        x = mul_mont_c(x, __ldg(a.c.qinv + u), __ldg(a.c.qinvp + u), sm.n[u]);
         xs[u * BCONV_THREADS + threadIdx.x] = make_int2((int)(x & ((1 << LIMB_BITS) - 1)), (int)(x >> LIMB_BITS));
     }
-    if (!live) return;
     const i128 half = (i128)1 << (a.c.shift - 1);
     const int2* xcol = xs + threadIdx.x;  // this thread's lifts, stride BCONV_THREADS
-    for (int b = 0; b < a.nb; b++) {
-        const int u0 = a.c.ucol[2 * b], u1 = a.c.ucol[2 * b + 1];
-        const int64_t* __restrict__ mq = a.c.mat + ((int64_t)b * (a.rd + 1) + a.rd) * a.r;
-        // the correction q = round(sum_u x_u round(2^shift / p_u) / 2^shift)
-        i128 corr;
-        if (a.c.corr_limb) {
-            int64_t c0 = 0, c1 = 0;
+    const int64_t* __restrict__ mq = a.c.mat + ((int64_t)b * (a.rd + 1) + a.rd) * a.r;
+    // the correction q = round(sum_u x_u round(2^shift / p_u) / 2^shift)
+    i128 corr;
+    if (a.c.corr_limb) {
+        int64_t c0 = 0, c1 = 0;
 #pragma unroll 4
-            for (int u = u0; u < u1; u++) {
-                const int2 x = xcol[u * BCONV_THREADS];
-                const int m = (int)__ldg(mq + u);
-                c0 += (int64_t)x.x * m;
-                c1 += (int64_t)x.y * m;
-            }
-            corr = (i128)c0 + (i128)((u128)(i128)c1 << LIMB_BITS);
-        } else {
-            corr = 0;
-            for (int u = u0; u < u1; u++) {
-                const int2 x = xcol[u * BCONV_THREADS];
-                const int64_t lift = (int64_t)x.y * ((int64_t)1 << LIMB_BITS) + x.x;
-                corr = (i128)((u128)corr + (u128)((i128)__ldg(mq + u) * (i128)lift));
-            }
+        for (int u = u0; u < u1; u++) {
+            const int2 x = xcol[u * BCONV_THREADS];
+            const int m = (int)__ldg(mq + u);
+            c0 += (int64_t)x.x * m;
+            c1 += (int64_t)x.y * m;
         }
-        const int64_t q = (int64_t)((i128)((u128)corr + (u128)half) >> a.c.shift);
-        // two output rows per pass over the lifts (each lift is read once for both); the
-        // reference's chunked matmul (src/ring.rs:1678-1691) splits the columns into chunks of
-        // `chunk` (one chunk whenever r <= chunk, which holds for all 57-bit bases up to 8192
-        // factors) and double-reduces each chunk's sum
-        for (int j = 0; j < a.rd; j += 2) {
-            const bool two = j + 1 < a.rd;
-            const int4* __restrict__ m0 = a.c.mat3 + ((int64_t)b * a.rd + j) * a.r;
-            const int4* __restrict__ m1 = two ? m0 + a.r : m0;
-            int64_t v0 = 0, v1 = 0;
-            bool first = true;
-            for (int c0 = 0; c0 < a.r; c0 += a.c.chunk) {
-                const int lo = max(c0, u0), hi = min(min(c0 + a.c.chunk, a.r), u1);
-                uint64_t l0 = 0, l1 = 0;
-                int64_t h0 = 0, h1 = 0;
-                limb_mac2(xcol, m0, m1, lo, hi, l0, h0, l1, h1);
-                const int64_t r0 = double_red_words(l0, h0, dm.n[j], dm.ninv[j]);
-                v0 = first ? r0 : wadd(v0, r0);
-                if (two) {
-                    const int64_t r1 = double_red_words(l1, h1, dm.n[j + 1], dm.ninv[j + 1]);
-                    v1 = first ? r1 : wadd(v1, r1);
-                }
-                first = false;
-            }
-            bconv_store(a, dm, b, j, q, v0, kat<int64_t>(a.dst, i * a.nb + b, j, k, l));
-            if (two) bconv_store(a, dm, b, j + 1, q, v1, kat<int64_t>(a.dst, i * a.nb + b, j + 1, k, l));
+        corr = (i128)c0 + (i128)((u128)(i128)c1 << LIMB_BITS);
+    } else {
+        corr = 0;
+        for (int u = u0; u < u1; u++) {
+            const int2 x = xcol[u * BCONV_THREADS];
+            const int64_t lift = (int64_t)x.y * ((int64_t)1 << LIMB_BITS) + x.x;
+            corr = (i128)((u128)corr + (u128)((i128)__ldg(mq + u) * (i128)lift));
         }
+    }
+    const int64_t q = (int64_t)((i128)((u128)corr + (u128)half) >> a.c.shift);
+    // two output rows per pass over the lifts (each lift is read once for both); the
+    // reference's chunked matmul (src/ring.rs:1678-1691) splits the columns into chunks of
+    // `chunk` (one chunk whenever r <= chunk, which holds for all 57-bit bases up to 8192
+    // factors) and double-reduces each chunk's sum
+    for (int j = jbeg; j < jend; j += 2) {
+        const bool two = j + 1 < jend;
+        const int4* __restrict__ m0 = a.c.mat3 + ((int64_t)b * a.rd + j) * a.r;
+        const int4* __restrict__ m1 = two ? m0 + a.r : m0;
+        int64_t v0 = 0, v1 = 0;
+        bool first = true;
+        for (int c0 = 0; c0 < a.r; c0 += a.c.chunk) {
+            const int lo = max(c0, u0), hi = min(min(c0 + a.c.chunk, a.r), u1);
+            uint64_t l0 = 0, l1 = 0;
+            int64_t h0 = 0, h1 = 0;
+            limb_mac2(xcol, m0, m1, lo, hi, l0, h0, l1, h1);
+            const int64_t r0 = double_red_words(l0, h0, dm.n[j], dm.ninv[j]);
+            v0 = first ? r0 : wadd(v0, r0);
+            if (two) {
+                const int64_t r1 = double_red_words(l1, h1, dm.n[j + 1], dm.ninv[j + 1]);
+                v1 = first ? r1 : wadd(v1, r1);
+            }
+            first = false;
+        }
+        bconv_store(a, dm, b, j, q, v0, kat<int64_t>(a.dst, i * a.nb + b, j, k, l));
+        if (two) bconv_store(a, dm, b, j + 1, q, v1, kat<int64_t>(a.dst, i * a.nb + b, j + 1, k, l));
     }
 }
 
@@ -299,8 +299,16 @@ hc_status launch_bconv_fused(hc_context ctx, const KView& src, const KView& dst,
         cudaError_t e = cudaFuncSetAttribute(bconv_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return cuda_check(e, "bconv smem attribute");
     }
-    if (ns > 65535) return fail(HC_ERR_UNSUPPORTED, "base conversion: batch too large");
-    dim3 grid((unsigned)((a.npos + BCONV_THREADS - 1) / BCONV_THREADS), (unsigned)ns);
+    if (ns * nb > 65535) return fail(HC_ERR_UNSUPPORTED, "base conversion: batch too large");
+    // split the outputs over CTAs while the grid is below about two waves of 8 CTAs per SM
+    // (each split recomputes the block's lifts and correction, a small part of the work)
+    const int64_t cols = (a.npos + BCONV_THREADS - 1) / BCONV_THREADS, base_ctas = cols * ns * nb;
+    const int64_t target = (int64_t)num_sms(ctx) * 16;
+    int splits = (int)std::min<int64_t>((target + base_ctas - 1) / base_ctas, (rd + 1) / 2);
+    splits = std::max(splits, 1);
+    a.ochunk = 2 * ((rd + 2 * splits - 1) / (2 * splits));
+    splits = (rd + a.ochunk - 1) / a.ochunk;
+    dim3 grid((unsigned)cols, (unsigned)(ns * nb), (unsigned)splits);
     bconv_fused_kernel<<<grid, BCONV_THREADS, smem, stream_of(ctx)>>>(a, sm, dm);
     count_launch(ctx);
     return cuda_check(cudaGetLastError(), "bconv kernel launch");
