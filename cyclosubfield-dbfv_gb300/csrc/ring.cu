@@ -2002,17 +2002,22 @@ struct hc_keyset_s {
 namespace {
 
 /// bfv_hom_gal (src/bfv.rs:783-841) with the keys of a keyset and one output view per automorphism.
+/// bfv_hom_gal (src/bfv.rs:783-841) of B ciphertexts at once (ct [2B, r], rows 2i, 2i + 1; each
+/// out [2B, r]) under the automorphisms gs with keys from a keyset: one gadget decomposition of all
+/// B ciphertexts, hoisted over gs, and one key-switch launch per automorphism for the whole batch.
 void hom_gal_keyset(hc_ring R, const hc_view& ct, const Base& b, const std::vector<uint64_t>& gs, hc_keyset ks,
                     const std::vector<hc_view>& outs) {
     if (gs.empty()) return;
-    const int64_t rr = (int64_t)b.size();
+    const int64_t rr = (int64_t)b.size(), B = ct.shape[0] / 2;
+    REQUIRE(B >= 1 && ct.shape[0] == 2 * B, HC_ERR_SHAPE, "ciphertexts must have 2 rows each");
+    for (auto& o : outs) REQUIRE(o.shape[0] == 2 * B, HC_ERR_SHAPE, "one output row pair per ciphertext");
     Digits dg = clip(ks->digits, b.size());
     REQUIRE(ks->r_key >= b.size(), HC_ERR_SHAPE, "keyset keys cover fewer RNS factors than the ciphertext");
-    Tensor c1(R->ctx, 1, rr, R->dl(), R->dk());
-    CK(hc_assign(R->ctx, c1.view(), vrows(ct, 1, 2)));
+    Tensor c1(R->ctx, B, rr, R->dl(), R->dk());
+    CK(hc_assign(R->ctx, c1.view(), vstep(ct, 1, 2, B)));
     R->transform(c1.view(), b, true);
     Tensor parts = gadget_decompose(R, c1.view(), b, dg);
-    hc_view c0 = vrows(ct, 0, 1);
+    hc_view c0 = vstep(ct, 0, 2, B);
     ks->each(gs, [&](size_t gi, const hc_view& key) {
         PermCache& pc = R->perms(gs[gi]);
         keyswitch(R, parts.view(), key, b, dg.size(), &c0, nullptr, outs[gi], pc.p2.as<uint32_t>(), pc.p3.as<uint32_t>());
@@ -2216,20 +2221,19 @@ hc_status hc_dbfv_hom_cyclic_transform(hc_ring R, size_t log2_b, size_t log2_t, 
             for (size_t j = 1; j < baby; j++) baby_exps.push_back(pow_mod_m(g, j, m));
             // babys: block j (rows j 2d .. (j + 1) 2d) = sigma^j(ct)
             Tensor B(R->ctx, (int64_t)(baby * 2 * d), rr, dl, dk, false, false);
-            if (d > 0) CK(hc_assign(R->ctx, vrows(B.view(), 0, 2 * (int64_t)d), ct));
-            for (size_t di = 0; di < d; di++) {
+            if (d > 0) {
+                // all d digits in one hoisted batch: block j holds sigma^j of every digit
+                CK(hc_assign(R->ctx, vrows(B.view(), 0, 2 * (int64_t)d), ct));
                 std::vector<hc_view> outs;
                 for (size_t j = 1; j < baby; j++)
-                    outs.push_back(vrows(B.view(), (int64_t)(j * 2 * d + 2 * di), (int64_t)(j * 2 * d + 2 * di + 2)));
-                hom_gal_keyset(R, vrows(B.view(), 2 * (int64_t)di, 2 * (int64_t)di + 2), b, baby_exps, ks, outs);
+                    outs.push_back(vrows(B.view(), (int64_t)(j * 2 * d), (int64_t)((j + 1) * 2 * d)));
+                hom_gal_keyset(R, vrows(B.view(), 0, 2 * (int64_t)d), b, baby_exps, ks, outs);
             }
             const uint64_t giant_exp = pow_mod_m(g, baby, m);
             for (size_t giant = giant_steps; giant-- > 0;) {
                 if (giant != giant_steps - 1 && od > 0) {
                     Tensor rot(R->ctx, 2 * (int64_t)od, rr, dl, dk, false, false);
-                    for (size_t di = 0; di < od; di++)
-                        hom_gal_keyset(R, vrows(O.view(), 2 * (int64_t)di, 2 * (int64_t)di + 2), b, {giant_exp}, ks,
-                                       {vrows(rot.view(), 2 * (int64_t)di, 2 * (int64_t)di + 2)});
+                    hom_gal_keyset(R, O.view(), b, {giant_exp}, ks, {rot.view()});  // all od digits at once
                     O = std::move(rot);
                 }
                 const size_t nterm = std::min(baby, len - giant * baby);
