@@ -32,7 +32,8 @@ hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys
                            const int64_t* one_dev, const uint32_t* p2, const uint32_t* p3);
 hc_status launch_tensor(hc_context ctx, const KView& d, const KView& lhs, const KView& rhs, const KMods& m, int f0,
                         int f1, int f2);
-hc_status launch_giant(hc_context ctx, const KView* lhs, const KView* rhs, int nterms, const KView* add, int full,
+hc_status launch_giant(hc_context ctx, const KView& babies, const KView& lcoef, int nbaby, int d, const int* lfirst,
+                       const int* lcount, const KView* add, int nadd, const unsigned char* full, int used,
                        const KView& dst, const KMods& m, const int64_t* one_dev);
 }  // namespace hc
 
@@ -2251,26 +2252,23 @@ hc_status hc_dbfv_hom_cyclic_transform(hc_ring R, size_t log2_b, size_t log2_t, 
                 const int64_t minp = R->min_p(b);
                 const KMods km = R->kmods(b);
                 const int64_t* one = R->one_dev(b);
-                for (size_t k = 0; k < used; k++) {
-                    std::vector<KView> lhs, rhs;
-                    for (size_t j = 0; j < nterm && k < max_new; j++) {
-                        const size_t ci = giant * baby + j, nr = bd[ci].size();
-                        if (d == 0 || nr == 0 || k >= std::min(digits, d + nr - 1)) continue;
-                        for (size_t jj = 0; jj < nr && jj <= k; jj++) {
-                            const size_t i = k - jj;
-                            if (i >= d) continue;
-                            lhs.push_back(kv(vrows(B.view(), (int64_t)(j * 2 * d + 2 * i), (int64_t)(j * 2 * d + 2 * i + 2))));
-                            rhs.push_back(kv(ltensor(ci, jj)));
-                        }
-                    }
-                    REQUIRE(lhs.size() <= HC_MAX_TERMS, HC_ERR_UNSUPPORTED, "too many inner-product terms per digit");
-                    const bool has_add = k < od;
-                    const u128 bound = (u128)lhs.size() * mp2 + (has_add ? mp2 : 0);
-                    KView addv = has_add ? kv(vrows(O.view(), 2 * (int64_t)k, 2 * (int64_t)k + 2)) : KView();
-                    CK(launch_giant(R->ctx, lhs.data(), rhs.data(), (int)lhs.size(), has_add ? &addv : nullptr,
-                                    needs_full(bound, minp), kv(vrows(n.view(), 2 * (int64_t)k, 2 * (int64_t)k + 2)), km,
-                                    one));
+                std::vector<int> lf(nterm, 0), lc(nterm, 0);
+                for (size_t j = 0; j < nterm; j++) {
+                    lf[j] = (int)first[giant * baby + j];
+                    lc[j] = (int)bd[giant * baby + j].size();
                 }
+                std::vector<unsigned char> fullv(used);
+                for (size_t k = 0; k < used; k++) {
+                    size_t cnt = 0;  // the inner product's terms for output digit k
+                    for (size_t j = 0; j < nterm && d > 0; j++)
+                        for (size_t jj = 0; jj < (size_t)lc[j] && jj <= k; jj++)
+                            if (k - jj < d) cnt++;
+                    fullv[k] = needs_full((u128)cnt * mp2 + (k < od ? mp2 : 0), minp);
+                }
+                KView addv = od > 0 ? kv(O.view()) : KView();
+                CK(launch_giant(R->ctx, kv(B.view()), nt > 0 ? kv(L.view()) : KView(), d > 0 ? (int)nterm : 0, (int)d,
+                                lf.data(), lc.data(), od > 0 ? &addv : nullptr, (int)od, fullv.data(), (int)used,
+                                kv(n.view()), km, one));
                 O = std::move(n);
                 od = used;
             }

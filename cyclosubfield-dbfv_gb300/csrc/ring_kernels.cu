@@ -9,8 +9,8 @@
 //  - keyswitch_kernel: the key-switch inner product, the addition of c0 / c1 through mont(1)
 //    and reduce_wide (src/bfv.rs:498-556, src/ring.rs:460-485, :503-509, :846-865).
 //  - tensor_kernel: hom_mul_raw_acc + reduce_wide (src/bfv.rs:667-683).
-//  - giant_kernel: one giant step of the homomorphic CRT transform for one output digit: the
-//    baby-step inner product over the digit convolution (dbfv_acc_inner_product_element_lprime,
+//  - giant_kernel: one giant step of the homomorphic CRT transform for up to four output digits:
+//    the baby-step inner product over the digit convolution (dbfv_acc_inner_product_element_lprime,
 //    src/dbfv.rs:291-399), the addition of the carried result (dbfv_acc_add, :153-163) and the
 //    reduction (dbfv_finish_accumulator, :401-404), without the wide accumulator in HBM.
 #include <algorithm>
@@ -238,14 +238,24 @@ __global__ void __launch_bounds__(256) tensor_kernel(KView d, KView lhs, KView r
     }
 }
 
+/// One giant step of the homomorphic CRT transform: output digit o (rows 2o, 2o + 1 of dst) is
+/// sum over the baby steps j and input digits i of baby(j, i) * L(coef_j, o - i), plus the carried
+/// digit o through mont(1), reduced. Each thread holds the accumulators of up to GIANT_OUT output
+/// digits, so every baby-step digit is read once for all the outputs it feeds.
+constexpr int GIANT_OUT = 4;
+constexpr int GIANT_MAX_BABY = 256;
+
 struct GiantArgs {
-    KView lhs[HC_MAX_TERMS];  // [2, r, dl, dk]: c0 / c1 rows of one digit of a baby step
-    KView rhs[HC_MAX_TERMS];  // [1, r, dl, 1]: one balanced digit of an L' coefficient (CRT basis)
-    int nterms;
-    KView add;                // [2, r, dl, dk]: the carried digit, through mont(1) (has_add)
-    int has_add;
-    int full;                 // the rows need the full double reduction
-    KView dst;                // [2, r, dl, dk]
+    KView babies;   // [nbaby * 2d, r, dl, dk]: block j holds sigma^j of the d input digits (rows 2i, 2i + 1)
+    KView lcoef;    // [nt, r, dl, 1]: balanced digits of the L' coefficients (CRT basis), broadcast on dim 3
+    int nbaby, d;
+    short lfirst[GIANT_MAX_BABY];  // row in lcoef of digit 0 of baby j's coefficient
+    short lcount[GIANT_MAX_BABY];  // its digit count
+    int out0, nout;                // output digits [out0, out0 + nout) of this launch (nout <= GIANT_OUT)
+    KView add;                     // the carried digits [2 nadd, ...] (through mont(1))
+    int nadd;
+    unsigned full;                 // bit o - out0: output digit o needs the full double reduction
+    KView dst;                     // [2 used, ...]
 };
 
 __global__ void __launch_bounds__(256) giant_kernel(GiantArgs a, KMods m, const int64_t* one, int64_t lines,
@@ -256,19 +266,40 @@ __global__ void __launch_bounds__(256) giant_kernel(GiantArgs a, KMods m, const 
         int64_t l = (tile - line * chunks) * blockDim.x + threadIdx.x;
         if (l >= a.dst.n3) continue;
         int64_t k = line % a.dst.n2, j = line / a.dst.n2;
-        i128 acc0 = 0, acc1 = 0;
-        for (int t = 0; t < a.nterms; t++) {
-            const int64_t f = *kat<int64_t>(a.rhs[t], 0, j, k, 0);
-            acc0 = (i128)((u128)acc0 + (u128)((i128)*kat<int64_t>(a.lhs[t], 0, j, k, l) * (i128)f));
-            acc1 = (i128)((u128)acc1 + (u128)((i128)*kat<int64_t>(a.lhs[t], 1, j, k, l) * (i128)f));
+        i128 acc0[GIANT_OUT], acc1[GIANT_OUT];
+#pragma unroll
+        for (int o = 0; o < GIANT_OUT; o++) acc0[o] = acc1[o] = 0;
+        for (int bj = 0; bj < a.nbaby; bj++) {
+            const int lf = a.lfirst[bj], lc = a.lcount[bj];
+            for (int i = 0; i < a.d; i++) {
+                // input digit i feeds output digits i + jj, jj < lc; skip it when none is in range
+                if (i + lc <= a.out0 || i >= a.out0 + a.nout) continue;
+                const int64_t row = (int64_t)bj * 2 * a.d + 2 * i;
+                const int64_t x0 = *kat<int64_t>(a.babies, row, j, k, l), x1 = *kat<int64_t>(a.babies, row + 1, j, k, l);
+#pragma unroll
+                for (int o = 0; o < GIANT_OUT; o++) {
+                    const int jj = a.out0 + o - i;
+                    if (o < a.nout && jj >= 0 && jj < lc) {
+                        const int64_t f = *kat<int64_t>(a.lcoef, lf + jj, j, k, 0);
+                        acc0[o] = (i128)((u128)acc0[o] + (u128)((i128)x0 * (i128)f));
+                        acc1[o] = (i128)((u128)acc1[o] + (u128)((i128)x1 * (i128)f));
+                    }
+                }
+            }
         }
-        if (a.has_add) {
-            const int64_t o = one[j];
-            acc0 = (i128)((u128)acc0 + (u128)((i128)*kat<int64_t>(a.add, 0, j, k, l) * (i128)o));
-            acc1 = (i128)((u128)acc1 + (u128)((i128)*kat<int64_t>(a.add, 1, j, k, l) * (i128)o));
+#pragma unroll
+        for (int o = 0; o < GIANT_OUT; o++) {
+            if (o >= a.nout) break;
+            const int od = a.out0 + o;
+            if (od < a.nadd) {
+                const int64_t on = one[j];
+                acc0[o] = (i128)((u128)acc0[o] + (u128)((i128)*kat<int64_t>(a.add, 2 * od, j, k, l) * (i128)on));
+                acc1[o] = (i128)((u128)acc1[o] + (u128)((i128)*kat<int64_t>(a.add, 2 * od + 1, j, k, l) * (i128)on));
+            }
+            const bool full = (a.full >> o) & 1;
+            *kat<int64_t>(a.dst, 2 * od, j, k, l) = finish_wide(acc0[o], full, m, (int)j);
+            *kat<int64_t>(a.dst, 2 * od + 1, j, k, l) = finish_wide(acc1[o], full, m, (int)j);
         }
-        *kat<int64_t>(a.dst, 0, j, k, l) = finish_wide(acc0, a.full, m, (int)j);
-        *kat<int64_t>(a.dst, 1, j, k, l) = finish_wide(acc1, a.full, m, (int)j);
     }
 }
 
@@ -350,28 +381,38 @@ hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys
     return cuda_check(cudaGetLastError(), "keyswitch kernel launch");
 }
 
-hc_status launch_giant(hc_context ctx, const KView* lhs, const KView* rhs, int nterms, const KView* add, int full,
+hc_status launch_giant(hc_context ctx, const KView& babies, const KView& lcoef, int nbaby, int d, const int* lfirst,
+                       const int* lcount, const KView* add, int nadd, const unsigned char* full, int used,
                        const KView& dst, const KMods& m, const int64_t* one_dev) {
-    if (nterms > HC_MAX_TERMS) return fail(HC_ERR_UNSUPPORTED, "too many inner-product terms per digit");
-    GiantArgs a;
-    for (int t = 0; t < nterms; t++) {
-        a.lhs[t] = lhs[t];
-        a.rhs[t] = rhs[t];
-        a.rhs[t].b3 = 1;  // broadcast along dimension 3
-    }
-    a.nterms = nterms;
-    a.has_add = add != nullptr;
-    if (add) a.add = *add;
-    a.full = full;
-    a.dst = dst;
+    if (nbaby > GIANT_MAX_BABY) return fail(HC_ERR_UNSUPPORTED, "too many baby steps");
     int64_t lines = dst.n1 * dst.n2;
-    if (lines == 0 || dst.n3 == 0) return HC_OK;
+    if (lines == 0 || dst.n3 == 0 || used == 0) return HC_OK;
+    GiantArgs a;
+    a.babies = babies;
+    a.lcoef = lcoef;
+    a.lcoef.b3 = 1;  // broadcast along dimension 3
+    a.nbaby = nbaby, a.d = d;
+    for (int j = 0; j < nbaby; j++) {
+        if (lfirst[j] > 32767 || lcount[j] > 32767) return fail(HC_ERR_UNSUPPORTED, "too many coefficient digits");
+        a.lfirst[j] = (short)lfirst[j], a.lcount[j] = (short)lcount[j];
+    }
+    a.nadd = add ? nadd : 0;
+    if (add) a.add = *add;
+    a.dst = dst;
     int chunks;
     unsigned blocks;
     grid_lines(ctx, dst.n3, lines, &chunks, &blocks);
-    giant_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(a, m, one_dev, lines, chunks);
-    count_launch(ctx);
-    return cuda_check(cudaGetLastError(), "giant-step kernel launch");
+    for (int o0 = 0; o0 < used; o0 += GIANT_OUT) {
+        a.out0 = o0;
+        a.nout = std::min(GIANT_OUT, used - o0);
+        a.full = 0;
+        for (int o = 0; o < a.nout; o++) a.full |= (unsigned)(full[o0 + o] != 0) << o;
+        giant_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(a, m, one_dev, lines, chunks);
+        count_launch(ctx);
+        hc_status st = cuda_check(cudaGetLastError(), "giant-step kernel launch");
+        if (st) return st;
+    }
+    return HC_OK;
 }
 
 hc_status launch_tensor(hc_context ctx, const KView& d, const KView& lhs, const KView& rhs, const KMods& m, int f0,
