@@ -46,7 +46,8 @@ int device_of(hc_context ctx) { return ctx->device; }
 hc_status build_plan(hc_context ctx, const hc_modulus* m, const size_t* shape, size_t k, hc_ntt_plan* out);
 hc_status destroy_plan(hc_ntt_plan p);
 hc_status launch_ntt(hc_context ctx, const KView& t, const hc_ntt_plan* plans, size_t nplans, int dim, int mode,
-                     const KView& mul, const KMods& mods);
+                     const KView& mul, const KMods& mods, const KView* src = nullptr);
+bool ntt_column_path(const hc_ntt_plan* plans, size_t nplans, int dim);
 hc_status launch_pointwise(hc_context ctx, int op, const KView& d, const KView& a, const KView& b, const KMods& m);
 hc_status launch_matmul(hc_context ctx, const KView& d, const KView& lhs, const KView& rhs, int64_t U);
 hc_status launch_inner_product(hc_context ctx, const KView& d, const KView* l, const KView* r, int n);
@@ -417,6 +418,27 @@ namespace hc {
 hc_status intt_mul_mont64_dim(hc_context ctx, hc_view dst, const hc_ntt_plan* plans, size_t nplans, hc_data_dim dim,
                               hc_view mul, const hc_modulus* mods, size_t nmods) {
     return ntt_call(ctx, dst, plans, nplans, dim, 3, &mul, mods, nmods);
+}
+
+/// hc_assign(dst, src) followed by hc_ntt_mul_mont64_dim on dst, with the copy folded into the
+/// transform's reads where the column kernel runs the call; used by the ring layer.
+hc_status ntt_mul_mont64_dim_from(hc_context ctx, hc_view dst, hc_view src, const hc_ntt_plan* plans, size_t nplans,
+                                  hc_data_dim dim, hc_view mul, const hc_modulus* mods, size_t nmods) {
+    hc_status st;
+    if (!ctx) return fail(HC_ERR_ARG, "null context");
+    if (nplans && !plans) return fail(HC_ERR_ARG, "null plans");
+    if (!ntt_column_path(plans, nplans, (int)dim)) {
+        if ((st = hc_assign(ctx, dst, src))) return st;
+        return ntt_call(ctx, dst, plans, nplans, dim, 2, &mul, mods, nmods);
+    }
+    if ((st = check_view(dst, "dst")) || (st = check_view(src, "src"))) return st;
+    for (int d = 0; d < 4; d++)
+        if (src.shape[d] != dst.shape[d]) return fail(HC_ERR_SHAPE, "source and destination shapes differ");
+    KView t = kview(dst), s = kview(src), m = t;
+    KMods km;
+    if ((st = bview(mul, dst.shape, "mul", &m))) return st;
+    if ((st = kmods(mods, nmods, dst.shape[1], &km))) return st;
+    return launch_ntt(ctx, t, plans, nplans, (int)dim, 2, m, km, &s);
 }
 }  // namespace hc
 

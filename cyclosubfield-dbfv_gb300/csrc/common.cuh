@@ -202,5 +202,7 @@ size_t max_smem_optin(hc_context ctx);
 int device_of(hc_context ctx);
 hc_status intt_mul_mont64_dim(hc_context ctx, hc_view dst, const hc_ntt_plan* plans, size_t nplans, hc_data_dim dim,
                               hc_view mul, const hc_modulus* mods, size_t nmods);
+hc_status ntt_mul_mont64_dim_from(hc_context ctx, hc_view dst, hc_view src, const hc_ntt_plan* plans, size_t nplans,
+                                  hc_data_dim dim, hc_view mul, const hc_modulus* mods, size_t nmods);
 
 }  // namespace hc

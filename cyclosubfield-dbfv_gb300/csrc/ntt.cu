@@ -613,9 +613,12 @@ __global__ void __cluster_dims__(3, 1, 1) __launch_bounds__(128, 5)
 }
 
 /// One specialised column (global element stride ge) of shape SHAPE, in registers.
+/// One column g[0], g[ge], ... transformed in registers; it is read from gs[0], gs[gse], ... (g
+/// itself for an in-place call).
 template <int SHAPE, int MODE, bool FIX>
 __device__ __forceinline__ void run_column(const DevPlanHeader* P, const fast::Ctx& c, int64_t* g, int64_t ge,
-                                           const int64_t* mulp, int64_t mstride, int64_t mn, int64_t mi) {
+                                           const int64_t* gs, int64_t gse, const int64_t* mulp, int64_t mstride,
+                                           int64_t mn, int64_t mi) {
     constexpr bool inv = MODE & 1;
     const DevStage* st = inv ? P->inv : P->fwd;
     constexpr int NST = SHAPE == HC_SHAPE_C12 ? 3 : 2;
@@ -634,7 +637,7 @@ __device__ __forceinline__ void run_column(const DevPlanHeader* P, const fast::C
 #pragma unroll
         for (int a = 0; a < 4; a++)
 #pragma unroll
-            for (int b = 0; b < 3; b++) x[a][b] = g[(3 * a + b) * ge];
+            for (int b = 0; b < 3; b++) x[a][b] = gs[(3 * a + b) * gse];
         fast::col12(c, f, inv, MODE == 0, x);
 #pragma unroll
         for (int a = 0; a < 4; a++)
@@ -647,7 +650,7 @@ __device__ __forceinline__ void run_column(const DevPlanHeader* P, const fast::C
     } else {
         int64_t x[4];
 #pragma unroll
-        for (int a = 0; a < 4; a++) x[a] = g[a * ge];
+        for (int a = 0; a < 4; a++) x[a] = gs[a * gse];
         fast::col4(c, f, inv, MODE == 0, x);
 #pragma unroll
         for (int a = 0; a < 4; a++) {
@@ -667,7 +670,7 @@ __device__ __forceinline__ void run_column(const DevPlanHeader* P, const fast::C
 /// Specialised dimension-2 NTT: one thread per column (i, j, l), CTAs over (i, j, column block).
 template <int SHAPE, int MODE, bool FIX>
 __global__ void __launch_bounds__(HC_COL_THREADS, SHAPE == HC_SHAPE_C12 ? HC_COL12_MIN_BLOCKS : 4) ntt_col_kernel(KView t, PlanPtrs plans, KView mul, KMods mods,
-                                                                    int ncb) {
+                                                                    int ncb, KView src) {
     __shared__ __align__(16) int64_t tws[HC_COL_TW];
     const int64_t tile = blockIdx.x;
     const int64_t cb = tile % ncb, r = tile / ncb;
@@ -686,13 +689,15 @@ __global__ void __launch_bounds__(HC_COL_THREADS, SHAPE == HC_SHAPE_C12 ? HC_COL
         ms = mul.s2;
         mn = mods.n[j], mi = mods.ninv[j];
     }
-    run_column<SHAPE, MODE, FIX>(P, c, g, t.s2, mulp, ms, mn, mi);
+    // out of place (src.p set): the column is read from src, written to t
+    const int64_t* gs = src.p ? reinterpret_cast<const int64_t*>(src.p) + i * src.s0 + j * src.s1 + l : g;
+    run_column<SHAPE, MODE, FIX>(P, c, g, t.s2, gs, src.p ? src.s2 : t.s2, mulp, ms, mn, mi);
 }
 
 /// Host: launches the specialised kernel of (shape, mode, fixed schedule).
 template <int SHAPE, int MODE, bool FIX>
 hc_status launch_special(hc_context ctx, const KView& t, const PlanPtrs& pp, const KView& mul, const KMods& mods,
-                         size_t smem, int64_t tiles, int ncb) {
+                         size_t smem, int64_t tiles, int ncb, const KView& src) {
     if constexpr (SHAPE == HC_SHAPE_L12288) {
         // one 3-CTA cluster per line: padded 4096-residue block + twiddles per CTA
         const size_t smem3 = smem - ((size_t)line_tile_words(SHAPE) - 4608) * 8;
@@ -708,7 +713,8 @@ hc_status launch_special(hc_context ctx, const KView& t, const PlanPtrs& pp, con
         if (e != cudaSuccess) return hc::cuda_check(e, "ntt smem attribute");
         kern<<<(unsigned)tiles, TH, smem, hc::stream_of(ctx)>>>(t, pp, mul, mods);
     } else {
-        ntt_col_kernel<SHAPE, MODE, FIX><<<(unsigned)tiles, HC_COL_THREADS, 0, hc::stream_of(ctx)>>>(t, pp, mul, mods, ncb);
+        ntt_col_kernel<SHAPE, MODE, FIX><<<(unsigned)tiles, HC_COL_THREADS, 0, hc::stream_of(ctx)>>>(t, pp, mul, mods, ncb,
+                                                                                                   src);
     }
     hc::count_launch(ctx);
     return hc::cuda_check(cudaGetLastError(), "ntt kernel launch");
@@ -716,17 +722,17 @@ hc_status launch_special(hc_context ctx, const KView& t, const PlanPtrs& pp, con
 
 template <int SHAPE>
 hc_status launch_special_mode(hc_context ctx, int mode, bool fix, const KView& t, const PlanPtrs& pp, const KView& mul,
-                              const KMods& mods, size_t smem, int64_t tiles, int ncb) {
+                              const KMods& mods, size_t smem, int64_t tiles, int ncb, const KView& src = KView()) {
     if (fix) {
-        if (mode == 0) return launch_special<SHAPE, 0, true>(ctx, t, pp, mul, mods, smem, tiles, ncb);
-        if (mode == 1) return launch_special<SHAPE, 1, true>(ctx, t, pp, mul, mods, smem, tiles, ncb);
-        if (mode == 2) return launch_special<SHAPE, 2, true>(ctx, t, pp, mul, mods, smem, tiles, ncb);
-        return launch_special<SHAPE, 3, true>(ctx, t, pp, mul, mods, smem, tiles, ncb);
+        if (mode == 0) return launch_special<SHAPE, 0, true>(ctx, t, pp, mul, mods, smem, tiles, ncb, src);
+        if (mode == 1) return launch_special<SHAPE, 1, true>(ctx, t, pp, mul, mods, smem, tiles, ncb, src);
+        if (mode == 2) return launch_special<SHAPE, 2, true>(ctx, t, pp, mul, mods, smem, tiles, ncb, src);
+        return launch_special<SHAPE, 3, true>(ctx, t, pp, mul, mods, smem, tiles, ncb, src);
     }
-    if (mode == 0) return launch_special<SHAPE, 0, false>(ctx, t, pp, mul, mods, smem, tiles, ncb);
-    if (mode == 1) return launch_special<SHAPE, 1, false>(ctx, t, pp, mul, mods, smem, tiles, ncb);
-    if (mode == 2) return launch_special<SHAPE, 2, false>(ctx, t, pp, mul, mods, smem, tiles, ncb);
-    return launch_special<SHAPE, 3, false>(ctx, t, pp, mul, mods, smem, tiles, ncb);
+    if (mode == 0) return launch_special<SHAPE, 0, false>(ctx, t, pp, mul, mods, smem, tiles, ncb, src);
+    if (mode == 1) return launch_special<SHAPE, 1, false>(ctx, t, pp, mul, mods, smem, tiles, ncb, src);
+    if (mode == 2) return launch_special<SHAPE, 2, false>(ctx, t, pp, mul, mods, smem, tiles, ncb, src);
+    return launch_special<SHAPE, 3, false>(ctx, t, pp, mul, mods, smem, tiles, ncb, src);
 }
 
 /// mode 0: forward (reduced), 1: inverse, 2: forward unreduced + Montgomery multiplication by `mul`.
@@ -800,11 +806,15 @@ __device__ __forceinline__ void slab_pass(const CrtSlab& S, const DevPlanHeader*
         const fast::Ctx c = make_ctx(P, tw);
         for (int l = threadIdx.x; l < S.dk; l += blockDim.x) {
             if (shape == HC_SHAPE_C12) {
-                if (mode == 2) run_column<HC_SHAPE_C12, 2, true>(P, c, S.data + l, S.s2, mulrow, 1, S.n, S.ninv);
-                else run_column<HC_SHAPE_C12, 1, true>(P, c, S.data + l, S.s2, mulrow, 1, S.n, S.ninv);
+                if (mode == 2) run_column<HC_SHAPE_C12, 2, true>(P, c, S.data + l, S.s2, S.data + l, S.s2, mulrow, 1, S.n,
+                                                             S.ninv);
+                else run_column<HC_SHAPE_C12, 1, true>(P, c, S.data + l, S.s2, S.data + l, S.s2, mulrow, 1, S.n,
+                                                             S.ninv);
             } else {
-                if (mode == 2) run_column<HC_SHAPE_C4, 2, true>(P, c, S.data + l, S.s2, mulrow, 1, S.n, S.ninv);
-                else run_column<HC_SHAPE_C4, 1, true>(P, c, S.data + l, S.s2, mulrow, 1, S.n, S.ninv);
+                if (mode == 2) run_column<HC_SHAPE_C4, 2, true>(P, c, S.data + l, S.s2, S.data + l, S.s2, mulrow, 1, S.n,
+                                                             S.ninv);
+                else run_column<HC_SHAPE_C4, 1, true>(P, c, S.data + l, S.s2, S.data + l, S.s2, mulrow, 1, S.n,
+                                                             S.ninv);
             }
         }
         __syncthreads();
@@ -1138,8 +1148,22 @@ hc_status launch_crt_batch(hc_context ctx, const CrtSlab* slabs, int nslabs, int
 }
 
 /// Launches the tile kernel for one HAL NTT call (mode 0 ntt, 1 intt, 2 ntt_mul).
+/// Whether launch_ntt runs a call on the specialised column kernel, the one form that can read a
+/// separate source (launch_ntt's `src`).
+bool ntt_column_path(const hc_ntt_plan* plans, size_t nplans, int dim) {
+    if (dim != 2 || nplans == 0 || !plans[0]) return false;
+    const int shape = plans[0]->shape;
+    int32_t max_tw = 0;
+    for (size_t j = 0; j < nplans; j++) {
+        if (!plans[j] || plans[j]->shape != shape) return false;
+        max_tw = std::max(max_tw, plans[j]->ntw);
+    }
+    return (shape == HC_SHAPE_C12 || shape == HC_SHAPE_C4) && 2 * max_tw <= HC_COL_TW;
+}
+
 hc_status launch_ntt(hc_context ctx, const KView& t, const hc_ntt_plan* plans, size_t nplans, int dim, int mode,
-                     const KView& mul, const KMods& mods) {
+                     const KView& mul, const KMods& mods, const KView* src) {
+    if (src && !ntt_column_path(plans, nplans, dim)) return fail(HC_ERR_UNSUPPORTED, "out-of-place NTT form");
     if ((int64_t)nplans != t.n1) return fail(HC_ERR_SHAPE, "one NTT plan per RNS row required");
     if (nplans > HC_MAX_MODS) return fail(HC_ERR_UNSUPPORTED, "too many RNS rows in one call");
     const int64_t len = dim == 3 ? t.n3 : t.n2;
@@ -1171,10 +1195,13 @@ hc_status launch_ntt(hc_context ctx, const KView& t, const hc_ntt_plan* plans, s
         const int64_t tiles = t.n0 * t.n1 * ncb;
         if (tiles <= 0x7fffffff) {
             if (shape == HC_SHAPE_C12)
-                return launch_special_mode<HC_SHAPE_C12>(ctx, mode, fix, t, pp, mul, mods, 0, tiles, (int)ncb);
-            return launch_special_mode<HC_SHAPE_C4>(ctx, mode, fix, t, pp, mul, mods, 0, tiles, (int)ncb);
+                return launch_special_mode<HC_SHAPE_C12>(ctx, mode, fix, t, pp, mul, mods, 0, tiles, (int)ncb,
+                                                         src ? *src : KView());
+            return launch_special_mode<HC_SHAPE_C4>(ctx, mode, fix, t, pp, mul, mods, 0, tiles, (int)ncb,
+                                                    src ? *src : KView());
         }
     }
+    if (src) return fail(HC_ERR_UNSUPPORTED, "out-of-place NTT form");
     int V = 1, logv = 0;
     int64_t ntile2 = 1;
     if (dim == 2) {

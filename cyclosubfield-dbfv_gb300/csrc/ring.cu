@@ -710,14 +710,20 @@ struct hc_ring_s {
 
     // ---------------------------------------------------------------- transforms
     /// pb_to_crt / crt_to_pb (src/ring.rs:1118-1161); `post_mul`: a Montgomery product applied to
-    /// the result in the epilogue of the last pass (the caller's next hal_mul_mont64, fused)
-    void transform(const hc_view& v, const Base& b, bool inverse, const hc_view* post_mul = nullptr) {
+    /// the result in the epilogue of the last pass (the caller's next hal_mul_mont64, fused);
+    /// `src`: transform a copy of src into v (the caller's hal_assign, folded into the first pass)
+    void transform(const hc_view& v, const Base& b, bool inverse, const hc_view* post_mul = nullptr,
+                   const hc_view* src = nullptr) {
         REQUIRE(v.shape[1] == (int64_t)b.size() && v.shape[2] == dl() && v.shape[3] == dk(), HC_ERR_SHAPE,
                 "transform: tensor shape does not match the ring and base");
         TransformCache& c = transform_cache(b);
         const size_t r = b.size();
-        CK(hc_ntt_mul_mont64_dim(ctx, v, c.plp.data(), r, HC_DIM2, inverse ? c.ikl.view() : c.kl.view(),
-                                 c.mods.data(), r));
+        if (src)
+            CK(ntt_mul_mont64_dim_from(ctx, v, *src, c.plp.data(), r, HC_DIM2, inverse ? c.ikl.view() : c.kl.view(),
+                                       c.mods.data(), r));
+        else
+            CK(hc_ntt_mul_mont64_dim(ctx, v, c.plp.data(), r, HC_DIM2, inverse ? c.ikl.view() : c.kl.view(),
+                                     c.mods.data(), r));
         CK(hc_ntt_mul_mont64_dim(ctx, v, c.pk.data(), r, HC_DIM3, inverse ? c.ikk.view() : c.kk.view(),
                                  c.mods.data(), r));
         CK(hc_intt_mont64_dim(ctx, v, c.plp.data(), r, HC_DIM2));
@@ -1520,8 +1526,7 @@ hc_status hc_bfv_hom_mul(hc_ring R, const int64_t t[2], hc_view ct1, hc_view ct2
         // lift both operands (src/bfv.rs:762-768)
         auto lift = [&](const hc_view& ct) {
             Tensor pb = temp(R->ctx, 2 * B, rr, R->dl(), R->dk());
-            CK(hc_assign(R->ctx, pb.view(), ct));
-            R->transform(pb.view(), b, true);
+            R->transform(pb.view(), b, true, nullptr, &ct);  // pb = crt_to_pb(ct)
             return lift_to_extended(R, pb.view(), &ct, b);
         };
         Tensor l = lift(ct1), rt = lift(ct2);
@@ -1572,8 +1577,8 @@ hc_status hc_bfv_hom_gal_batch(hc_ring R, hc_view ct, const size_t* base, size_t
         Digits dg = clip(digits_of(digits, d), r);
         REQUIRE(gk.shape[0] >= 2 * (int64_t)dg.size() && gk.shape[1] >= rr, HC_ERR_SHAPE, "Galois key tensor shape");
         Tensor c1(R->ctx, B, rr, R->dl(), R->dk());
-        CK(hc_assign(R->ctx, c1.view(), vstep(ct, 1, 2, B)));
-        R->transform(c1.view(), b, true);
+        const hc_view c1_crt = vstep(ct, 1, 2, B);
+        R->transform(c1.view(), b, true, nullptr, &c1_crt);
         Tensor parts = gadget_decompose(R, c1.view(), b, dg);
         hc_view c0 = vstep(ct, 0, 2, B);
         PermCache& pc = R->perms(g);
@@ -1595,8 +1600,8 @@ hc_status hc_bfv_hom_gal(hc_ring R, hc_view ct, const size_t* base, size_t r, co
         const int64_t per = 2 * (int64_t)d;
         REQUIRE(gks.shape[0] == per * (int64_t)ngs && gks.shape[1] >= rr, HC_ERR_SHAPE, "galois key tensor shape");
         Tensor c1(R->ctx, 1, rr, R->dl(), R->dk());
-        CK(hc_assign(R->ctx, c1.view(), vrows(ct, 1, 2)));
-        R->transform(c1.view(), b, true);
+        const hc_view c1_crt = vrows(ct, 1, 2);
+        R->transform(c1.view(), b, true, nullptr, &c1_crt);
         Tensor parts = gadget_decompose(R, c1.view(), b, dg);
         hc_view c0 = vrows(ct, 0, 1);
         for (size_t gi = 0; gi < ngs; gi++) {
@@ -2015,8 +2020,8 @@ void hom_gal_keyset(hc_ring R, const hc_view& ct, const Base& b, const std::vect
     Digits dg = clip(ks->digits, b.size());
     REQUIRE(ks->r_key >= b.size(), HC_ERR_SHAPE, "keyset keys cover fewer RNS factors than the ciphertext");
     Tensor c1(R->ctx, B, rr, R->dl(), R->dk());
-    CK(hc_assign(R->ctx, c1.view(), vstep(ct, 1, 2, B)));
-    R->transform(c1.view(), b, true);
+    const hc_view c1_crt = vstep(ct, 1, 2, B);
+    R->transform(c1.view(), b, true, nullptr, &c1_crt);
     Tensor parts = gadget_decompose(R, c1.view(), b, dg);
     hc_view c0 = vstep(ct, 0, 2, B);
     ks->each(gs, [&](size_t gi, const hc_view& key) {
