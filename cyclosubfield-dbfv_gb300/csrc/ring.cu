@@ -30,7 +30,8 @@ hc_status launch_galois(hc_context ctx, const KView& d, const KView& s, const ui
 hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys, int nterms, const KView* add0,
                            const KView* add1, int full0, int full1, const KView& dst, const KMods& m,
                            const int64_t* one_dev, const uint32_t* p2, const uint32_t* p3);
-hc_status launch_tensor(hc_context ctx, const KView& d, const KView& lhs, const KView& rhs, const KMods& m, int f0,
+hc_status launch_tensor(hc_context ctx, const KView& d, const KView& lhs_lo, const KView& lhs_hi, const KView& rhs_lo,
+                        const KView& rhs_hi, int rsplit, const KMods& m, int f0,
                         int f1, int f2);
 hc_status launch_giant(hc_context ctx, const KView& babies, const KView& lcoef, int nbaby, int d, const int* lfirst,
                        const int* lcount, const KView* add, int nadd, const unsigned char* full, int used,
@@ -1199,23 +1200,37 @@ void keyswitch(hc_ring R, const hc_view& parts, const hc_view& keys, const Base&
                         needs_full(b0, minp), needs_full(b1, minp), kv(out), R->kmods(base), R->one_dev(base), p2, p3));
 }
 
+/// The extension base of lift_to_extended (src/bfv.rs:564-598, src/ring.rs:716-731): extension
+/// primes until log2 Q + t_bits + 60 bits are covered.
+Base extension_of(hc_ring R, const Base& base) {
+    Base ext;
+    double need = (double)(product_bits([&] {
+                               std::vector<int64_t> ps;
+                               for (size_t i : base) ps.push_back(R->prime(i));
+                               return ps;
+                           }()) +
+                           R->t_bits + 60);
+    double bits = 0;
+    for (size_t i = R->initial_len; i < R->factors.size() && bits < need; i++) {
+        ext.push_back(i);
+        bits += std::log2((double)R->prime(i));
+    }
+    REQUIRE(bits >= need, HC_ERR_ARG, "extension pool too small for lifted multiplication over this base");
+    return ext;
+}
+
+/// The extension rows of lift_to_extended for a CRT-basis input whose period-basis form is pb:
+/// [count, |ext|] in CRT basis (the base rows would be the input itself).
+Tensor lift_extension_rows(hc_ring R, const hc_view& pb, const Base& base, const Base& ext) {
+    Tensor hi = temp(R->ctx, pb.shape[0], (int64_t)ext.size(), R->dl(), R->dk());
+    R->bconv(hi.view(), ext, pb, base);
+    R->transform(hi.view(), ext, false);
+    return hi;
+}
+
 Tensor lift_to_extended(hc_ring R, const hc_view& pb, const hc_view* crt, const Base& base) {
     const int64_t count = pb.shape[0], r = (int64_t)base.size();
-    Base ext;
-    {
-        double need = (double)(product_bits([&] {
-                                   std::vector<int64_t> ps;
-                                   for (size_t i : base) ps.push_back(R->prime(i));
-                                   return ps;
-                               }()) +
-                               R->t_bits + 60);
-        double bits = 0;
-        for (size_t i = R->initial_len; i < R->factors.size() && bits < need; i++) {
-            ext.push_back(i);
-            bits += std::log2((double)R->prime(i));
-        }
-        REQUIRE(bits >= need, HC_ERR_ARG, "extension pool too small for lifted multiplication over this base");
-    }
+    const Base ext = extension_of(R, base);
     Base lifted = base;
     lifted.insert(lifted.end(), ext.begin(), ext.end());
     Tensor res = temp(R->ctx, count, (int64_t)lifted.size(), R->dl(), R->dk());
@@ -1523,23 +1538,25 @@ hc_status hc_bfv_hom_mul(hc_ring R, const int64_t t[2], hc_view ct1, hc_view ct2
         check_view(ct1, 2 * B, rr, R->dl(), R->dk(), "ct1");
         check_view(ct2, 2 * B, rr, R->dl(), R->dk(), "ct2");
         check_view(out, 2 * B, rr, R->dl(), R->dk(), "output");
-        // lift both operands (src/bfv.rs:762-768)
+        // lift both operands (src/bfv.rs:762-768): the lifted tensors' base rows are the operands
+        // themselves, so only the extension rows are formed and the tensor product reads both parts
+        const Base ext = extension_of(R, b);
         auto lift = [&](const hc_view& ct) {
             Tensor pb = temp(R->ctx, 2 * B, rr, R->dl(), R->dk());
             R->transform(pb.view(), b, true, nullptr, &ct);  // pb = crt_to_pb(ct)
-            return lift_to_extended(R, pb.view(), &ct, b);
+            return lift_extension_rows(R, pb.view(), b, ext);
         };
-        Tensor l = lift(ct1), rt = lift(ct2);
+        Tensor lh = lift(ct1), rh = lift(ct2);
         Base lifted = b;
-        for (int64_t i = rr; i < l.shape[1]; i++) lifted.push_back(R->initial_len + (size_t)(i - rr));
+        lifted.insert(lifted.end(), ext.begin(), ext.end());
         // tensor product + reduce_wide (src/bfv.rs:667-683, :769-771); rows 2i, 2i + 1 hold
         // (c0, c1) of product i and row 2B + i its c2, so that both groups are contiguous
         Tensor prod = temp(R->ctx, 3 * B, (int64_t)lifted.size(), R->dl(), R->dk());
         {
             u128 mp = (u128)R->max_p(lifted), s1 = mp * mp;
             int64_t mn = R->min_p(lifted);
-            CK(launch_tensor(R->ctx, kv(prod.view()), kv(l.view()), kv(rt.view()), R->kmods(lifted), needs_full(s1, mn),
-                             needs_full(2 * s1, mn), needs_full(s1, mn)));
+            CK(launch_tensor(R->ctx, kv(prod.view()), kv(ct1), kv(lh.view()), kv(ct2), kv(rh.view()), (int)rr,
+                             R->kmods(lifted), needs_full(s1, mn), needs_full(2 * s1, mn), needs_full(s1, mn)));
         }
         const Tensor& tscale = R->scalar_tensor(lifted, words(t));
         const hc_view tsv = tscale.view();

@@ -216,9 +216,11 @@ __global__ void __launch_bounds__(256) keyswitch_kernel(KsArgs a, KMods m, const
 
 /// (l0 r0, l0 r1 + l1 r0, l1 r1) of B pairs of 2-row ciphertext tensors ([2B, ...] each),
 /// reduced per row into [3B, ...]: rows 2i and 2i + 1 receive the first two components of pair i,
-/// row 2B + i the third.
-__global__ void __launch_bounds__(256) tensor_kernel(KView d, KView lhs, KView rhs, KMods m, int full0, int full1,
-                                                     int full2, int64_t lines, int chunks) {
+/// row 2B + i the third. Each operand comes in two parts along the RNS dimension: rows j < rsplit
+/// from *_lo, rows j >= rsplit from *_hi (row j - rsplit).
+__global__ void __launch_bounds__(256) tensor_kernel(KView d, KView lhs_lo, KView lhs_hi, KView rhs_lo, KView rhs_hi,
+                                                     int rsplit, KMods m, int full0, int full1, int full2,
+                                                     int64_t lines, int chunks) {
     const int64_t tiles = lines * chunks;
     for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         int64_t line = tile / chunks;  // (i, j, k)
@@ -226,8 +228,13 @@ __global__ void __launch_bounds__(256) tensor_kernel(KView d, KView lhs, KView r
         if (l >= d.n3) continue;
         int64_t k = line % d.n2, r = line / d.n2;
         int64_t j = r % d.n1, i = r / d.n1;
-        int64_t l0 = *kat<int64_t>(lhs, 2 * i, j, k, l), l1 = *kat<int64_t>(lhs, 2 * i + 1, j, k, l);
-        int64_t r0 = *kat<int64_t>(rhs, 2 * i, j, k, l), r1 = *kat<int64_t>(rhs, 2 * i + 1, j, k, l);
+        const bool lo = j < rsplit;
+        const int64_t js = lo ? j : j - rsplit;
+        const int64_t* lp = lo ? kat<int64_t>(lhs_lo, 2 * i, js, k, l) : kat<int64_t>(lhs_hi, 2 * i, js, k, l);
+        const int64_t* rp = lo ? kat<int64_t>(rhs_lo, 2 * i, js, k, l) : kat<int64_t>(rhs_hi, 2 * i, js, k, l);
+        const int64_t ls = lo ? lhs_lo.s0 : lhs_hi.s0, rs = lo ? rhs_lo.s0 : rhs_hi.s0;
+        int64_t l0 = lp[0], l1 = lp[ls];
+        int64_t r0 = rp[0], r1 = rp[rs];
         i128 a0 = (i128)l0 * (i128)r0;
         i128 a1 = (i128)((u128)((i128)l0 * (i128)r1) + (u128)((i128)l1 * (i128)r0));
         i128 a2 = (i128)l1 * (i128)r1;
@@ -415,14 +422,15 @@ hc_status launch_giant(hc_context ctx, const KView& babies, const KView& lcoef, 
     return HC_OK;
 }
 
-hc_status launch_tensor(hc_context ctx, const KView& d, const KView& lhs, const KView& rhs, const KMods& m, int f0,
-                        int f1, int f2) {
+hc_status launch_tensor(hc_context ctx, const KView& d, const KView& lhs_lo, const KView& lhs_hi, const KView& rhs_lo,
+                        const KView& rhs_hi, int rsplit, const KMods& m, int f0, int f1, int f2) {
     int64_t lines = (d.n0 / 3) * d.n1 * d.n2;
     if (lines == 0 || d.n3 == 0) return HC_OK;
     int chunks;
     unsigned blocks;
     grid_lines(ctx, d.n3, lines, &chunks, &blocks);
-    tensor_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(d, lhs, rhs, m, f0, f1, f2, lines, chunks);
+    tensor_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(d, lhs_lo, lhs_hi, rhs_lo, rhs_hi, rsplit, m, f0, f1, f2, lines,
+                                                       chunks);
     count_launch(ctx);
     return cuda_check(cudaGetLastError(), "tensor kernel launch");
 }
