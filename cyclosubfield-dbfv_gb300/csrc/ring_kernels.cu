@@ -72,14 +72,18 @@ __device__ __forceinline__ void limb_mac2(const int2* __restrict__ xcol, const i
 
 /// The conversion's epilogue for output j of block b: v (the double-reduced sums) plus the
 /// correction mul_mont(q, qmodp), to Montgomery form, optionally dst <- mul_mont(dst - y, b_j).
+template <bool SUB>
 __device__ __forceinline__ void bconv_store(const BconvArgs& a, const KMods& dm, int b, int j, int64_t q, int64_t v,
                                             int64_t* p) {
     const int64_t n = dm.n[j], ninv = dm.ninv[j];
-    const int64_t* qt = a.c.qtab + ((int64_t)b * a.rd + j) * (2 * a.c.qhalf + 1) + a.c.qhalf;
+    const int64_t* qt = a.c.qtab + (b * a.rd + j) * (2 * a.c.qhalf + 1) + a.c.qhalf;
     const int64_t qm = (q >= -a.c.qhalf && q <= a.c.qhalf) ? __ldg(qt + q)
-                                                            : mul_mont(q, a.c.qmodp[(int64_t)b * a.rd + j], n, ninv);
+                                                            : mul_mont(q, a.c.qmodp[b * a.rd + j], n, ninv);
     const int64_t y = mul_mont_c(wadd(v, qm), dm.r2[j], __ldg(a.c.r2p + j), n);  // to_mont64
-    *p = a.sub_mul ? mul_mont_c(wsub(*p, y), __ldg(a.sub_mul + j), __ldg(a.sub_mul + a.rd + j), n) : y;
+    if constexpr (SUB)
+        *p = mul_mont_c(wsub(*p, y), __ldg(a.sub_mul + j), __ldg(a.sub_mul + a.rd + j), n);
+    else
+        *p = y;
 }
 
 /// BEHZ base conversion of one position per thread (BConvCache::bconv, src/ring.rs:1660-1702,
@@ -87,6 +91,9 @@ __device__ __forceinline__ void bconv_store(const BconvArgs& a, const KMods& dm,
 /// block y % nb (a gadget digit), outputs [z ochunk, (z + 1) ochunk) of the block; only the
 /// block's own source columns are lifted. The products with the conversion matrix use its limb
 /// form: the shared array holds each lift as its limb pair (x mod 2^29, x >> 29).
+/// ONE_CHUNK: the block's columns form one chunk of the reference's chunked matmul (always for
+/// 57-bit primes); SUB: rescale's subtract-and-multiply store (BconvArgs::sub_mul).
+template <bool ONE_CHUNK, bool SUB>
 __global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a, KMods sm, KMods dm) {
     extern __shared__ int2 xs[];  // [r][BCONV_THREADS]
     const int b = (int)(blockIdx.y % (unsigned)a.nb);
@@ -96,9 +103,11 @@ __global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a,
     const int64_t pos = (int64_t)blockIdx.x * BCONV_THREADS + threadIdx.x;
     if (pos >= a.npos) return;
     const int64_t k = pos / a.src.n3, l = pos - k * a.src.n3;
+    const int64_t* __restrict__ srcp = kat<int64_t>(a.src, i, 0, k, l);       // row u at u * src.s1
+    int64_t* __restrict__ dstp = kat<int64_t>(a.dst, i * a.nb + b, 0, k, l);  // row j at j * dst.s1
     // the source is multiplied by (Q/p)^-1 in Montgomery form, giving plain lifts in (-p, p)
     for (int u = u0; u < u1; u++) {
-        int64_t x = *kat<int64_t>(a.src, i, u, k, l);
+        int64_t x = srcp[u * a.src.s1];
         x = mul_mont_c(x, __ldg(a.c.qinv + u), __ldg(a.c.qinvp + u), sm.n[u]);
         xs[u * BCONV_THREADS + threadIdx.x] = make_int2((int)(x & ((1 << LIMB_BITS) - 1)), (int)(x >> LIMB_BITS));
     }
@@ -135,22 +144,30 @@ __global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a,
         const int4* __restrict__ m0 = a.c.mat3 + ((int64_t)b * a.rd + j) * a.r;
         const int4* __restrict__ m1 = two ? m0 + a.r : m0;
         int64_t v0 = 0, v1 = 0;
-        bool first = true;
-        for (int c0 = 0; c0 < a.r; c0 += a.c.chunk) {
-            const int lo = max(c0, u0), hi = min(min(c0 + a.c.chunk, a.r), u1);
+        if constexpr (ONE_CHUNK) {
             uint64_t l0 = 0, l1 = 0;
             int64_t h0 = 0, h1 = 0;
-            limb_mac2(xcol, m0, m1, lo, hi, l0, h0, l1, h1);
-            const int64_t r0 = double_red_words(l0, h0, dm.n[j], dm.ninv[j]);
-            v0 = first ? r0 : wadd(v0, r0);
-            if (two) {
-                const int64_t r1 = double_red_words(l1, h1, dm.n[j + 1], dm.ninv[j + 1]);
-                v1 = first ? r1 : wadd(v1, r1);
+            limb_mac2(xcol, m0, m1, u0, u1, l0, h0, l1, h1);
+            v0 = double_red_words(l0, h0, dm.n[j], dm.ninv[j]);
+            v1 = double_red_words(l1, h1, dm.n[j + two], dm.ninv[j + two]);
+        } else {
+            bool first = true;
+            for (int c0 = 0; c0 < a.r; c0 += a.c.chunk) {
+                const int lo = max(c0, u0), hi = min(min(c0 + a.c.chunk, a.r), u1);
+                uint64_t l0 = 0, l1 = 0;
+                int64_t h0 = 0, h1 = 0;
+                limb_mac2(xcol, m0, m1, lo, hi, l0, h0, l1, h1);
+                const int64_t r0 = double_red_words(l0, h0, dm.n[j], dm.ninv[j]);
+                v0 = first ? r0 : wadd(v0, r0);
+                if (two) {
+                    const int64_t r1 = double_red_words(l1, h1, dm.n[j + 1], dm.ninv[j + 1]);
+                    v1 = first ? r1 : wadd(v1, r1);
+                }
+                first = false;
             }
-            first = false;
         }
-        bconv_store(a, dm, b, j, q, v0, kat<int64_t>(a.dst, i * a.nb + b, j, k, l));
-        if (two) bconv_store(a, dm, b, j + 1, q, v1, kat<int64_t>(a.dst, i * a.nb + b, j + 1, k, l));
+        bconv_store<SUB>(a, dm, b, j, q, v0, dstp + j * a.dst.s1);
+        if (two) bconv_store<SUB>(a, dm, b, j + 1, q, v1, dstp + (j + 1) * a.dst.s1);
     }
 }
 
@@ -334,8 +351,11 @@ hc_status launch_bconv_fused(hc_context ctx, const KView& src, const KView& dst,
     size_t smem = (size_t)r * BCONV_THREADS * 8;
     if (smem > 49152) {
         if (smem > max_smem_optin(ctx)) return fail(HC_ERR_UNSUPPORTED, "base conversion: too many source rows");
-        cudaError_t e = cudaFuncSetAttribute(bconv_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return cuda_check(e, "bconv smem attribute");
+        for (auto kern : {bconv_fused_kernel<true, false>, bconv_fused_kernel<true, true>,
+                          bconv_fused_kernel<false, false>, bconv_fused_kernel<false, true>}) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return cuda_check(e, "bconv smem attribute");
+        }
     }
     if (ns * nb > 65535) return fail(HC_ERR_UNSUPPORTED, "base conversion: batch too large");
     // split the outputs over CTAs while the grid is below about two waves of 8 CTAs per SM
@@ -347,7 +367,10 @@ hc_status launch_bconv_fused(hc_context ctx, const KView& src, const KView& dst,
     a.ochunk = 2 * ((rd + 2 * splits - 1) / (2 * splits));
     splits = (rd + a.ochunk - 1) / a.ochunk;
     dim3 grid((unsigned)cols, (unsigned)(ns * nb), (unsigned)splits);
-    bconv_fused_kernel<<<grid, BCONV_THREADS, smem, stream_of(ctx)>>>(a, sm, dm);
+    const bool one_chunk = c.chunk >= r, sub = sub_mul != nullptr;
+    auto kern = one_chunk ? (sub ? bconv_fused_kernel<true, true> : bconv_fused_kernel<true, false>)
+                          : (sub ? bconv_fused_kernel<false, true> : bconv_fused_kernel<false, false>);
+    kern<<<grid, BCONV_THREADS, smem, stream_of(ctx)>>>(a, sm, dm);
     count_launch(ctx);
     return cuda_check(cudaGetLastError(), "bconv kernel launch");
 }
