@@ -98,6 +98,8 @@ def test_hom_gal_keyset(setups, name, budget):
 @pytest.mark.parametrize("name,length,log2_b,log2_t,dct,budget", [
     ("field_18", 8, 4, 8, 2, 100), ("field_18", 8, 4, 8, 2, 0), ("field_18", 1, 4, 8, 2, 0),
     ("field_18", 3, 3, 9, 1, 1), ("field_49152", 20, 6, 18, 3, 2), ("field_49152", 5, 8, 16, 2, 100),
+    # six output digits: the giant-step kernel runs in two launches of up to four digits
+    ("field_18", 8, 2, 12, 4, 100), ("field_18", 6, 2, 12, 6, 1),
 ])
 def test_hom_cyclic_transform(setups, name, length, log2_b, log2_t, dct, budget):
     import ringcuda
