@@ -2,9 +2,9 @@
 // BFV layer with one pass over the data, computing exactly the same integers:
 //  - bconv_fused_kernel: BEHZ base conversion, plain (BConvCache::bconv,
 //    cyclosubfield-dbfv/src/ring.rs:1663-1701) and gadget-batched (GadgetBConvCache::bconv,
-//    src/ring.rs:1809-1851): mul_mont64 by (q/p)^-1, the small-K i128 matmul, the double reduction,
-//    the q~-scaled correction and the conversion to Montgomery form, without the i128 `tmp` /
-//    `correction` tensors ever reaching HBM.
+//    src/ring.rs:1809-1851): mul_mont64 by (q/p)^-1, the small-K matmul (exact, in 29-bit limbs),
+//    the double reduction, the q~-scaled correction and the conversion to Montgomery form, without
+//    the i128 `tmp` / `correction` tensors ever reaching HBM.
 //  - galois_kernel: both permutation passes of apply_galois (src/ring.rs:1212-1222) as one gather.
 //  - keyswitch_kernel: the key-switch inner product, the addition of c0 / c1 through mont(1)
 //    and reduce_wide (src/bfv.rs:498-556, src/ring.rs:460-485, :503-509, :846-865).
