@@ -445,6 +445,9 @@ def e2e_steps(be, work, steps):
 # `python bench.py --roofline-only` (profiles/ntt_line_kernel_intt_dim3_field36864_r34.md): the
 # tensor is read once; its writes stay in L2 during the launch.
 NCU_TRAFFIC_BYTES = 30239232
+# Busy fraction of the integer multiply (fmaheavy, IMAD family) pipe over the same launch's elapsed
+# cycles, from the same capture: the bound the kernel actually sits against.
+NCU_IMAD_PIPE_FRAC = 0.632
 
 
 def kernel_roofline(be, R, base, reps, peaks):
@@ -475,6 +478,8 @@ def kernel_roofline(be, R, base, reps, peaks):
             "traffic": NCU_TRAFFIC_BYTES if len(lifted) == 34 else None,
             "bytes_per_launch": bytes_alg, "launch_ms": round(ms, 5),
             "peak_source": "measured" if not peaks.get("fallback") else "fallback",
+            "int_pipe": {"pipe": "fmaheavy (IMAD)", "busy_frac_of_elapsed": NCU_IMAD_PIPE_FRAC,
+                         "source": "ncu capture of the same launch (--roofline-only)"},
             "note": "bit-exact lazy Barrett NTT: bound by the 32-bit integer multiply pipe, not by HBM"}
 
 
