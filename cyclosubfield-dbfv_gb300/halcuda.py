@@ -386,6 +386,14 @@ class CudaBackend:
 
 
 # ---------------------------------------------------------------------------------- runtime
+def barrett_peak(be):
+    """The GPU's rate (products/s) of the transforms' exact 64-bit Barrett product, measured by a
+    register-only kernel (hc_barrett_peak)."""
+    v = ctypes.c_double()
+    check(lib().hc_barrett_peak(be.h, ctypes.byref(v)))
+    return float(v.value)
+
+
 class PinnedBuffer:
     """Page-locked host memory viewed as a numpy int64 array."""
 

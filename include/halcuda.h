@@ -193,6 +193,10 @@ hc_status hc_event_query(hc_event ev, int* done);
  * HC_ERR_TIMEOUT; timeout_ms <= 0 waits without bound). */
 hc_status hc_event_elapsed_ms(hc_event start, hc_event end, double timeout_ms, float* ms);
 hc_status hc_device_memory(hc_context ctx, size_t* free_bytes, size_t* total_bytes);
+/* Measurement utility (no reference counterpart): the GPU's rate of the transforms' exact 64-bit
+ * Barrett product, from a register-only kernel on the context's stream (about a millisecond;
+ * synchronises the stream). The integer-pipe roofline denominator of the compute-bound NTTs. */
+hc_status hc_barrett_peak(hc_context ctx, double* products_per_s);
 
 /* CUDA-graph capture of a sequence of calls on the context's stream (for launch-bound loops):
  * every call between begin and end is recorded, not executed; hc_graph_launch replays it. The
