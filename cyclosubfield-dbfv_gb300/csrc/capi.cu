@@ -427,7 +427,19 @@ hc_status ntt_mul_mont64_dim_from(hc_context ctx, hc_view dst, hc_view src, cons
     hc_status st;
     if (!ctx) return fail(HC_ERR_ARG, "null context");
     if (nplans && !plans) return fail(HC_ERR_ARG, "null plans");
-    if (!ntt_column_path(plans, nplans, (int)dim)) {
+    // the column kernel reads each column whole before writing it: an exact alias is an in-place
+    // call; any other overlap of the two views' address ranges takes the copy path
+    auto range = [](const hc_view& v, const char** lo, const char** hi) {
+        int64_t last = 0;
+        for (int d = 0; d < 4; d++) last += (v.shape[d] > 0 ? v.shape[d] - 1 : 0) * (d == 3 ? 1 : v.strides[d]);
+        *lo = (const char*)v.ptr;
+        *hi = (const char*)v.ptr + 8 * (last + 1);
+    };
+    const char *dl, *dh, *sl, *sh;
+    range(dst, &dl, &dh);
+    range(src, &sl, &sh);
+    const bool overlap = src.ptr != dst.ptr && sl < dh && dl < sh;
+    if (overlap || !ntt_column_path(plans, nplans, (int)dim)) {
         if ((st = hc_assign(ctx, dst, src))) return st;
         return ntt_call(ctx, dst, plans, nplans, dim, 2, &mul, mods, nmods);
     }
