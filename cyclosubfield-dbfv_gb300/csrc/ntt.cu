@@ -662,6 +662,9 @@ __device__ __forceinline__ void run_column(const DevPlanHeader* P, const fast::C
 }
 
 #define HC_COL_THREADS 256
+#ifndef HC_L3072_MIN_BLOCKS
+#define HC_L3072_MIN_BLOCKS 7  // resident CTAs per SM the 3072-residue line kernel's registers must allow (7 fit its shared memory)
+#endif
 #ifndef HC_COL12_MIN_BLOCKS
 #define HC_COL12_MIN_BLOCKS 4  // resident CTAs per SM the [4, 3] column kernel's registers must allow
 #endif
@@ -707,7 +710,7 @@ hc_status launch_special(hc_context ctx, const KView& t, const PlanPtrs& pp, con
         if (tiles * 3 > 0x7fffffff) return hc::fail(HC_ERR_UNSUPPORTED, "too many NTT lines in one call");
         kern<<<(unsigned)(tiles * 3), 128, smem3, hc::stream_of(ctx)>>>(t, pp, mul, mods);
     } else if constexpr (SHAPE == HC_SHAPE_L3072) {
-        constexpr int TH = SHAPE == HC_SHAPE_L3072 ? 128 : 256, MB = SHAPE == HC_SHAPE_L3072 ? 6 : 2;
+        constexpr int TH = SHAPE == HC_SHAPE_L3072 ? 128 : 256, MB = SHAPE == HC_SHAPE_L3072 ? HC_L3072_MIN_BLOCKS : 2;
         auto kern = ntt_line_kernel<SHAPE, MODE, FIX, TH, MB>;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return hc::cuda_check(e, "ntt smem attribute");
