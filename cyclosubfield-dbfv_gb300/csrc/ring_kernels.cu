@@ -47,26 +47,42 @@ __device__ __forceinline__ void fold_limbs(uint64_t& lo, int64_t& hi, int64_t a0
 /// with |x| < 2^57 and |m| < 2^56 (so |x1| <= 2^28, |m1| <= 2^27) the products x0 m0 < 2^58,
 /// |x1 m1| <= 2^55 and |(x0 + x1)(m0 + m1)| < 2^58.91 add up over 16 terms in int64 without
 /// overflow; the middle column x0 m1 + x1 m0 is the Karatsuba difference of the three sums.
+/// Terms [u, u + n) of one group into the six int64 column sums (xp, p0, p1 at term u).
+template <int N>
+__device__ __forceinline__ void limb_terms(const int2* __restrict__ xp, const int4* __restrict__ p0,
+                                           const int4* __restrict__ p1, int n, int64_t (&s)[6]) {
+#pragma unroll
+    for (int t = 0; t < N; t++) {
+        if (N == LIMB_GROUP || t < n) {
+            const int2 x = xp[t * BCONV_THREADS];
+            const int xs = x.x + x.y;
+            const int4 p = __ldg(p0 + t), q = __ldg(p1 + t);
+            s[0] += (int64_t)x.x * p.x;
+            s[1] += (int64_t)x.y * p.y;
+            s[2] += (int64_t)xs * p.z;
+            s[3] += (int64_t)x.x * q.x;
+            s[4] += (int64_t)x.y * q.y;
+            s[5] += (int64_t)xs * q.z;
+        }
+    }
+}
+
 __device__ __forceinline__ void limb_mac2(const int2* __restrict__ xcol, const int4* __restrict__ m0,
                                           const int4* __restrict__ m1, int lo, int hi, uint64_t& l0, int64_t& h0,
                                           uint64_t& l1, int64_t& h1) {
     for (int g0 = lo; g0 < hi; g0 += LIMB_GROUP) {
-        const int g1 = min(g0 + LIMB_GROUP, hi);
-        int64_t a00 = 0, am = 0, a11 = 0, b00 = 0, bm = 0, b11 = 0;
-#pragma unroll 4
-        for (int u = g0; u < g1; u++) {
-            const int2 x = xcol[u * BCONV_THREADS];
-            const int xs = x.x + x.y;
-            const int4 p = __ldg(m0 + u), q = __ldg(m1 + u);
-            a00 += (int64_t)x.x * p.x;
-            a11 += (int64_t)x.y * p.y;
-            am += (int64_t)xs * p.z;
-            b00 += (int64_t)x.x * q.x;
-            b11 += (int64_t)x.y * q.y;
-            bm += (int64_t)xs * q.z;
+        const int n = min(LIMB_GROUP, hi - g0);
+        int64_t s[6] = {0, 0, 0, 0, 0, 0};  // a00, a11, am, b00, b11, bm
+        const int2* xp = xcol + g0 * BCONV_THREADS;
+        // a full group fully unrolled (every address an immediate offset), a partial one in
+        // steps of four
+        if (n == LIMB_GROUP) {
+            limb_terms<LIMB_GROUP>(xp, m0 + g0, m1 + g0, n, s);
+        } else {
+            for (int t = 0; t < n; t += 4) limb_terms<4>(xp + t * BCONV_THREADS, m0 + g0 + t, m1 + g0 + t, n - t, s);
         }
-        fold_limbs(l0, h0, a00, am - a00 - a11, a11);
-        fold_limbs(l1, h1, b00, bm - b00 - b11, b11);
+        fold_limbs(l0, h0, s[0], s[2] - s[0] - s[1], s[1]);
+        fold_limbs(l1, h1, s[3], s[5] - s[3] - s[4], s[4]);
     }
 }
 
