@@ -349,6 +349,9 @@ def serving_bench(be, n=4000, rate=2000.0):
     for label, batched in (("batched", True), ("plain", False)):
         reqs = serving.make_stream(n, rate, [0.5, 0.35, 0.15], sorted(fields), (4, 20), 2, seed=7)
         out[label] = serving.Engine(be, fields, 16 << 30).run(reqs, batched=batched)
+    # capacity: the same requests all arriving at once (the engine's saturated throughput)
+    reqs = serving.make_stream(n, 1e9, [0.5, 0.35, 0.15], sorted(fields), (4, 20), 2, seed=7)
+    out["capacity_batched"] = serving.Engine(be, fields, 16 << 30).run(reqs, batched=True)
     for f in fields.values():
         f.ring.close()
     return out
