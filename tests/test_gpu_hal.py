@@ -335,3 +335,31 @@ def test_errors_are_reported(be):
         be.hal_add_i64(a, b)
     with pytest.raises(halcuda.HalError, match="modulus"):
         be.hal_mul_mont64(a, a, [be.hal_create_modulus(97)] * 2)
+
+
+def test_runtime_stream_wait_and_barrett_peak(be):
+    """hc_stream_wait_event orders work across streams (a copy on a second stream waits for a fill
+    on the first); hc_barrett_peak returns a positive finite rate."""
+    import math
+
+    import halcuda
+
+    n = 1 << 20
+    src = be.hal_allocate_i64((1, 1, 1, n))
+    dst = be.hal_allocate_i64((1, 1, 1, n))
+    be.synchronize()
+    halcuda.memset_async(be, src.ptr, 0x11, n * 8)
+    ev = halcuda.Event()
+    ev.record(be)
+    s = halcuda.Stream()
+    with be.on(s):
+        ev.wait(be)
+        halcuda.memcpy_async(be, dst.ptr, src.ptr, n * 8, halcuda.D2D)
+        done = halcuda.Event()
+        done.record(be)
+    be.synchronize()
+    done.elapsed_ms(done)
+    assert (dst.to_numpy() == 0x1111111111111111).all()
+    s.close()
+    rate = halcuda.barrett_peak(be)
+    assert math.isfinite(rate) and rate > 1e9
