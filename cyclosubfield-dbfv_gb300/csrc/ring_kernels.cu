@@ -90,14 +90,14 @@ __device__ __forceinline__ void limb_mac2(const int2* __restrict__ xcol, const i
 /// correction mul_mont(q, qmodp), to Montgomery form, optionally dst <- mul_mont(dst - y, b_j).
 template <bool SUB>
 __device__ __forceinline__ void bconv_store(const BconvArgs& a, const KMods& dm, int b, int j, int64_t q, int64_t v,
-                                            int64_t* p) {
+                                            int64_t* p, int64_t old) {
     const int64_t n = dm.n[j], ninv = dm.ninv[j];
     const int64_t* qt = a.c.qtab + (b * a.rd + j) * (2 * a.c.qhalf + 1) + a.c.qhalf;
     const int64_t qm = (q >= -a.c.qhalf && q <= a.c.qhalf) ? __ldg(qt + q)
                                                             : mul_mont(q, a.c.qmodp[b * a.rd + j], n, ninv);
     const int64_t y = mul_mont_c(wadd(v, qm), dm.r2[j], __ldg(a.c.r2p + j), n);  // to_mont64
     if constexpr (SUB)
-        *p = mul_mont_c(wsub(*p, y), __ldg(a.sub_mul + j), __ldg(a.sub_mul + a.rd + j), n);
+        *p = mul_mont_c(wsub(old, y), __ldg(a.sub_mul + j), __ldg(a.sub_mul + a.rd + j), n);
     else
         *p = y;
 }
@@ -160,6 +160,13 @@ __global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a,
         const int4* __restrict__ m0 = a.c.mat3 + ((int64_t)b * a.rd + j) * a.r;
         const int4* __restrict__ m1 = two ? m0 + a.r : m0;
         int64_t v0 = 0, v1 = 0;
+        // the subtract-and-multiply store's operands, loaded before the sums so that their
+        // latency hides behind the multiply-accumulate
+        int64_t old0 = 0, old1 = 0;
+        if constexpr (SUB) {
+            old0 = dstp[j * a.dst.s1];
+            if (two) old1 = dstp[(j + 1) * a.dst.s1];
+        }
         if constexpr (ONE_CHUNK) {
             uint64_t l0 = 0, l1 = 0;
             int64_t h0 = 0, h1 = 0;
@@ -182,8 +189,8 @@ __global__ void __launch_bounds__(BCONV_THREADS) bconv_fused_kernel(BconvArgs a,
                 first = false;
             }
         }
-        bconv_store<SUB>(a, dm, b, j, q, v0, dstp + j * a.dst.s1);
-        if (two) bconv_store<SUB>(a, dm, b, j + 1, q, v1, dstp + (j + 1) * a.dst.s1);
+        bconv_store<SUB>(a, dm, b, j, q, v0, dstp + j * a.dst.s1, old0);
+        if (two) bconv_store<SUB>(a, dm, b, j + 1, q, v1, dstp + (j + 1) * a.dst.s1, old1);
     }
 }
 
