@@ -539,6 +539,14 @@ struct PermCache {
 
 struct hc_ring_s {
     hc_context ctx;
+    // a second stream for independent branches of one call (SideBranch), with its fork / join events
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    void create_side() {
+        CK(cuda_check(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking), "ring side stream"));
+        CK(cuda_check(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming), "ring branch event"));
+        CK(cuda_check(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming), "ring branch event"));
+    }
     Field field;
     std::vector<Factor> factors;
     size_t initial_len = 0;
@@ -554,6 +562,12 @@ struct hc_ring_s {
 
     ~hc_ring_s() {
         cudaStreamSynchronize(stream_of(ctx));
+        if (side) {
+            cudaStreamSynchronize(side);
+            cudaStreamDestroy(side);
+        }
+        if (fork_ev) cudaEventDestroy(fork_ev);
+        if (join_ev) cudaEventDestroy(join_ev);
         for (auto& f : factors) {
             if (f.plan_lp) hc_destroy_ntt_plan(ctx, f.plan_lp);
             if (f.plan_k) hc_destroy_ntt_plan(ctx, f.plan_k);
@@ -1200,6 +1214,45 @@ void keyswitch(hc_ring R, const hc_view& parts, const hc_view& keys, const Base&
                         needs_full(b0, minp), needs_full(b1, minp), kv(out), R->kmods(base), R->one_dev(base), p2, p3));
 }
 
+/// Independent work of one call on the ring's side stream: begin() orders the branch after the
+/// current stream's prior work and makes the side stream current, back() makes the original stream
+/// current again while the branch keeps running, join() makes the original stream wait for the
+/// branch (device-side; the host does not block). Inside a graph capture the branch becomes a
+/// parallel path of the graph. The destructor restores the original stream and joins on every
+/// exit path.
+struct SideBranch {
+    hc_ring R;
+    void* main;
+    bool on_side = false, open = false;
+    explicit SideBranch(hc_ring r) : R(r), main(hc_context_stream(r->ctx)) {}
+    void begin() {
+        CK(cuda_check(cudaEventRecord(R->fork_ev, (cudaStream_t)main), "branch fork"));
+        CK(cuda_check(cudaStreamWaitEvent(R->side, R->fork_ev, 0), "branch fork"));
+        CK(hc_context_set_stream(R->ctx, R->side));
+        on_side = open = true;
+    }
+    void back() {
+        CK(hc_context_set_stream(R->ctx, main));
+        on_side = false;
+    }
+    void join() {
+        if (on_side) back();
+        if (!open) return;
+        open = false;
+        CK(cuda_check(cudaEventRecord(R->join_ev, R->side), "branch join"));
+        CK(cuda_check(cudaStreamWaitEvent((cudaStream_t)main, R->join_ev, 0), "branch join"));
+    }
+    ~SideBranch() {
+        if (on_side) hc_context_set_stream(R->ctx, main);
+        if (open) {
+            cudaEventRecord(R->join_ev, R->side);
+            cudaStreamWaitEvent((cudaStream_t)main, R->join_ev, 0);
+        }
+    }
+    SideBranch(const SideBranch&) = delete;
+    SideBranch& operator=(const SideBranch&) = delete;
+};
+
 /// The extension base of lift_to_extended (src/bfv.rs:564-598, src/ring.rs:716-731): extension
 /// primes until log2 Q + t_bits + 60 bits are covered.
 Base extension_of(hc_ring R, const Base& base) {
@@ -1272,6 +1325,7 @@ hc_status hc_ring_create(hc_context ctx, const char* field, size_t lo, size_t hi
         REQUIRE(hi > lo, HC_ERR_ARG, "log2 q range");
         auto R = std::make_unique<hc_ring_s>();
         R->ctx = ctx;
+        R->create_side();
         R->field = Field::make(field);
         int64_t rou = (int64_t)R->field.rou_order();
         std::vector<int64_t> base = sample_primes({}, lo, hi, 57, rou);
@@ -1288,6 +1342,7 @@ hc_status hc_ring_create_raw(hc_context ctx, const char* field, const int64_t* p
         REQUIRE(ctx && field && out && (n == 0 || primes), HC_ERR_ARG, "null argument");
         auto R = std::make_unique<hc_ring_s>();
         R->ctx = ctx;
+        R->create_side();
         R->field = Field::make(field);
         R->initial_len = n;
         for (size_t i = 0; i < n; i++) {
@@ -1546,7 +1601,13 @@ hc_status hc_bfv_hom_mul(hc_ring R, const int64_t t[2], hc_view ct1, hc_view ct2
             R->transform(pb.view(), b, true, nullptr, &ct);  // pb = crt_to_pb(ct)
             return lift_extension_rows(R, pb.view(), b, ext);
         };
-        Tensor lh = lift(ct1), rh = lift(ct2);
+        // the two lifts are independent: the second runs on the side stream beside the first
+        SideBranch lifts(R);
+        lifts.begin();
+        Tensor rh = lift(ct2);
+        lifts.back();
+        Tensor lh = lift(ct1);
+        lifts.join();
         Base lifted = b;
         lifted.insert(lifted.end(), ext.begin(), ext.end());
         // tensor product + reduce_wide (src/bfv.rs:667-683, :769-771); rows 2i, 2i + 1 hold
@@ -1565,13 +1626,19 @@ hc_status hc_bfv_hom_mul(hc_ring R, const int64_t t[2], hc_view ct1, hc_view ct2
         // relinearisation (src/bfv.rs:699-741)
         Digits dg = clip(digits_of(digits, d), r);
         REQUIRE(rk.shape[0] >= 2 * (int64_t)dg.size() && rk.shape[1] >= rr, HC_ERR_SHAPE, "relinearisation key shape");
-        Tensor parts = gadget_decompose(R, vrows(resc.view(), 2 * B, 3 * B), b, dg);
         hc_view c01 = vrows(resc.view(), 0, 2 * B);
         if (!period_output) {
+            // c2's decomposition (side stream) and c0, c1's transform are independent
+            SideBranch relin(R);
+            relin.begin();
+            Tensor parts = gadget_decompose(R, vrows(resc.view(), 2 * B, 3 * B), b, dg);
+            relin.back();
             R->transform(c01, b, false);
+            relin.join();
             hc_view a0 = vstep(c01, 0, 2, B), a1 = vstep(c01, 1, 2, B);
             keyswitch(R, parts.view(), rk, b, dg.size(), &a0, &a1, out);
         } else {
+            Tensor parts = gadget_decompose(R, vrows(resc.view(), 2 * B, 3 * B), b, dg);
             keyswitch(R, parts.view(), rk, b, dg.size(), nullptr, nullptr, out);
             R->transform(out, b, true);
             CK(hc_add_i64(R->ctx, out, c01));
