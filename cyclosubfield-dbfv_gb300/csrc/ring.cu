@@ -1621,24 +1621,28 @@ hc_status hc_bfv_hom_mul(hc_ring R, const int64_t t[2], hc_view ct1, hc_view ct2
         }
         const Tensor& tscale = R->scalar_tensor(lifted, words(t));
         const hc_view tsv = tscale.view();
-        R->transform(prod.view(), lifted, true, &tsv);
-        Tensor resc = rescale_to_base(R, prod.view(), lifted, r, words(t), true);
         // relinearisation (src/bfv.rs:699-741)
         Digits dg = clip(digits_of(digits, d), r);
         REQUIRE(rk.shape[0] >= 2 * (int64_t)dg.size() && rk.shape[1] >= rr, HC_ERR_SHAPE, "relinearisation key shape");
-        hc_view c01 = vrows(resc.view(), 0, 2 * B);
+        // from here the (c0, c1) rows and the c2 rows are independent until the key switch: c2's
+        // transform, rescale and gadget decomposition run on the side stream beside c0, c1's
+        // transform, rescale and (CRT output) forward transform
+        const hc_view p01 = vrows(prod.view(), 0, 2 * B), p2 = vrows(prod.view(), 2 * B, 3 * B);
+        SideBranch c2_branch(R);
+        c2_branch.begin();
+        R->transform(p2, lifted, true, &tsv);
+        Tensor resc2 = rescale_to_base(R, p2, lifted, r, words(t), true);
+        Tensor parts = gadget_decompose(R, resc2.view(), b, dg);
+        c2_branch.back();
+        R->transform(p01, lifted, true, &tsv);
+        Tensor resc01 = rescale_to_base(R, p01, lifted, r, words(t), true);
+        const hc_view c01 = resc01.view();
+        if (!period_output) R->transform(c01, b, false);
+        c2_branch.join();
         if (!period_output) {
-            // c2's decomposition (side stream) and c0, c1's transform are independent
-            SideBranch relin(R);
-            relin.begin();
-            Tensor parts = gadget_decompose(R, vrows(resc.view(), 2 * B, 3 * B), b, dg);
-            relin.back();
-            R->transform(c01, b, false);
-            relin.join();
             hc_view a0 = vstep(c01, 0, 2, B), a1 = vstep(c01, 1, 2, B);
             keyswitch(R, parts.view(), rk, b, dg.size(), &a0, &a1, out);
         } else {
-            Tensor parts = gadget_decompose(R, vrows(resc.view(), 2 * B, 3 * B), b, dg);
             keyswitch(R, parts.view(), rk, b, dg.size(), nullptr, nullptr, out);
             R->transform(out, b, true);
             CK(hc_add_i64(R->ctx, out, c01));
