@@ -2,12 +2,14 @@
 
 Workload (BFV ciphertext multiplication at full size): field_36864 (n = 36864 = 12 x 3072), an
 initial RNS base of r = 16 primes of 57 bits (log2 q in 900..930), plaintext modulus t = 256,
-secret key sparse ternary, error sigma = 3.2, relinearisation key with ceil(r/4) = 4 gadget digits;
-one step multiplies B independent ciphertext pairs (bfv_hom_mul incl. lifting, tensoring,
-rescaling and relinearisation). Inputs are seeded synthetic ciphertexts of that shape.
+secret key sparse ternary, error sigma = 3.2, relinearisation key with ceil(r/4) = 4 gadget digits.
+The plain GPU form: one step is one ciphertext multiplication per launch (bfv_hom_mul incl.
+lifting, tensoring, rescaling and relinearisation, replayed from a CUDA graph of the call), the
+steps cycling over B = 8 seeded synthetic ciphertext pairs (larger than L2 together) on two
+streams. The batched form (all B pairs in one call) is reported beside it.
 
 Prints one JSON line. `value` is ct-mults/s with the operands resident in HBM; `e2e` is the same
-metric through the C ABI with the operands copied from pinned host memory and the results
+metric through the C ABI with each step's operands copied from pinned host memory and its result
 copied back inside the timed region. `--impl reference` times the oracle, the CPU restatement of
 the reference's hal::cpu path (the Rust crate cannot be built here), on all host cores.
 """
@@ -34,7 +36,7 @@ L2_BYTES = 129 * 1024 * 1024
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=8, help="ciphertext pairs multiplied per step")
@@ -154,28 +156,30 @@ class Workload:
         self.step()  # first use builds the ring's caches (host synchronising); then capture
         be.synchronize()
         self.graph = halcuda.Graph(be, self.step)
+        # one graph per pair: one ct-mult per launch
+        self.single = [halcuda.Graph(be, lambda b=b: self.plain(b)) for b in range(batch)]
 
     def step(self):
         """All B ct-mults in one call: every stage launches once over the whole batch."""
         self.ring.hom_mul(T, self.ct1, self.ct2, self.base, self.rk, self.digits, out=self.out)
 
     def slots(self):
-        """Two operand slots for double buffering: this workload's own (operands, result, graph) and
-        a second set with copies of the operands and its own captured step."""
+        """Two one-pair operand slots for double buffering: pair 0 with its one-ct-mult graph, and a
+        second set with copies of pair 0's operands and its own captured call."""
         import halcuda
         import types
 
         R = self.ring
-        b = types.SimpleNamespace(ct1=R.allocate(2 * self.batch, self.r), ct2=R.allocate(2 * self.batch, self.r),
-                                  out=R.allocate(2 * self.batch, self.r))
-        self.be.hal_assign(b.ct1, self.ct1)
-        self.be.hal_assign(b.ct2, self.ct2)
+        b = types.SimpleNamespace(ct1=R.allocate(2, self.r), ct2=R.allocate(2, self.r), out=R.allocate(2, self.r))
+        self.be.hal_assign(b.ct1, self.ct1.rows(0, 2))
+        self.be.hal_assign(b.ct2, self.ct2.rows(0, 2))
         self.be.synchronize()
         b.graph = halcuda.Graph(self.be, lambda: R.hom_mul(T, b.ct1, b.ct2, self.base, self.rk, self.digits,
                                                            out=b.out))
         b.graph.launch()  # the first replay uploads the graph; keep it out of the timed region
         self.be.synchronize()
-        a = types.SimpleNamespace(ct1=self.ct1, ct2=self.ct2, out=self.out, graph=self.graph)
+        a = types.SimpleNamespace(ct1=self.ct1.rows(0, 2), ct2=self.ct2.rows(0, 2), out=self.out.rows(0, 2),
+                                  graph=self.single[0])
         return [a, b]
 
     def plain(self, b):
@@ -378,6 +382,31 @@ def timed_steps(be, work, steps, scratch):
     return total
 
 
+def single_steps(be, work, steps, streams, start=0):
+    """`steps` ct-mults, one per launch: step k replays the one-pair graph of pair (start + k) mod B
+    on stream k mod 2 (a graph stays on one stream), back to back. The pairs' operands and results
+    (B = 8: 226 MB) exceed L2, so a step's inputs are not cached from its previous use. Returns the
+    CUDA-event time from before the first to after the last step."""
+    import halcuda
+
+    ev0, ev1 = halcuda.Event(), halcuda.Event()
+    ends = [halcuda.Event() for _ in streams]
+    ev0.record(be)
+    for st in streams:
+        with be.on(st):
+            ev0.wait(be)
+    for k in range(steps):
+        b = (start + k) % work.batch
+        with be.on(streams[b % len(streams)]):
+            work.single[b].launch()
+    for e, st in zip(ends, streams):
+        with be.on(st):
+            e.record(be)
+        e.wait(be)
+    ev1.record(be)
+    return ev0.elapsed_ms(ev1)
+
+
 def plain_calls(be, work, rounds, scratch):
     """Per-call event times of the plain form (one ct-mult per call, no graph)."""
     import halcuda
@@ -395,40 +424,39 @@ def plain_calls(be, work, rounds, scratch):
 
 
 def e2e_steps(be, work, steps):
-    """ct-mults through the C ABI with host buffers: every step copies its operands from pinned host
-    memory, replays the step and copies its result back to pinned host memory, all inside the timed
-    region. Two operand slots on two streams alternate (double buffering), so that one slot's copies
-    overlap the other slot's compute. Every step's result is checked against the resident run's."""
+    """One ct-mult per step through the C ABI with host buffers: step k copies pair k mod B's
+    operands from pinned host memory into one of two device slots, replays the slot's one-pair call
+    and copies the result back to pinned host memory, all inside the timed region. The two slots
+    alternate on two streams (double buffering), so one slot's copies overlap the other slot's
+    compute. Every copied-back result is checked against the resident run's."""
     import halcuda
     import numpy as np
 
     R = work.ring
-    shape = (2 * work.batch, work.r, R.dl, R.dk)
+    full = (2 * work.batch, work.r, R.dl, R.dk)
     slots = work.slots()
-    h1, h2 = halcuda.PinnedBuffer(shape), halcuda.PinnedBuffer(shape)
-    houts = [halcuda.PinnedBuffer(shape) for _ in slots]
+    h1, h2, hout = halcuda.PinnedBuffer(full), halcuda.PinnedBuffer(full), halcuda.PinnedBuffer(full)
     h1.array[...] = work.ct1.to_numpy()
     h2.array[...] = work.ct2.to_numpy()
+    hout.array[...] = 0
     streams = [halcuda.Stream() for _ in slots]
-    nbytes = work.ct_bytes * work.batch
+    nbytes = work.ct_bytes  # one ciphertext pair's operand (or result) bytes
     ev0, ev1 = halcuda.Event(), halcuda.Event()
     ends = [halcuda.Event() for _ in slots]
     be.synchronize()
     expect = work.out.to_numpy()
-    for h in houts:
-        h.array[...] = 0
     ev0.record(be)
     for st in streams:
         with be.on(st):
             ev0.wait(be)
     for step in range(steps):
-        k = step % len(slots)
-        sl = slots[k]
+        k, b = step % len(slots), step % work.batch
+        sl, off = slots[k], b * nbytes
         with be.on(streams[k]):
-            halcuda.memcpy_async(be, sl.ct1.ptr, h1.ptr, nbytes, halcuda.H2D)
-            halcuda.memcpy_async(be, sl.ct2.ptr, h2.ptr, nbytes, halcuda.H2D)
+            halcuda.memcpy_async(be, sl.ct1.ptr, h1.ptr + off, nbytes, halcuda.H2D)
+            halcuda.memcpy_async(be, sl.ct2.ptr, h2.ptr + off, nbytes, halcuda.H2D)
             sl.graph.launch()
-            halcuda.memcpy_async(be, houts[k].ptr, sl.out.ptr, nbytes, halcuda.D2H)
+            halcuda.memcpy_async(be, hout.ptr + off, sl.out.ptr, nbytes, halcuda.D2H)
     for k, st in enumerate(streams):
         with be.on(st):
             ends[k].record(be)
@@ -436,12 +464,12 @@ def e2e_steps(be, work, steps):
     ev1.record(be)
     ms = ev0.elapsed_ms(ev1)
     be.synchronize()
-    for k in range(min(steps, len(slots))):
-        if not np.array_equal(houts[k].array, expect):
-            raise RuntimeError("e2e: the result copied back from slot %d differs from the resident run" % k)
+    for b in range(min(steps, work.batch)):
+        if not np.array_equal(hout.array[2 * b:2 * b + 2], expect[2 * b:2 * b + 2]):
+            raise RuntimeError("e2e: the result of pair %d copied back differs from the resident run" % b)
     for st in streams:
         st.close()
-    return ms, 2 * nbytes, nbytes, houts[(steps - 1) % len(slots)]
+    return ms, 2 * nbytes, nbytes, hout
 
 
 # DRAM bytes (read + written) of one launch of that kernel on that tensor, from an ncu capture of
@@ -626,8 +654,10 @@ def main():
     scratch = be.hal_allocate_i64((1, 1, 1, 2 * L2_BYTES // 8))
     peaks = load_peaks()
 
-    for _ in range(args.warmup):
-        timed_steps(be, work, 1, scratch)
+    streams = [halcuda.Stream(), halcuda.Stream()]
+    for g in work.single:  # first replays upload the graphs
+        g.launch()
+    single_steps(be, work, args.warmup, streams)
     be.synchronize()
 
     clocks = ClockSampler(dist.local_rank)
@@ -635,13 +665,21 @@ def main():
     be.synchronize()
     clocks.start()
     launches0 = be.launch_count()
-    total_ms = timed_steps(be, work, args.steps, scratch)
+    total_ms = single_steps(be, work, args.steps, streams, start=args.warmup)
     be.synchronize()
     launches = be.launch_count() - launches0
     clk = clocks.stop()
     dist.barrier()
     total_ms = dist.max(total_ms)
-    value = dist.world * work.batch * args.steps / (total_ms * 1e-3)
+    value = dist.world * args.steps / (total_ms * 1e-3)
+
+    # the batched form: all B pairs in one call (one graph), L2 flushed before every step
+    for _ in range(args.warmup):
+        timed_steps(be, work, 1, scratch)
+    batched_ms = timed_steps(be, work, args.steps, scratch)
+    batched = {"ct_mults_per_s": round(work.batch * args.steps / (batched_ms * 1e-3), 3), "batch": work.batch,
+               "ms_per_step": round(batched_ms / args.steps, 4),
+               "l2": "flushed before every step (512 MB memset, untimed)"}
 
     # plain form (one ct-mult per timed call) and its latency distribution
     per = plain_calls(be, work, max(2, args.steps // 2), scratch)
@@ -649,8 +687,9 @@ def main():
     plain = 1e3 / statistics.mean(per)
     p50, p99 = per[len(per) // 2], per[min(len(per) - 1, int(math.ceil(0.99 * len(per))) - 1)]
 
-    e2e_ms, h2d, d2h, _ = e2e_steps(be, work, args.steps)
-    e2e_val = dist.world * work.batch * args.steps / (e2e_ms * 1e-3)
+    e2e_n = max(args.steps, 40)  # at least 40 steps, so that the pipeline's fill and drain stay small
+    e2e_ms, h2d, d2h, _ = e2e_steps(be, work, e2e_n)
+    e2e_val = dist.world * e2e_n / (e2e_ms * 1e-3)
     roof = kernel_roofline(be, work.ring, work.base, 20, peaks)
     crt = None if args.no_crt_batch else crt_batch_bench(be, max(3, args.steps // 2), args.warmup)
     hcrt = None if args.no_homcrt else homcrt_bench(be)
@@ -672,11 +711,14 @@ def main():
         "vs_baseline": None,
         "dtype": "int64",
         "data": "synthetic (seeded encryptions of the reference's parameter shapes)",
-        "config": {"workload": "bfv_hom_mul %s r=%d t=%d d=%d, %d ct pairs per step (one batched call, "
-                               "CUDA-graph replay)" % (FIELD, work.r, T, len(work.digits), work.batch),
+        "config": {"workload": "plain GPU form: one bfv_hom_mul per launch (one CUDA-graph replay of the call) "
+                               "at %s r=%d t=%d d=%d" % (FIELD, work.r, T, len(work.digits)),
                    "field": FIELD, "rns_len": work.r,
                    "extension_len": len(work.ring.extension_base(work.base)), "gadget_digits": len(work.digits),
-                   "batch": work.batch, "l2": "flushed before every timed step (512 MB memset, untimed)"},
+                   "ct_mults_per_step": 1, "streams": 2,
+                   "l2": "steps cycle over %d ciphertext pairs (%d MB of operands and results, larger than L2); "
+                         "no flush" % (work.batch, 3 * work.ct_bytes * work.batch // 2**20)},
+        "batched": batched,
         "plain_ct_mults_per_s": round(plain, 3),
         "latency_ms": {"p50": round(p50, 4), "p99": round(p99, 4), "samples": len(per)},
         "e2e": {"value": round(e2e_val, 3), "unit": "ct-mults/s", "h2d_bytes_per_step": h2d,
