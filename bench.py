@@ -39,7 +39,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--batch", type=int, default=8, help="ciphertext pairs multiplied per step")
+    ap.add_argument("--batch", type=int, default=8, help="ciphertext pairs (cycled one per step; all in one "
+                                                            "call in the batched form)")
+    ap.add_argument("--streams", type=int, default=2, help="streams the one-ct-mult launches alternate on")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-crt-batch", action="store_true", help="skip the batched CRT-transform workload")
     ap.add_argument("--no-homcrt", action="store_true", help="skip the homomorphic CRT transform workload")
@@ -654,7 +656,7 @@ def main():
     scratch = be.hal_allocate_i64((1, 1, 1, 2 * L2_BYTES // 8))
     peaks = load_peaks()
 
-    streams = [halcuda.Stream(), halcuda.Stream()]
+    streams = [halcuda.Stream() for _ in range(args.streams)]
     for g in work.single:  # first replays upload the graphs
         g.launch()
     single_steps(be, work, args.warmup, streams)
@@ -715,7 +717,7 @@ def main():
                                "at %s r=%d t=%d d=%d" % (FIELD, work.r, T, len(work.digits)),
                    "field": FIELD, "rns_len": work.r,
                    "extension_len": len(work.ring.extension_base(work.base)), "gadget_digits": len(work.digits),
-                   "ct_mults_per_step": 1, "streams": 2,
+                   "ct_mults_per_step": 1, "streams": len(streams),
                    "l2": "steps cycle over %d ciphertext pairs (%d MB of operands and results, larger than L2); "
                          "no flush" % (work.batch, 3 * work.ct_bytes * work.batch // 2**20)},
         "batched": batched,
