@@ -16,6 +16,12 @@
  * passed as d (start, end) pairs of base positions. Plaintext moduli t are i128 values given as
  * (low, high) int64 words. Random numbers come from the reference's splitmix64 generator
  * (src/bfv.rs:880-886) whose 64-bit state the caller owns and which the call advances.
+ *
+ * Threads and streams: a ring (its table caches and its side streams) is used from one host thread
+ * at a time; calls are asynchronous on the context's current stream (hc_context_set_stream), and
+ * calls issued on different streams of one context may run concurrently on the GPU. Some calls
+ * (hc_bfv_hom_mul) run independent parts on the ring's side stream, forked from and joined back
+ * into the current stream, which a CUDA-graph capture of the call records as parallel paths.
  */
 #ifndef RINGCUDA_H
 #define RINGCUDA_H
