@@ -36,7 +36,7 @@ L2_BYTES = 129 * 1024 * 1024
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=8, help="ciphertext pairs (cycled one per step; all in one "
@@ -85,48 +85,66 @@ class Dist:
 class ClockSampler:
     """nvidia-smi samples of SM clocks and throttle reasons during the timed region."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-         "clocks_event_reasons.sw_power_cap")
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
+        self.begin = self.end = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
+        time.sleep(0.1)  # the sampler's first query precedes the timed region
+
+    def mark(self, begin):
+        """Host wall-clock bounds of the timed region (the samples inside them are the ones reported)."""
+        import datetime
+
+        if begin:
+            self.begin = datetime.datetime.now()
+        else:
+            self.end = datetime.datetime.now()
 
     def stop(self):
+        import datetime
+
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        time.sleep(0.3)
+        time.sleep(0.05)
         self.proc.terminate()
         try:
             out, _ = self.proc.communicate(timeout=5)
         except Exception:
             self.proc.kill()
             out = ""
-        sm, smax, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for line in out.strip().splitlines():
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 9:
+            if len(f) < 10:
                 continue
             try:
-                sm.append(float(f[1]))
-                smax = float(f[2])
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f")
+                rows.append((ts, float(f[2]), float(f[3]), f[6:10]))
             except ValueError:
                 continue
-            for name, val in zip(names, f[5:9]):
+        inside = [r for r in rows if self.begin and self.end and self.begin <= r[0] <= self.end]
+        use = inside or rows  # a region shorter than the sampling period: the samples around it
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in use:
+            for name, val in zip(names, r[3]):
                 if val.lower() == "active":
                     reasons.add(name)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "samples": len(sm),
-                "reasons": sorted(reasons)}
+        sm = [r[1] for r in use]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": use[-1][2] if use else None,
+                "samples": len(use), "samples_in_timed_region": len(inside), "reasons": sorted(reasons)}
 
 
 # ------------------------------------------------------------------------------ workload
@@ -667,8 +685,10 @@ def main():
     be.synchronize()
     clocks.start()
     launches0 = be.launch_count()
+    clocks.mark(True)
     total_ms = single_steps(be, work, args.steps, streams, start=args.warmup)
     be.synchronize()
+    clocks.mark(False)
     launches = be.launch_count() - launches0
     clk = clocks.stop()
     dist.barrier()
@@ -678,13 +698,14 @@ def main():
     # the batched form: all B pairs in one call (one graph), L2 flushed before every step
     for _ in range(args.warmup):
         timed_steps(be, work, 1, scratch)
-    batched_ms = timed_steps(be, work, args.steps, scratch)
-    batched = {"ct_mults_per_s": round(work.batch * args.steps / (batched_ms * 1e-3), 3), "batch": work.batch,
-               "ms_per_step": round(batched_ms / args.steps, 4),
+    nb = min(args.steps, 40)
+    batched_ms = timed_steps(be, work, nb, scratch)
+    batched = {"ct_mults_per_s": round(work.batch * nb / (batched_ms * 1e-3), 3), "batch": work.batch,
+               "ms_per_step": round(batched_ms / nb, 4), "steps": nb,
                "l2": "flushed before every step (512 MB memset, untimed)"}
 
     # plain form (one ct-mult per timed call) and its latency distribution
-    per = plain_calls(be, work, max(2, args.steps // 2), scratch)
+    per = plain_calls(be, work, min(20, max(2, args.steps // 2)), scratch)
     per.sort()
     plain = 1e3 / statistics.mean(per)
     p50, p99 = per[len(per) // 2], per[min(len(per) - 1, int(math.ceil(0.99 * len(per))) - 1)]
@@ -693,7 +714,7 @@ def main():
     e2e_ms, h2d, d2h, _ = e2e_steps(be, work, e2e_n)
     e2e_val = dist.world * e2e_n / (e2e_ms * 1e-3)
     roof = kernel_roofline(be, work.ring, work.base, 20, peaks)
-    crt = None if args.no_crt_batch else crt_batch_bench(be, max(3, args.steps // 2), args.warmup)
+    crt = None if args.no_crt_batch else crt_batch_bench(be, min(20, max(3, args.steps // 2)), args.warmup)
     hcrt = None if args.no_homcrt else homcrt_bench(be)
     srv = None if args.no_serving else serving_bench(be)
 
