@@ -195,7 +195,8 @@ def test_key_switch_lift_rescale_modswitch(rings):
 
 
 HOM_MUL_CASES = [("field_192", 100, 120, 8, 256, 1.0), ("field_18", 300, 320, 16, 1 << 16, 1.0),
-                 ("field_192", 200, 220, 64, 1 << 64, 0.5), ("field_36864", 900, 930, 8, 256, 0.25)]
+                 ("field_192", 200, 220, 64, 1 << 64, 0.5), ("field_36864", 900, 930, 8, 256, 0.25),
+                 ("field_49152", 600, 630, 2, 4, 0.5)]
 
 
 @pytest.mark.parametrize("case", HOM_MUL_CASES, ids=lambda c: "%s-t%d" % (c[0], c[4].bit_length() - 1))
@@ -287,6 +288,29 @@ def test_hom_mul_batched_matches_single(po, be):
             one = d.hom_mul(256, d.tensor(c1[2 * b:2 * b + 2]), d.tensor(c2[2 * b:2 * b + 2]), base, rk, digits,
                             period_output=period).to_numpy()
             assert (got[2 * b:2 * b + 2] == one).all(), (b, period)
+
+
+def test_hom_mul_batched_full_size_matches_oracle(po, be):
+    """Two field_36864 r = 16 ciphertext pairs in one call (the batched form of the benchmark,
+    with its parallel branches) equal the oracle's per-pair hom_mul."""
+    import ringcuda
+
+    o = po.Ring("field_36864", 900, 930, 8)
+    d = ringcuda.RingContext("field_36864", 900, 930, 8, backend=be)
+    base = o.initial_base()
+    la = o.log2_alpha_for_sigma(base, 3.2)
+    st = [19]
+    sk = o.gen_sk(st)
+    digits = po_digits(4, len(base))
+    rk = o.gen_rk(st, sk, digits, la)
+    rk_d = d.tensor(rk.reshape((-1,) + rk.shape[2:]))
+    B = 2
+    c1 = [o.enc(st, base, 256, [(i * (b + 3)) % 256 for i in range(o.n)], sk, la) for b in range(B)]
+    c2 = [o.enc(st, base, 256, [(5 * i + b) % 256 for i in range(o.n)], sk, la) for b in range(B)]
+    got = d.hom_mul(256, d.tensor(np.concatenate(c1)), d.tensor(np.concatenate(c2)), base, rk_d, digits).to_numpy()
+    for b in range(B):
+        exp = o.hom_mul(256, c1[b], c2[b], base, rk, digits)
+        assert (got[2 * b:2 * b + 2] == exp).all(), b
 
 
 def test_graph_replay_matches(po, be):
