@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=8, help="ciphertext pairs (cycled one per step; all in one "
                                                             "call in the batched form)")
     ap.add_argument("--streams", type=int, default=2, help="streams the one-ct-mult launches alternate on")
+    ap.add_argument("--e2e-slots", type=int, default=4, help="operand slots (and streams) of the e2e pipeline "
+                                                              "(a divisor of --batch)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-crt-batch", action="store_true", help="skip the batched CRT-transform workload")
     ap.add_argument("--no-homcrt", action="store_true", help="skip the homomorphic CRT transform workload")
@@ -183,24 +185,26 @@ class Workload:
         """All B ct-mults in one call: every stage launches once over the whole batch."""
         self.ring.hom_mul(T, self.ct1, self.ct2, self.base, self.rk, self.digits, out=self.out)
 
-    def slots(self):
-        """Two one-pair operand slots for double buffering: pair 0 with its one-ct-mult graph, and a
-        second set with copies of pair 0's operands and its own captured call."""
+    def slots(self, n=2):
+        """`n` one-pair operand slots for multi-buffering: pair 0 with its one-ct-mult graph, and
+        n - 1 more sets with copies of pair 0's operands and their own captured calls."""
         import halcuda
         import types
 
         R = self.ring
-        b = types.SimpleNamespace(ct1=R.allocate(2, self.r), ct2=R.allocate(2, self.r), out=R.allocate(2, self.r))
-        self.be.hal_assign(b.ct1, self.ct1.rows(0, 2))
-        self.be.hal_assign(b.ct2, self.ct2.rows(0, 2))
-        self.be.synchronize()
-        b.graph = halcuda.Graph(self.be, lambda: R.hom_mul(T, b.ct1, b.ct2, self.base, self.rk, self.digits,
-                                                           out=b.out))
-        b.graph.launch()  # the first replay uploads the graph; keep it out of the timed region
-        self.be.synchronize()
-        a = types.SimpleNamespace(ct1=self.ct1.rows(0, 2), ct2=self.ct2.rows(0, 2), out=self.out.rows(0, 2),
-                                  graph=self.single[0])
-        return [a, b]
+        out = [types.SimpleNamespace(ct1=self.ct1.rows(0, 2), ct2=self.ct2.rows(0, 2), out=self.out.rows(0, 2),
+                                     graph=self.single[0])]
+        for _ in range(n - 1):
+            b = types.SimpleNamespace(ct1=R.allocate(2, self.r), ct2=R.allocate(2, self.r), out=R.allocate(2, self.r))
+            self.be.hal_assign(b.ct1, self.ct1.rows(0, 2))
+            self.be.hal_assign(b.ct2, self.ct2.rows(0, 2))
+            self.be.synchronize()
+            b.graph = halcuda.Graph(self.be, lambda b=b: R.hom_mul(T, b.ct1, b.ct2, self.base, self.rk, self.digits,
+                                                                   out=b.out))
+            b.graph.launch()  # the first replay uploads the graph; keep it out of the timed region
+            self.be.synchronize()
+            out.append(b)
+        return out
 
     def plain(self, b):
         """One ct-mult per call, the reference's calling pattern."""
@@ -443,18 +447,18 @@ def plain_calls(be, work, rounds, scratch):
     return per
 
 
-def e2e_steps(be, work, steps):
+def e2e_steps(be, work, steps, nslots=4):
     """One ct-mult per step through the C ABI with host buffers: step k copies pair k mod B's
-    operands from pinned host memory into one of two device slots, replays the slot's one-pair call
-    and copies the result back to pinned host memory, all inside the timed region. The two slots
-    alternate on two streams (double buffering), so one slot's copies overlap the other slot's
-    compute. Every copied-back result is checked against the resident run's."""
+    operands from pinned host memory into device slot k mod nslots, replays the slot's one-pair
+    call and copies the result back to pinned host memory, all inside the timed region. The slots
+    take turns on their own streams, so some slots' copies overlap the others' compute. Every
+    copied-back result is checked against the resident run's."""
     import halcuda
     import numpy as np
 
     R = work.ring
     full = (2 * work.batch, work.r, R.dl, R.dk)
-    slots = work.slots()
+    slots = work.slots(nslots)
     h1, h2, hout = halcuda.PinnedBuffer(full), halcuda.PinnedBuffer(full), halcuda.PinnedBuffer(full)
     h1.array[...] = work.ct1.to_numpy()
     h2.array[...] = work.ct2.to_numpy()
@@ -711,7 +715,7 @@ def main():
     p50, p99 = per[len(per) // 2], per[min(len(per) - 1, int(math.ceil(0.99 * len(per))) - 1)]
 
     e2e_n = max(args.steps, 40)  # at least 40 steps, so that the pipeline's fill and drain stay small
-    e2e_ms, h2d, d2h, _ = e2e_steps(be, work, e2e_n)
+    e2e_ms, h2d, d2h, _ = e2e_steps(be, work, e2e_n, args.e2e_slots)
     e2e_val = dist.world * e2e_n / (e2e_ms * 1e-3)
     roof = kernel_roofline(be, work.ring, work.base, 20, peaks)
     crt = None if args.no_crt_batch else crt_batch_bench(be, min(20, max(3, args.steps // 2)), args.warmup)
