@@ -580,8 +580,9 @@ __global__ void __launch_bounds__(THREADS, MINB) ntt_line_kernel(KView t, PlanPt
 
 /// [3, 64, 64] lines along dimension 3 as 3-CTA clusters: CTA `blk` of a cluster computes block
 /// blk (4096 residues) of one line.
+static_assert(sizeof(DevPlanHeader) % 16 == 0, "plan twiddle table must be 16-byte aligned");
 template <int MODE, bool FIX>
-__global__ void __cluster_dims__(3, 1, 1) __launch_bounds__(128, 5)
+__global__ void __cluster_dims__(3, 1, 1) __launch_bounds__(128, 6)
     ntt_line3_kernel(KView t, PlanPtrs plans, KView mul, KMods mods) {
     extern __shared__ int64_t smem[];
     const int64_t tile = blockIdx.x / 3;
@@ -589,10 +590,9 @@ __global__ void __cluster_dims__(3, 1, 1) __launch_bounds__(128, 5)
     const int64_t k = tile % t.n2, r = tile / t.n2;
     const int64_t j = r % t.n1, i = r / t.n1;
     const DevPlanHeader* P = plans.p[j];
-    int64_t* tws = smem + 4608;
-    stage_twiddles(P, tws);
-    __syncthreads();
-    const fast::Ctx c = make_ctx(P, tws);
+    // twiddles read from the plan in global memory (L1-cached): the CTA's shared memory holds only
+    // its 4096-residue block, so that six CTAs fit on an SM
+    const fast::Ctx c = make_ctx(P, reinterpret_cast<const int64_t*>(P + 1));
     int64_t* g = reinterpret_cast<int64_t*>(t.p) + i * t.s0 + j * t.s1 + k * t.s2;
     const int64_t* mulp = nullptr;
     int64_t me = 0, mn = 0, mi = 0;
@@ -703,7 +703,7 @@ hc_status launch_special(hc_context ctx, const KView& t, const PlanPtrs& pp, con
                          size_t smem, int64_t tiles, int ncb, const KView& src) {
     if constexpr (SHAPE == HC_SHAPE_L12288) {
         // one 3-CTA cluster per line: padded 4096-residue block + twiddles per CTA
-        const size_t smem3 = smem - ((size_t)line_tile_words(SHAPE) - 4608) * 8;
+        const size_t smem3 = 4608 * 8;
         auto kern = ntt_line3_kernel<MODE, FIX>;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3);
         if (e != cudaSuccess) return hc::cuda_check(e, "ntt smem attribute");
