@@ -40,3 +40,23 @@ def test_library_exports_every_declared_function():
     lib = ctypes.CDLL(path)
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
     assert not missing, missing
+
+
+def test_rust_binding_declares_only_exported_functions():
+    """The Rust `hal::cuda` module (include/hal_cuda.rs) binds only functions the C headers declare,
+    with the headers' parameter counts."""
+    text = open(os.path.join(ROOT, "include", "hal_cuda.rs")).read()
+    rust = {}
+    for m in re.finditer(r"fn (hc_\w+)\s*\(([^)]*)\)", text, flags=re.S):
+        params = [p for p in m.group(2).split(",") if p.strip()]
+        rust[m.group(1)] = len(params)
+    assert len(rust) >= 30
+    c = {}
+    for h in HEADERS:
+        src = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        for m in re.finditer(r"(hc_\w+)\s*\(([^;{]*?)\)\s*;", src, flags=re.S):
+            params = [p for p in m.group(2).split(",") if p.strip() and p.strip() != "void"]
+            c.setdefault(m.group(1), len(params))
+    for name, n in sorted(rust.items()):
+        assert name in c, name
+        assert c[name] == n, (name, c[name], n)
