@@ -563,10 +563,8 @@ __global__ void __launch_bounds__(THREADS, MINB) ntt_line_kernel(KView t, PlanPt
     const int64_t k = tile % t.n2, r = tile / t.n2;
     const int64_t j = r % t.n1, i = r / t.n1;
     const DevPlanHeader* P = plans.p[j];
-    int64_t* tws = smem + line_tile_words(SHAPE);
-    stage_twiddles(P, tws);
-    __syncthreads();
-    const fast::Ctx c = make_ctx(P, tws);
+    // twiddles read from the plan in global memory (L1-cached): shared memory holds only the line
+    const fast::Ctx c = make_ctx(P, reinterpret_cast<const int64_t*>(P + 1));
     int64_t* g = reinterpret_cast<int64_t*>(t.p) + i * t.s0 + j * t.s1 + k * t.s2;
     const int64_t* mulp = nullptr;
     int64_t me = 0, mn = 0, mi = 0;
@@ -663,7 +661,7 @@ __device__ __forceinline__ void run_column(const DevPlanHeader* P, const fast::C
 
 #define HC_COL_THREADS 256
 #ifndef HC_L3072_MIN_BLOCKS
-#define HC_L3072_MIN_BLOCKS 7  // resident CTAs per SM the 3072-residue line kernel's registers must allow (7 fit its shared memory)
+#define HC_L3072_MIN_BLOCKS 8  // resident CTAs per SM the 3072-residue line kernel's registers must allow (8 fit its shared memory)
 #endif
 #ifndef HC_COL12_MIN_BLOCKS
 #define HC_COL12_MIN_BLOCKS 4  // resident CTAs per SM the [4, 3] column kernel's registers must allow
@@ -1185,7 +1183,7 @@ hc_status launch_ntt(hc_context ctx, const KView& t, const hc_ntt_plan* plans, s
     bool fix = true;
     for (size_t j = 0; j < nplans; j++) fix = fix && plans[j]->fixed;
     if (dim == 3 && (shape == HC_SHAPE_L3072 || shape == HC_SHAPE_L12288)) {
-        const size_t smem = ((size_t)line_tile_words(shape) + 2 * (size_t)max_tw) * 8;
+        const size_t smem = ((size_t)line_tile_words(shape) + (shape == HC_SHAPE_L3072 ? 0 : 2 * (size_t)max_tw)) * 8;
         const int64_t tiles = t.n0 * t.n1 * t.n2;
         if (smem <= max_smem_optin(ctx) && tiles <= 0x7fffffff) {
             if (shape == HC_SHAPE_L3072)
