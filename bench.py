@@ -502,7 +502,7 @@ def e2e_steps(be, work, steps, nslots=4):
 NCU_TRAFFIC_BYTES = 30239232
 # Busy fraction of the integer multiply (fmaheavy, IMAD family) pipe over the same launch's elapsed
 # cycles, from the same capture: the bound the kernel actually sits against.
-NCU_IMAD_PIPE_FRAC = 0.638
+NCU_IMAD_PIPE_FRAC = 0.640
 
 
 def kernel_roofline(be, R, base, reps, peaks):
