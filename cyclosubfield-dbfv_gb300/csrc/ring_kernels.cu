@@ -228,7 +228,7 @@ __device__ __forceinline__ int64_t finish_wide(i128 acc, bool full, const KMods&
                 : red128(acc, m.n[j], m.ninv[j]);
 }
 
-__global__ void __launch_bounds__(256) keyswitch_kernel(KsArgs a, KMods m, const int64_t* one, int64_t lines,
+__global__ void __launch_bounds__(256) keyswitch1_kernel(KsArgs a, KMods m, const int64_t* one, int64_t lines,
                                                         int chunks) {
     const int64_t tiles = lines * chunks;
     for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
@@ -251,6 +251,46 @@ __global__ void __launch_bounds__(256) keyswitch_kernel(KsArgs a, KMods m, const
         if (a.has_add1) acc1 = (i128)((u128)acc1 + (u128)((i128)*kat<int64_t>(a.add1, i, j, sk, sl) * (i128)o));
         *kat<int64_t>(a.dst, 2 * i, j, k, l) = finish_wide(acc0, a.full0, m, (int)j);
         *kat<int64_t>(a.dst, 2 * i + 1, j, k, l) = finish_wide(acc1, a.full1, m, (int)j);
+    }
+}
+
+__global__ void __launch_bounds__(256) keyswitch_kernel(KsArgs a, KMods m, const int64_t* one, int64_t lines,
+                                                        int chunks) {
+    // two adjacent positions l, l + 1 per thread: the keys and the output are read and written as
+    // 16-byte pairs (dimension 3 is contiguous and even), the parts and summands gathered singly
+    const int64_t tiles = lines * chunks;
+    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        int64_t line = tile / chunks;  // (i, j, k)
+        int64_t l = 2 * ((tile - line * chunks) * blockDim.x + threadIdx.x);
+        if (l >= a.dst.n3) continue;
+        int64_t k = line % a.dst.n2, r = line / a.dst.n2;
+        int64_t j = r % a.dst.n1, i = r / a.dst.n1;
+        const int64_t sk = a.p2 ? (int64_t)a.p2[k] : k;
+        const int64_t sl0 = a.p3 ? (int64_t)a.p3[l] : l, sl1 = a.p3 ? (int64_t)a.p3[l + 1] : l + 1;
+        i128 acc00 = 0, acc01 = 0, acc10 = 0, acc11 = 0;  // acc<row><position>
+        for (int t = 0; t < a.nterms; t++) {
+            const int64_t x0 = *kat<int64_t>(a.parts[t], i, j, sk, sl0), x1 = *kat<int64_t>(a.parts[t], i, j, sk, sl1);
+            const longlong2 k0 = *reinterpret_cast<const longlong2*>(kat<int64_t>(a.keys[t], 0, j, k, l));
+            const longlong2 k1 = *reinterpret_cast<const longlong2*>(kat<int64_t>(a.keys[t], 1, j, k, l));
+            acc00 = (i128)((u128)acc00 + (u128)((i128)x0 * (i128)k0.x));
+            acc01 = (i128)((u128)acc01 + (u128)((i128)x1 * (i128)k0.y));
+            acc10 = (i128)((u128)acc10 + (u128)((i128)x0 * (i128)k1.x));
+            acc11 = (i128)((u128)acc11 + (u128)((i128)x1 * (i128)k1.y));
+        }
+        const int64_t o = one[j];
+        if (a.has_add0) {
+            acc00 = (i128)((u128)acc00 + (u128)((i128)*kat<int64_t>(a.add0, i, j, sk, sl0) * (i128)o));
+            acc01 = (i128)((u128)acc01 + (u128)((i128)*kat<int64_t>(a.add0, i, j, sk, sl1) * (i128)o));
+        }
+        if (a.has_add1) {
+            acc10 = (i128)((u128)acc10 + (u128)((i128)*kat<int64_t>(a.add1, i, j, sk, sl0) * (i128)o));
+            acc11 = (i128)((u128)acc11 + (u128)((i128)*kat<int64_t>(a.add1, i, j, sk, sl1) * (i128)o));
+        }
+        longlong2 w0, w1;
+        w0.x = finish_wide(acc00, a.full0, m, (int)j), w0.y = finish_wide(acc01, a.full0, m, (int)j);
+        w1.x = finish_wide(acc10, a.full1, m, (int)j), w1.y = finish_wide(acc11, a.full1, m, (int)j);
+        *reinterpret_cast<longlong2*>(kat<int64_t>(a.dst, 2 * i, j, k, l)) = w0;
+        *reinterpret_cast<longlong2*>(kat<int64_t>(a.dst, 2 * i + 1, j, k, l)) = w1;
     }
 }
 
@@ -426,9 +466,21 @@ hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys
     a.batch = dst.n0 / 2;
     int64_t lines = a.batch * dst.n1 * dst.n2;
     if (lines == 0 || dst.n3 == 0) return HC_OK;
+    // the paired kernel needs an even dimension 3 and 16-byte aligned key and output rows
+    auto aligned = [](const KView& v) {
+        return ((uintptr_t)v.p % 16) == 0 && v.s0 % 2 == 0 && v.s1 % 2 == 0 && v.s2 % 2 == 0 && !v.b3;
+    };
+    bool pair = dst.n3 % 2 == 0 && aligned(dst);
+    for (int t = 0; t < nterms; t++) pair = pair && aligned(keys[t]);
     int chunks;
     unsigned blocks;
-    grid_lines(ctx, dst.n3, lines, &chunks, &blocks);
+    if (!pair) {
+        grid_lines(ctx, dst.n3, lines, &chunks, &blocks);
+        keyswitch1_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(a, m, one_dev, lines, chunks);
+        count_launch(ctx);
+        return cuda_check(cudaGetLastError(), "keyswitch kernel launch");
+    }
+    grid_lines(ctx, dst.n3 / 2, lines, &chunks, &blocks);
     keyswitch_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(a, m, one_dev, lines, chunks);
     count_launch(ctx);
     return cuda_check(cudaGetLastError(), "keyswitch kernel launch");
