@@ -257,14 +257,16 @@ __global__ void __launch_bounds__(256) keyswitch1_kernel(KsArgs a, KMods m, cons
 __global__ void __launch_bounds__(256) keyswitch_kernel(KsArgs a, KMods m, const int64_t* one, int64_t lines,
                                                         int chunks) {
     // two adjacent positions l, l + 1 per thread: the keys and the output are read and written as
-    // 16-byte pairs (dimension 3 is contiguous and even), the parts and summands gathered singly
+    // 16-byte pairs (dimension 3 is contiguous and even), the parts and summands gathered singly.
+    // Tiles run as ((j, k), chunk, i) with the ciphertext index innermost: the B tiles that read
+    // one block of the key are adjacent, so the key comes from DRAM once and B - 1 reads hit L2.
     const int64_t tiles = lines * chunks;
     for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        int64_t line = tile / chunks;  // (i, j, k)
-        int64_t l = 2 * ((tile - line * chunks) * blockDim.x + threadIdx.x);
+        const int64_t i = tile % a.batch, u = tile / a.batch;
+        const int64_t line = u / chunks;  // (j, k)
+        const int64_t l = 2 * ((u - line * chunks) * blockDim.x + threadIdx.x);
         if (l >= a.dst.n3) continue;
-        int64_t k = line % a.dst.n2, r = line / a.dst.n2;
-        int64_t j = r % a.dst.n1, i = r / a.dst.n1;
+        const int64_t k = line % a.dst.n2, j = line / a.dst.n2;
         const int64_t sk = a.p2 ? (int64_t)a.p2[k] : k;
         const int64_t sl0 = a.p3 ? (int64_t)a.p3[l] : l, sl1 = a.p3 ? (int64_t)a.p3[l + 1] : l + 1;
         i128 acc00 = 0, acc01 = 0, acc10 = 0, acc11 = 0;  // acc<row><position>
