@@ -539,7 +539,8 @@ using FixedSched = fast::FixSched<INV ? fixed_masks(SHAPE).ired : fixed_masks(SH
                                   INV ? 0u : fixed_masks(SHAPE).fskip,
                                   INV ? fixed_masks(SHAPE).ilast : fixed_masks(SHAPE).flast>;
 
-/// One specialised line (twiddles staged, barrier passed); FIX: the plan has the fixed schedule.
+/// One specialised line g of plan P through the CTA's shared-memory line buffer s; FIX: the plan
+/// has the fixed schedule.
 template <int SHAPE, int MODE, bool FIX>
 __device__ __forceinline__ void run_line(const DevPlanHeader* P, const fast::Ctx& c, int64_t* s, int64_t* g,
                                          const int64_t* mulp, int64_t me, int64_t mn, int64_t mi) {
@@ -610,9 +611,8 @@ __global__ void __cluster_dims__(3, 1, 1) __launch_bounds__(128, 6)
     }
 }
 
-/// One specialised column (global element stride ge) of shape SHAPE, in registers.
-/// One column g[0], g[ge], ... transformed in registers; it is read from gs[0], gs[gse], ... (g
-/// itself for an in-place call).
+/// One specialised column g[0], g[ge], ... of shape SHAPE transformed in registers; it is read
+/// from gs[0], gs[gse], ... (g itself for an in-place call).
 template <int SHAPE, int MODE, bool FIX>
 __device__ __forceinline__ void run_column(const DevPlanHeader* P, const fast::Ctx& c, int64_t* g, int64_t ge,
                                            const int64_t* gs, int64_t gse, const int64_t* mulp, int64_t mstride,
