@@ -296,17 +296,40 @@ __global__ void __launch_bounds__(256) keyswitch_kernel(KsArgs a, KMods m, const
     }
 }
 
+/// W consecutive words at p (W = 2: one 16-byte access; p must be 16-byte aligned).
+template <int W>
+__device__ __forceinline__ void load_words(const int64_t* p, int64_t (&v)[W]) {
+    if constexpr (W == 2) {
+        const longlong2 t = *reinterpret_cast<const longlong2*>(p);
+        v[0] = t.x, v[1] = t.y;
+    } else {
+        v[0] = *p;
+    }
+}
+template <int W>
+__device__ __forceinline__ void store_words(int64_t* p, const int64_t (&v)[W]) {
+    if constexpr (W == 2) {
+        longlong2 t;
+        t.x = v[0], t.y = v[1];
+        *reinterpret_cast<longlong2*>(p) = t;
+    } else {
+        *p = v[0];
+    }
+}
+
 /// (l0 r0, l0 r1 + l1 r0, l1 r1) of B pairs of 2-row ciphertext tensors ([2B, ...] each),
 /// reduced per row into [3B, ...]: rows 2i and 2i + 1 receive the first two components of pair i,
 /// row 2B + i the third. Each operand comes in two parts along the RNS dimension: rows j < rsplit
-/// from *_lo, rows j >= rsplit from *_hi (row j - rsplit).
+/// from *_lo, rows j >= rsplit from *_hi (row j - rsplit). W adjacent positions per thread (W = 2
+/// needs an even dimension 3 and 16-byte aligned rows in every view).
+template <int W>
 __global__ void __launch_bounds__(256) tensor_kernel(KView d, KView lhs_lo, KView lhs_hi, KView rhs_lo, KView rhs_hi,
                                                      int rsplit, KMods m, int full0, int full1, int full2,
                                                      int64_t lines, int chunks) {
     const int64_t tiles = lines * chunks;
     for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         int64_t line = tile / chunks;  // (i, j, k)
-        int64_t l = (tile - line * chunks) * blockDim.x + threadIdx.x;
+        int64_t l = W * ((tile - line * chunks) * blockDim.x + threadIdx.x);
         if (l >= d.n3) continue;
         int64_t k = line % d.n2, r = line / d.n2;
         int64_t j = r % d.n1, i = r / d.n1;
@@ -315,15 +338,22 @@ __global__ void __launch_bounds__(256) tensor_kernel(KView d, KView lhs_lo, KVie
         const int64_t* lp = lo ? kat<int64_t>(lhs_lo, 2 * i, js, k, l) : kat<int64_t>(lhs_hi, 2 * i, js, k, l);
         const int64_t* rp = lo ? kat<int64_t>(rhs_lo, 2 * i, js, k, l) : kat<int64_t>(rhs_hi, 2 * i, js, k, l);
         const int64_t ls = lo ? lhs_lo.s0 : lhs_hi.s0, rs = lo ? rhs_lo.s0 : rhs_hi.s0;
-        int64_t l0 = lp[0], l1 = lp[ls];
-        int64_t r0 = rp[0], r1 = rp[rs];
-        i128 a0 = (i128)l0 * (i128)r0;
-        i128 a1 = (i128)((u128)((i128)l0 * (i128)r1) + (u128)((i128)l1 * (i128)r0));
-        i128 a2 = (i128)l1 * (i128)r1;
+        int64_t l0[W], l1[W], r0[W], r1[W], o0[W], o1[W], o2[W];
+        load_words<W>(lp, l0), load_words<W>(lp + ls, l1);
+        load_words<W>(rp, r0), load_words<W>(rp + rs, r1);
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+            const i128 a0 = (i128)l0[w] * (i128)r0[w];
+            const i128 a1 = (i128)((u128)((i128)l0[w] * (i128)r1[w]) + (u128)((i128)l1[w] * (i128)r0[w]));
+            const i128 a2 = (i128)l1[w] * (i128)r1[w];
+            o0[w] = finish_wide(a0, full0, m, (int)j);
+            o1[w] = finish_wide(a1, full1, m, (int)j);
+            o2[w] = finish_wide(a2, full2, m, (int)j);
+        }
         const int64_t B = d.n0 / 3;
-        *kat<int64_t>(d, 2 * i, j, k, l) = finish_wide(a0, full0, m, (int)j);
-        *kat<int64_t>(d, 2 * i + 1, j, k, l) = finish_wide(a1, full1, m, (int)j);
-        *kat<int64_t>(d, 2 * B + i, j, k, l) = finish_wide(a2, full2, m, (int)j);
+        store_words<W>(kat<int64_t>(d, 2 * i, j, k, l), o0);
+        store_words<W>(kat<int64_t>(d, 2 * i + 1, j, k, l), o1);
+        store_words<W>(kat<int64_t>(d, 2 * B + i, j, k, l), o2);
     }
 }
 
@@ -526,11 +556,23 @@ hc_status launch_tensor(hc_context ctx, const KView& d, const KView& lhs_lo, con
                         const KView& rhs_hi, int rsplit, const KMods& m, int f0, int f1, int f2) {
     int64_t lines = (d.n0 / 3) * d.n1 * d.n2;
     if (lines == 0 || d.n3 == 0) return HC_OK;
+    // two adjacent positions per thread where every view allows 16-byte accesses
+    auto aligned = [](const KView& v) {
+        return ((uintptr_t)v.p % 16) == 0 && v.s0 % 2 == 0 && v.s1 % 2 == 0 && v.s2 % 2 == 0 && !v.b3;
+    };
+    const bool pair = d.n3 % 2 == 0 && aligned(d) && aligned(lhs_lo) && aligned(lhs_hi) && aligned(rhs_lo) &&
+                      aligned(rhs_hi);
     int chunks;
     unsigned blocks;
-    grid_lines(ctx, d.n3, lines, &chunks, &blocks);
-    tensor_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(d, lhs_lo, lhs_hi, rhs_lo, rhs_hi, rsplit, m, f0, f1, f2, lines,
-                                                       chunks);
+    if (pair) {
+        grid_lines(ctx, d.n3 / 2, lines, &chunks, &blocks);
+        tensor_kernel<2><<<blocks, 256, 0, stream_of(ctx)>>>(d, lhs_lo, lhs_hi, rhs_lo, rhs_hi, rsplit, m, f0, f1, f2,
+                                                              lines, chunks);
+    } else {
+        grid_lines(ctx, d.n3, lines, &chunks, &blocks);
+        tensor_kernel<1><<<blocks, 256, 0, stream_of(ctx)>>>(d, lhs_lo, lhs_hi, rhs_lo, rhs_hi, rsplit, m, f0, f1, f2,
+                                                              lines, chunks);
+    }
     count_launch(ctx);
     return cuda_check(cudaGetLastError(), "tensor kernel launch");
 }

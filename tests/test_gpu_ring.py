@@ -313,6 +313,45 @@ def test_hom_mul_batched_full_size_matches_oracle(po, be):
         assert (got[2 * b:2 * b + 2] == exp).all(), b
 
 
+def word_offset(be, arr):
+    """`arr` in a view whose rows start one word into a wider buffer: 8-byte aligned only, with an
+    odd dimension-2 stride, so no 16-byte access fits it."""
+    n0, n1, n2, n3 = arr.shape
+    buf = be.hal_allocate_i64((n0, n1, n2, n3 + 1))
+    return buf.slice(None, None, None, (1, n3 + 1)).copy_from(arr)
+
+
+@pytest.mark.parametrize("name", ["field_18", "field_36864"])
+def test_unaligned_views_match_oracle(rings, name, po, be):
+    """Operands and keys in views that admit no 16-byte access (the one-position forms of the key
+    switch and the tensor product) give the oracle's hom_mul, key switch and hom_gal."""
+    o, d = rings(name)
+    base = o.initial_base()
+    la = o.log2_alpha_for_sigma(base, 3.2)
+    st = [29]
+    sk, sk2 = o.gen_sk(st), o.gen_sk(st)
+    digits = po_digits(len(base) if len(base) < 8 else len(base) // 4, len(base))
+    ct1 = o.enc(st, base, 16, [i % 16 for i in range(o.n)], sk, la)
+    ct2 = o.enc(st, base, 16, [(3 * i + 1) % 16 for i in range(o.n)], sk, la)
+    rk = o.gen_rk(st, sk, digits, la)
+    exp = o.hom_mul(16, ct1, ct2, base, rk, digits)
+    got = d.hom_mul(16, word_offset(be, ct1), word_offset(be, ct2), base,
+                    word_offset(be, rk.reshape((-1,) + rk.shape[2:])), digits).to_numpy()
+    assert (got == exp).all()
+    ksk = o.gen_ksk(st, base, sk, sk2, digits, la)
+    c1 = o.crt_to_pb(ct1[1:2], base)
+    exp_k = o.key_switch(ct1[0:1], c1, base, ksk, digits)
+    got_k = d.key_switch(d.tensor(ct1[0:1]), d.tensor(c1), base, word_offset(be, ksk.reshape((-1,) + ksk.shape[2:])),
+                         digits).to_numpy()
+    assert (got_k == exp_k).all()
+    g = list(o.info["gens"])[0]
+    gk = o.gen_gk(st, sk, g, digits, la)
+    exp_g = o.hom_gal(ct2, base, [g], gk[None], digits)[0]
+    got_g = d.hom_gal_batch(d.tensor(ct2), base, g, word_offset(be, gk.reshape((-1,) + gk.shape[2:])),
+                            digits).to_numpy()
+    assert (got_g == exp_g).all()
+
+
 def test_graph_replay_matches(po, be):
     """A captured hom_mul replayed from a CUDA graph reproduces the direct result."""
     import halcuda
