@@ -581,7 +581,8 @@ def cpu_baseline(seconds_budget=12.0):
         if el > seconds_budget:
             break
     return {"value": round(n / el, 4), "unit": "ct-mults/s", "cores": 1, "kind": "port",
-            "sample": "%d bfv_hom_mul on %s r=%d (oracle C++ restatement of hal::cpu, 1 thread, %.1f s)"
+            "sample": "%d bfv_hom_mul on %s r=%d (oracle C++ restatement of hal::cpu, g++ -O3 without CPU "
+                      "tuning, 1 thread, %.1f s)"
                       % (n, FIELD, len(base), el)}
 
 
@@ -644,7 +645,8 @@ def reference_arm(args, dist):
                                    % (FIELD, cores), "field": FIELD, "rns_len": 16},
             "cpu_baseline": {"value": round(value, 4), "unit": "ct-mults/s", "cores": cores, "kind": "port",
                              "sample": "%d ct-mults per step on %d processes; oracle C++ restatement of the "
-                                       "reference's hal::cpu path (the Rust crate is not buildable here)"
+                                       "reference's hal::cpu path, g++ -O3 without CPU tuning (the Rust crate is not "
+                                       "buildable here)"
                                        % (cores, cores)},
             "e2e": {"value": round(value, 4), "unit": "ct-mults/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}

@@ -2,10 +2,10 @@
 
 Compiles the C++ restatement of the reference's CPU backend, ring and BFV layers into
 ``oracle/_build/liboracle.so``. It is single-threaded and optimised like the reference's release
-profile (``-O3``, native CPU tuning), so it doubles as the timed CPU baseline.
+profile (``-O3``, no CPU-specific tuning, as a Cargo release build sets no target CPU), so it
+doubles as the timed CPU baseline; the same flags build it on x86-64 and on aarch64.
 """
 import os
-import platform
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -13,11 +13,6 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD_DIR, "liboracle.so")
 SOURCES = ["capi.cpp"]
 HEADERS = ["arith.hpp", "ntt.hpp", "cpu_backend.hpp", "field.hpp", "ring.hpp", "bfv.hpp"]
-
-
-def _native_flag():
-    # x86 takes -march, aarch64 (the Grace host) takes -mcpu
-    return "-mcpu=native" if platform.machine() in ("aarch64", "arm64") else "-march=native"
 
 
 def build(force=False):
@@ -28,7 +23,7 @@ def build(force=False):
         if all(os.path.getmtime(d) <= lib_mtime for d in deps):
             return LIB
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = ["g++", "-O3", _native_flag(), "-std=c++17", "-shared", "-fPIC", "-o", tmp] + [
+    cmd = ["g++", "-O3", "-std=c++17", "-shared", "-fPIC", "-o", tmp] + [
         os.path.join(HERE, s) for s in SOURCES
     ]
     subprocess.check_call(cmd)
