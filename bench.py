@@ -496,24 +496,24 @@ def e2e_steps(be, work, steps, nslots=4):
     return ms, 2 * nbytes, nbytes, hout
 
 
-# DRAM bytes (read + written) of one launch of that kernel on that tensor, from an ncu capture of
-# `python bench.py --roofline-only` (profiles/ntt_line_kernel_intt_dim3_field36864_r34.md): the
-# tensor is read once; its writes stay in L2 during the launch.
-NCU_TRAFFIC_BYTES = 30239232
-# Busy fraction of the integer multiply (fmaheavy, IMAD family) pipe over the same launch's elapsed
-# cycles, from the same capture: the bound the kernel actually sits against.
-NCU_IMAD_PIPE_FRAC = 0.640
+# DRAM bytes (read + written) of one launch of that kernel on the [24, 34, 12, 3072] tensor, and
+# the busy fraction of the integer multiply (fmaheavy, IMAD family) pipe over its elapsed cycles,
+# from one ncu capture of `python bench.py --roofline-only` (None: not captured for this build).
+NCU_TRAFFIC_BYTES = None
+NCU_IMAD_PIPE_FRAC = None
+ROOF_ROWS = 24  # ciphertext rows of the roofline tensor: 240 MB, larger than L2
 
 
 def kernel_roofline(be, R, base, reps, peaks):
     """Dominant kernel: the dimension-3 lazy NTT of the transforms (one HAL launch of the
-    specialised [2, 3, 8, 64] line kernel), timed alone on the lifted-product tensor of one
-    ct-mult [3, r + e, 12, 3072]. Algorithmic bytes per launch: one read and one write of every
-    i64 residue (16 B per residue)."""
+    specialised [2, 3, 8, 64] line kernel), timed alone on a [24, r + e, 12, 3072] tensor of
+    lifted products (eight ct-mults' worth, 240 MB: larger than L2, so every launch reads and
+    writes HBM). Algorithmic bytes per launch: one read and one write of every i64 residue
+    (16 B per residue)."""
     import halcuda
 
     lifted = base + R.extension_base(base)
-    t = R.allocate(3, len(lifted))
+    t = R.allocate(ROOF_ROWS, len(lifted))
     plans = [R_plan for R_plan in _k_plans(R, lifted)]
     ev0, ev1 = halcuda.Event(), halcuda.Event()
     for _ in range(3):
@@ -524,23 +524,25 @@ def kernel_roofline(be, R, base, reps, peaks):
         be.hal_intt_mont64_dim(t, plans, halcuda.DIM3)
     ev1.record(be)
     ms = ev0.elapsed_ms(ev1) / reps
-    bytes_alg = 16 * 3 * len(lifted) * R.n
+    bytes_alg = 16 * ROOF_ROWS * len(lifted) * R.n
     achieved = bytes_alg / (ms * 1e-3) / 1e9
     peak = peaks.get("hbm_gbs")
     # the binding roof: Barrett products. The pass's algorithmic count is 7 per residue (ten radix-2
     # stages at 1/2 and one radix-3 stage at 2, the reference's formula), against the GPU's
     # measured rate of the same product in a register-only kernel
-    products = 7 * 3 * len(lifted) * R.n
+    products = 7 * ROOF_ROWS * len(lifted) * R.n
     bpeak = halcuda.barrett_peak(be)
     int_roof = {"bound": "int (exact 64-bit Barrett products)", "achieved": round(products / (ms * 1e-3) / 1e9, 1),
                 "peak": round(bpeak / 1e9, 1), "unit": "G products/s",
                 "frac": round(products / (ms * 1e-3) / bpeak, 4), "products_per_launch": products,
                 "peak_source": "measured here: register-only kernel of the same product (hc_barrett_peak)"}
-    return {"kernel": "ntt_line_kernel (inverse, dim 3, lines [2, 3, 8, 64], tensor [3, %d, 12, 3072])" % len(lifted),
+    return {"kernel": "ntt_line_kernel (inverse, dim 3, lines [2, 3, 8, 64], tensor [%d, %d, 12, 3072])"
+                      % (ROOF_ROWS, len(lifted)),
             "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4) if peak else None,
             "traffic": NCU_TRAFFIC_BYTES if len(lifted) == 34 else None,
             "bytes_per_launch": bytes_alg, "launch_ms": round(ms, 5),
+            "l2": "tensor of %d MB, larger than L2" % (bytes_alg // 2 // 2**20),
             "peak_source": "measured" if not peaks.get("fallback") else "fallback",
             "int_pipe": {"pipe": "fmaheavy (IMAD)", "busy_frac_of_elapsed": NCU_IMAD_PIPE_FRAC,
                          "source": "ncu capture of the same launch (--roofline-only)"},

@@ -1,6 +1,7 @@
 // The C ABI of include/halcuda.h, part 1: contexts, device tensors and the Backend methods.
 // Host-side argument checks mirror the assertions of the reference implementation
 // (cyclosubfield-dbfv/src/hal/cpu.rs) and turn them into status codes.
+#include <atomic>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -36,6 +37,9 @@ hc_status cuda_check(cudaError_t e, const char* what) {
                 std::string(what) + ": " + cudaGetErrorString(e));
 }
 cudaStream_t stream_of(hc_context ctx) { return ctx->stream; }
+static std::atomic<uint64_t> g_alloc_calls{0};
+void count_alloc() { g_alloc_calls.fetch_add(1, std::memory_order_relaxed); }
+uint64_t alloc_calls() { return g_alloc_calls.load(std::memory_order_relaxed); }
 void count_launch(hc_context ctx, uint64_t n) { ctx->launches += n; }
 uint64_t launch_counter(hc_context ctx) { return ctx->launches; }
 int num_sms(hc_context ctx) { return ctx->sms; }
@@ -201,6 +205,7 @@ hc_status transfer(hc_context ctx, const hc_view& v, void* host, size_t len, boo
     }
     // strided view: stage contiguously on the device and scatter / gather with a copy kernel
     void* tmp = nullptr;
+    count_alloc();
     if ((st = cuda_check(cudaMallocAsync(&tmp, bytes, s), "staging allocation"))) return st;
     hc_view tv = contiguous_view(tmp, v.shape);
     int op = esize == 16 ? OP_ASSIGN_I128 : OP_ASSIGN;
@@ -227,6 +232,7 @@ hc_status alloc(hc_context ctx, const int64_t shape[4], size_t esize, void** out
     size_t bytes = n * esize;
     *out = nullptr;
     if (bytes == 0) bytes = 16;
+    count_alloc();
     hc_status st = cuda_check(cudaMallocAsync(out, bytes, ctx->stream), "device allocation");
     if (st) return st;
     return cuda_check(cudaMemsetAsync(*out, 0, bytes, ctx->stream), "zero fill");
@@ -546,6 +552,7 @@ hc_status hc_create_permutation(hc_context ctx, const size_t* inner_shape, const
     auto* p = new hc_perm_plan_s();
     p->len = n;
     p->dev = nullptr;
+    count_alloc();
     hc_status st = cuda_check(cudaMalloc(&p->dev, n * sizeof(uint32_t) + 4), "permutation allocation");
     if (!st) st = cuda_check(cudaMemcpy(p->dev, perm.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice), "upload");
     if (st) {

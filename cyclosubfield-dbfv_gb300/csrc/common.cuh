@@ -197,6 +197,9 @@ hc_status fail(hc_status st, const std::string& msg);
 hc_status cuda_check(cudaError_t e, const char* what);
 cudaStream_t stream_of(hc_context ctx);
 void count_launch(hc_context ctx, uint64_t n = 1);
+/// Every device or pinned-host allocation call of the library counts itself (hc_memory_stats).
+void count_alloc();
+uint64_t alloc_calls();
 int num_sms(hc_context ctx);
 size_t max_smem_optin(hc_context ctx);
 int device_of(hc_context ctx);

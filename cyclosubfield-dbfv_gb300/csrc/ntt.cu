@@ -1069,6 +1069,7 @@ hc_status build_plan(hc_context ctx, const hc_modulus* m, const size_t* shape, s
     std::memcpy(blob.data(), &hp.h, sizeof(DevPlanHeader));
     if (!hp.tw.empty()) std::memcpy(blob.data() + sizeof(DevPlanHeader), hp.tw.data(), hp.tw.size() * sizeof(int64_t));
     void* dev = nullptr;
+    count_alloc();
     if (cudaMalloc(&dev, bytes) != cudaSuccess) return fail(HC_ERR_OOM, "cannot allocate NTT plan");
     hc_status st = cuda_check(cudaMemcpy(dev, blob.data(), bytes, cudaMemcpyHostToDevice), "plan upload");
     if (st != HC_OK) {

@@ -40,6 +40,7 @@ hc_status hc_barrett_peak(hc_context ctx, double* products_per_s) {
     const size_t words = (size_t)blocks * PEAK_THREADS;
     cudaStream_t s = stream_of(ctx);
     int64_t* out = nullptr;
+    count_alloc();
     hc_status st = cuda_check(cudaMallocAsync((void**)&out, words * 8, s), "peak buffer");
     if (st) return st;
     cudaEvent_t e0 = nullptr, e1 = nullptr;

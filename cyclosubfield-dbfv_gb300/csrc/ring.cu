@@ -334,6 +334,7 @@ struct DBuf {
     void* p = nullptr;
     DBuf() {}
     DBuf(hc_context c, size_t bytes) : ctx(c) {
+        count_alloc();
         CK(cuda_check(cudaMallocAsync(&p, bytes ? bytes : 16, stream_of(c)), "ring buffer allocation"));
     }
     DBuf(hc_context c, const void* host, size_t bytes) : DBuf(c, bytes) {
@@ -371,6 +372,7 @@ struct Tensor {
             CK(w ? hc_allocate_i128(c, shape, &buf.p) : hc_allocate_i64(c, shape, &buf.p));
         } else {
             size_t bytes = (size_t)(a * b * cc * d) * (w ? 16 : 8);
+            count_alloc();
             CK(cuda_check(cudaMallocAsync(&buf.p, bytes ? bytes : 16, stream_of(c)), "temporary allocation"));
         }
         buf.ctx = c;
@@ -1191,6 +1193,16 @@ Tensor gadget_decompose(hc_ring R, const hc_view& c_pb, const Base& base, const 
     return parts;
 }
 
+/// A key-switching key for `nd` gadget digits over the first r factors: [>= 2 nd, >= r, deg_L',
+/// deg_K], dimension 3 contiguous (the kernel reads every key block through these strides).
+void check_keys(hc_ring R, const hc_view& keys, int64_t r, size_t nd) {
+    REQUIRE(keys.shape[1] >= r && keys.shape[0] >= 2 * (int64_t)nd, HC_ERR_SHAPE, "key tensor too small");
+    REQUIRE(keys.shape[2] == R->dl() && keys.shape[3] == R->dk(), HC_ERR_SHAPE,
+            "key tensor: dimensions 2 and 3 must be the ring's deg_L' and deg_K");
+    REQUIRE(keys.strides[3] == 1 || R->dk() <= 1, HC_ERR_SHAPE, "key tensor: dimension 3 must be contiguous");
+    REQUIRE(keys.ptr, HC_ERR_ARG, "key tensor: null data");
+}
+
 /// acc[0..2] = sum_t parts[t] * key_t (+ summands through mont(1)), reduced (fused), for B
 /// ciphertexts at once: parts [B d, r] (row i d + t), summand views with one row per ciphertext,
 /// out [2B, r] (rows 2i, 2i + 1).
@@ -1198,8 +1210,11 @@ void keyswitch(hc_ring R, const hc_view& parts, const hc_view& keys, const Base&
                const hc_view* add0, const hc_view* add1, const hc_view& out, const uint32_t* p2 = nullptr,
                const uint32_t* p3 = nullptr) {
     const int64_t r = (int64_t)base.size(), B = out.shape[0] / 2;
-    REQUIRE(keys.shape[1] >= r && keys.shape[0] >= 2 * (int64_t)nd, HC_ERR_SHAPE, "key tensor too small");
+    check_keys(R, keys, r, nd);
     REQUIRE(parts.shape[0] == B * (int64_t)nd, HC_ERR_SHAPE, "gadget digits per ciphertext");
+    // the summands have one row per ciphertext over the base, in the ring's shape
+    if (add0) check_view(*add0, B, r, R->dl(), R->dk(), "key switch summand c0");
+    if (add1) check_view(*add1, B, r, R->dl(), R->dk(), "key switch summand c1");
     std::vector<KView> pv, kvv;
     u128 mp = (u128)R->max_p(base), step = 0;
     for (size_t t = 0; t < nd; t++) {
@@ -1535,7 +1550,10 @@ hc_status hc_bfv_key_switch(hc_ring R, hc_view c0, hc_view c1_pb, const size_t* 
         REQUIRE(R, HC_ERR_ARG, "null ring");
         Base b = base_of(base, r);
         check_view(out, 2, (int64_t)r, R->dl(), R->dk(), "key switch output");
+        check_view(c0, 1, (int64_t)r, R->dl(), R->dk(), "key switch c0");
+        check_view(c1_pb, 1, (int64_t)r, R->dl(), R->dk(), "key switch c1");
         Digits dg = clip(digits_of(digits, d), r);
+        check_keys(R, keys, (int64_t)r, dg.size());
         Tensor parts = gadget_decompose(R, c1_pb, b, dg);
         keyswitch(R, parts.view(), keys, b, dg.size(), &c0, nullptr, out);
     });
@@ -1725,7 +1743,9 @@ std::mutex ks_noalloc_mu;
 std::map<int, int64_t*> ks_noalloc_addr;  // device ordinal -> address of the scratch array there
 
 /// Address of the scratch array on `device`, looked up on the first call for that device with
-/// the device made current for the lookup (and the caller's current device restored).
+/// the device made current for the lookup (and the caller's current device restored). It is kept
+/// for the life of the process; a device reset would leave it stale, like every other device
+/// object of the library, which is why no call may follow a reset.
 int64_t* ks_noalloc_scratch(int device) {
     std::lock_guard<std::mutex> lock(ks_noalloc_mu);
     auto it = ks_noalloc_addr.find(device);
@@ -1759,16 +1779,19 @@ extern "C" hc_status hc_bfv_key_switch_noalloc(hc_ring R, hc_view c0, hc_view c1
         REQUIRE(R, HC_ERR_ARG, "null ring");
         Base b = base_of(base, r);
         check_view(out, 2, (int64_t)r, R->dl(), R->dk(), "key switch output");
+        check_view(c0, 1, (int64_t)r, R->dl(), R->dk(), "key switch c0");
         check_view(c1_pb, 1, (int64_t)r, R->dl(), R->dk(), "key switch c1");
         Digits dg = clip(digits_of(digits, d), r);
         REQUIRE(!dg.empty(), HC_ERR_ARG, "at least one gadget digit required");
+        check_keys(R, keys, (int64_t)r, dg.size());
         const size_t words = dg.size() * r * (size_t)R->dl() * (size_t)R->dk();
         REQUIRE(words <= HC_KS_NOALLOC_WORDS, HC_ERR_UNSUPPORTED,
                 "no-allocation key switch: digits x RNS factors x ring degree = " + std::to_string(words) +
                     " exceeds the scratch array of " + std::to_string(HC_KS_NOALLOC_WORDS) + " words (32 MiB)");
         REQUIRE(ks_tables_ready(R, b, dg), HC_ERR_ARG,
-                "no-allocation key switch: the ring has no tables for this base and digit split yet; one "
-                "hc_bfv_key_switch call with the same base and digits builds them");
+                "no-allocation key switch: the ring has no tables for this base and digit split yet; any "
+                "key-switching call with this base and digit split (hc_bfv_key_switch, the relinearisation of "
+                "hc_bfv_hom_mul, hc_bfv_hom_gal) builds them");
         int64_t* scratch = ks_noalloc_scratch(device_of(R->ctx));
         hc_view parts;
         parts.ptr = scratch;
@@ -2195,6 +2218,7 @@ hc_status hc_keyset_add(hc_keyset ks, uint64_t g, hc_view key) {
             CK(cuda_check(cudaMemcpyAsync(e.dev.p, key.ptr, ks->key_bytes(), cudaMemcpyDeviceToDevice, st), "key copy"));
             ks->resident_bytes += ks->key_bytes();
         } else {
+            count_alloc();
             CK(cuda_check(cudaMallocHost(&e.host, ks->key_bytes()), "pinned key allocation"));
             CK(cuda_check(cudaMemcpyAsync(e.host, key.ptr, ks->key_bytes(), cudaMemcpyDeviceToHost, st), "key copy"));
             CK(cuda_check(cudaStreamSynchronize(st), "key copy"));

@@ -25,6 +25,7 @@ extern "C" {
 
 hc_status hc_host_alloc(size_t bytes, void** out) {
     if (!out) return fail(HC_ERR_ARG, "null output");
+    count_alloc();
     return cuda_check(cudaHostAlloc(out, bytes ? bytes : 16, cudaHostAllocDefault), "pinned host allocation");
 }
 
@@ -161,6 +162,27 @@ hc_status hc_graph_destroy(hc_graph graph) {
 hc_status hc_device_memory(hc_context ctx, size_t* free_bytes, size_t* total_bytes) {
     if (!ctx || !free_bytes || !total_bytes) return fail(HC_ERR_ARG, "null argument");
     return cuda_check(cudaMemGetInfo(free_bytes, total_bytes), "memory query");
+}
+
+hc_status hc_memory_stats(hc_context ctx, int reset_high, uint64_t out[3]) {
+    if (!ctx || !out) return fail(HC_ERR_ARG, "null argument");
+    cudaMemPool_t pool;
+    hc_status st = cuda_check(cudaDeviceGetDefaultMemPool(&pool, device_of(ctx)), "default memory pool");
+    if (st) return st;
+    unsigned long long used = 0, high = 0;  // the pool attributes are 64-bit unsigned
+    if (reset_high) {
+        unsigned long long zero = 0;  // resets the high-water mark to the bytes in use now
+        if ((st = cuda_check(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero), "pool high-water reset")))
+            return st;
+    }
+    if ((st = cuda_check(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used), "pool use")))
+        return st;
+    if ((st = cuda_check(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &high), "pool high-water")))
+        return st;
+    out[0] = alloc_calls();
+    out[1] = used;
+    out[2] = high;
+    return HC_OK;
 }
 
 }  // extern "C"

@@ -482,6 +482,14 @@ def device_memory(be):
     return int(f.value), int(t.value)
 
 
+def memory_stats(be, reset_high=False):
+    """(allocation calls made by the library so far, bytes in use in the device's default memory
+    pool, that pool's high-water mark); `reset_high` first resets the mark to the bytes in use."""
+    out = (ctypes.c_uint64 * 3)()
+    check(lib().hc_memory_stats(be.h, ctypes.c_int(1 if reset_high else 0), out))
+    return int(out[0]), int(out[1]), int(out[2])
+
+
 class Graph:
     """A captured sequence of calls (hc_graph_*), replayed with launch()."""
 

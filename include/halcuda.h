@@ -193,6 +193,12 @@ hc_status hc_event_query(hc_event ev, int* done);
  * HC_ERR_TIMEOUT; timeout_ms <= 0 waits without bound). */
 hc_status hc_event_elapsed_ms(hc_event start, hc_event end, double timeout_ms, float* ms);
 hc_status hc_device_memory(hc_context ctx, size_t* free_bytes, size_t* total_bytes);
+/* Device-memory bookkeeping (no trait counterpart), for callers that budget HBM and for tests that
+ * a call allocates nothing: out[0] = allocation calls this library has made in the process (device
+ * and pinned host, every kind), out[1] / out[2] = bytes in use / high-water mark of the device's
+ * default memory pool, from which the library's stream-ordered allocations come. reset_high != 0
+ * first resets the high-water mark to the bytes in use. */
+hc_status hc_memory_stats(hc_context ctx, int reset_high, uint64_t out[3]);
 /* Measurement utility (no reference counterpart): the GPU's rate of the transforms' exact 64-bit
  * Barrett product, from a register-only kernel on the context's stream (about a millisecond;
  * synchronises the stream). The integer-pipe roofline denominator of the compute-bound NTTs. */

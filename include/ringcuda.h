@@ -196,10 +196,13 @@ hc_status hc_dbfv_hom_mul(hc_ring ring, size_t log2_b, size_t log2_t, hc_view lh
  * loading this library holds until the process exits.
  *  - d x r x deg_L' x deg_K must be at most 2^22 (field_36864: d r <= 113), else
  *    HC_ERR_UNSUPPORTED.
- *  - The ring's tables for this base and digit split must exist: one hc_bfv_key_switch call with
- *    the same base and digits builds them; without it the call fails with HC_ERR_ARG.
- *  - The first call on a device looks up the array's device address (cudaGetSymbolAddress); make
- *    that first call before any stream capture.
+ *  - The ring's tables for this base and digit split must exist: any key-switching call with the
+ *    same base and digit split builds them (hc_bfv_key_switch, the relinearisation of
+ *    hc_bfv_hom_mul, hc_bfv_hom_gal); without them the call fails with HC_ERR_ARG.
+ *  - The first call on a device looks up the array's device address (cudaGetSymbolAddress, with
+ *    that device current); make that first call before any stream capture. The address is kept
+ *    for the life of the process: a device reset (cudaDeviceReset) invalidates it, as it
+ *    invalidates every device object of this library, so no call may follow a reset.
  *  - All calls share the one array: calls whose kernels may overlap on the GPU (other streams,
  *    other contexts on the same device) race and corrupt each other's results. */
 hc_status hc_bfv_key_switch_noalloc(hc_ring ring, hc_view c0_crt, hc_view c1_pb, const size_t* base, size_t r,
