@@ -33,6 +33,10 @@ hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys
 hc_status launch_tensor(hc_context ctx, const KView& d, const KView& lhs_lo, const KView& lhs_hi, const KView& rhs_lo,
                         const KView& rhs_hi, int rsplit, const KMods& m, int f0,
                         int f1, int f2);
+bool crt_pass_ready(hc_context ctx, const hc_ntt_plan* plans2, const hc_ntt_plan* plans3, size_t r, const KView& t);
+hc_status launch_crt_pass(hc_context ctx, int dir, const KView& t, const KView* src, const hc_ntt_plan* plans2,
+                          const hc_ntt_plan* plans3, size_t r, const KView& m2, const KView& m3, bool post,
+                          const KMods& mods);
 hc_status launch_giant(hc_context ctx, const KView& babies, const KView& lcoef, int nbaby, int d, const int* lfirst,
                        const int* lcount, const KView* add, int nadd, const unsigned char* full, int used,
                        const KView& dst, const KMods& m, const int64_t* one_dev);
@@ -726,6 +730,58 @@ struct hc_ring_s {
     }
 
     // ---------------------------------------------------------------- transforms
+    /// The two fused launches of a transform (csrc/crt_fused.cu: both dimensions' NTTs of each
+    /// half in one cluster launch) where the plans are the fused shapes; false: nothing was
+    /// launched, the caller runs the per-dimension calls.
+    bool fused_transform(TransformCache& c, const hc_view& v, bool inverse, const hc_view* post_mul,
+                         const hc_view* src) {
+        const size_t r = c.base.size();
+        if (v.strides[3] != 1 || (src && src->strides[3] != 1)) return false;
+        // broadcast view of a multiplier m over v's shape (the HAL's length-1 rule)
+        auto bcast = [&](const hc_view& m, KView* out) {
+            *out = kv(m);
+            int64_t* st[3] = {&out->s0, &out->s1, &out->s2};
+            for (int d = 0; d < 4; d++) {
+                if (m.shape[d] == v.shape[d]) continue;
+                if (m.shape[d] != 1) return false;
+                if (d < 3) *st[d] = 0;
+                else out->b3 = 1;
+            }
+            return m.strides[3] == 1 || m.shape[3] == 1;
+        };
+        KView m2{}, m3{}, pm{};
+        if (!bcast(inverse ? c.ikl.view() : c.kl.view(), &m2) || !bcast(inverse ? c.ikk.view() : c.kk.view(), &m3))
+            return false;
+        if (post_mul && !bcast(*post_mul, &pm)) return false;
+        const KView t = kv(v);
+        KView sv;
+        const KView* sp = nullptr;
+        bool copy_first = false;
+        if (src && src->ptr != v.ptr) {
+            for (int d = 0; d < 4; d++)
+                if (src->shape[d] != v.shape[d]) return false;
+            // a source that overlaps the destination other than exactly is copied first
+            auto range = [](const hc_view& x, const char** lo, const char** hi) {
+                int64_t last = 0;
+                for (int d = 0; d < 4; d++) last += (x.shape[d] > 0 ? x.shape[d] - 1 : 0) * (d == 3 ? 1 : x.strides[d]);
+                *lo = (const char*)x.ptr;
+                *hi = (const char*)x.ptr + 8 * (last + 1);
+            };
+            const char *dlo, *dhi, *slo, *shi;
+            range(v, &dlo, &dhi);
+            range(*src, &slo, &shi);
+            copy_first = slo < dhi && dlo < shi;
+            sv = kv(*src);
+            sp = copy_first ? nullptr : &sv;
+        }
+        const KMods km = kmods(c.base);
+        if (!crt_pass_ready(ctx, c.plp.data(), c.pk.data(), r, t)) return false;
+        if (copy_first) CK(hc_assign(ctx, v, *src));
+        CK(launch_crt_pass(ctx, 0, t, sp, c.plp.data(), c.pk.data(), r, m2, m3, false, km));
+        CK(launch_crt_pass(ctx, 1, t, nullptr, c.plp.data(), c.pk.data(), r, KView(), pm, post_mul != nullptr, km));
+        return true;
+    }
+
     /// pb_to_crt / crt_to_pb (src/ring.rs:1118-1161); `post_mul`: a Montgomery product applied to
     /// the result in the epilogue of the last pass (the caller's next hal_mul_mont64, fused);
     /// `src`: transform a copy of src into v (the caller's hal_assign, folded into the first pass)
@@ -735,6 +791,7 @@ struct hc_ring_s {
                 "transform: tensor shape does not match the ring and base");
         TransformCache& c = transform_cache(b);
         const size_t r = b.size();
+        if (fused_transform(c, v, inverse, post_mul, src)) return;
         if (src)
             CK(ntt_mul_mont64_dim_from(ctx, v, *src, c.plp.data(), r, HC_DIM2, inverse ? c.ikl.view() : c.kl.view(),
                                        c.mods.data(), r));

@@ -62,7 +62,7 @@ def test_noalloc_key_switch_matches_key_switch_and_oracle(setup, ndigits):
     sk1, sk2 = ring.gen_sk(st), ring.gen_sk(st)
     digits = _digits(len(base), ndigits)
     ksk = ring.gen_ksk(st, base, sk1, sk2, digits, la)
-    ksk_host = ksk.to_numpy()
+    ksk_host = ksk.to_numpy().reshape(len(digits), 2, len(base), ring.dl, ring.dk)  # the oracle's key layout
     out = ring.allocate(2, len(base))
     for call, seed in enumerate((1, 2)):
         c0, c1 = _ciphertext_parts(ring, st, base, sk1, la, 10 * ndigits + seed)
