@@ -52,6 +52,8 @@ def parse():
                     help="run just this workload and print its result (for profiling it alone)")
     ap.add_argument("--roofline-only", action="store_true",
                     help="time only the dominant NTT kernel (the launches a profile of it captures)")
+    ap.add_argument("--transform-only", action="store_true",
+                    help="time only the fused CRT transform passes (the launches a profile of them captures)")
     return ap.parse_args()
 
 
@@ -551,6 +553,72 @@ def kernel_roofline(be, R, base, reps, peaks):
                     "roof is int_roofline (%.2f of the measured Barrett-product rate)" % int_roof["frac"]}
 
 
+# Exact 64-bit products per residue of one CRT transform (pb_to_crt or crt_to_pb, the reference's
+# formula: F = sum over NTT stages of 1/2 per radix-2 and 2 per radix-3 stage, forward and inverse,
+# plus the two kernel products): field_36864 rows [4, 3] and lines [2, 3, 8, 64]: F = 3 + 7 per
+# direction, 22 per transform; field_49152 rows [4] and lines [3, 64, 64]: F = 1 + 8, 20.
+TRANSFORM_PRODUCTS = {"field_36864": 22, "field_49152": 20}
+
+
+def transform_roofline(be, R, base, reps, peaks, rows=ROOF_ROWS):
+    """The fused CRT transform passes (csrc/crt_fused.cu): pb_to_crt of a [rows, r + e, 12, 3072]
+    tensor of lifted products (240 MB, larger than L2) in its two cluster launches, timed with
+    CUDA events on the library's stream. Algorithmic bytes: one read and one write of every
+    residue per launch (32 B per residue per transform); algorithmic products: 22 per residue."""
+    import halcuda
+
+    lifted = base + R.extension_base(base)
+    t = R.allocate(rows, len(lifted))
+    ev0, ev1 = halcuda.Event(), halcuda.Event()
+    for _ in range(3):
+        R.pb_to_crt(t, lifted)
+    be.synchronize()
+    l0 = be.launch_count()
+    ev0.record(be)
+    for _ in range(reps):
+        R.pb_to_crt(t, lifted)
+    ev1.record(be)
+    ms = ev0.elapsed_ms(ev1) / reps
+    launches = (be.launch_count() - l0) // reps
+    # the same transform as the reference's four HAL calls, one launch per dimension and direction
+    import numpy as np
+
+    ker = [R.crt_kernels(i) for i in lifted]
+    kl = be.tensor(np.stack([k[0] for k in ker]).reshape(1, len(lifted), R.dl, 1))
+    kk = be.tensor(np.stack([k[1] for k in ker]).reshape(1, len(lifted), 1, R.dk))
+    p2 = [be.hal_create_ntt_plan(R.modulus(i), [4, 3]) for i in lifted]
+    p3 = _k_plans(R, lifted)
+    mods = R.mods_for(lifted)
+
+    def four_calls():
+        be.hal_ntt_mul_mont64_dim(t, p2, halcuda.DIM2, kl, mods)
+        be.hal_ntt_mul_mont64_dim(t, p3, halcuda.DIM3, kk, mods)
+        be.hal_intt_mont64_dim(t, p2, halcuda.DIM2)
+        be.hal_intt_mont64_dim(t, p3, halcuda.DIM3)
+
+    four_calls()
+    be.synchronize()
+    ev0.record(be)
+    for _ in range(reps):
+        four_calls()
+    ev1.record(be)
+    ms4 = ev0.elapsed_ms(ev1) / reps
+    residues = rows * len(lifted) * R.n
+    bytes_alg = 16 * launches * residues
+    products = TRANSFORM_PRODUCTS[FIELD] * residues
+    bpeak = halcuda.barrett_peak(be)
+    peak = peaks.get("hbm_gbs")
+    achieved = bytes_alg / (ms * 1e-3) / 1e9
+    return {"kernel": "crt_slab3072_kernel (fused CRT passes, pb_to_crt of [%d, %d, 12, 3072])" % (rows, len(lifted)),
+            "launches_per_transform": launches, "ms_per_transform": round(ms, 5),
+            "four_hal_calls_ms_per_transform": round(ms4, 5),
+            "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4) if peak else None, "bytes_per_transform": bytes_alg,
+            "int_roofline": {"achieved": round(products / (ms * 1e-3) / 1e9, 1), "peak": round(bpeak / 1e9, 1),
+                             "unit": "G products/s", "frac": round(products / (ms * 1e-3) / bpeak, 4),
+                             "products_per_transform": products}}
+
+
 _PLAN_CACHE = {}
 
 
@@ -671,6 +739,13 @@ def main():
               "homcrt": lambda: homcrt_bench(be, reps=max(1, args.steps // 3)),
               "serving": lambda: serving_bench(be)}[args.only]
         print(json.dumps({args.only: fn()}), flush=True)
+        return
+    if args.transform_only:
+        import ringcuda
+
+        ring = ringcuda.RingContext(FIELD, LOG2_Q[0], LOG2_Q[1], T_BITS, backend=be)
+        print(json.dumps(transform_roofline(be, ring, ring.initial_base(), max(1, args.steps), load_peaks())),
+              flush=True)
         return
     if args.roofline_only:
         import ringcuda

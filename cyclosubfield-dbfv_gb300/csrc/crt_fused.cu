@@ -1,32 +1,26 @@
-// Fused CRT-transform passes of the two large field descriptors: both dimensions' NTTs of one
-// half of pb_to_crt / crt_to_pb in one launch.
+// Fused CRT-transform passes of field_49152: both dimensions' NTTs of one half of pb_to_crt /
+// crt_to_pb in one launch.
 //
 // The reference transforms a batch [count, r, deg_L', deg_K] in four HAL calls
 // (src/ring.rs:1118-1161): ntt_mul along dimension 2 (deg_L' columns, times the kernel K_L'),
 // ntt_mul along dimension 3 (deg_K lines, times K_K), intt along dimension 2, intt along
-// dimension 3. Each call reads and writes the whole batch. Here each (element, factor) slab -
-// deg_L' x deg_K residues, 295 KB (field_36864) or 393 KB (field_49152), more than one SM's shared
-// memory - is held by a cluster of 12 CTAs in distributed shared memory, and one launch runs a
-// dimension-2 pass and the following dimension-3 pass of every slab:
+// dimension 3. Each call reads and writes the whole batch. Here each (element, factor) slab of
+// field_49152 - 4 rows ([4]) of 12288 residues ([3, 64, 64]), 393 KB, more than one SM's shared
+// memory - is held by a cluster of 12 CTAs in distributed shared memory, CTA 3k + b owning block b
+// (4096 residues) of row k, and one launch runs a dimension-2 pass and the following dimension-3
+// pass of every slab:
 //   launch A: ntt_mul along dimension 2, then ntt_mul along dimension 3;
 //   launch B: intt along dimension 2, then intt along dimension 3 (times an optional factor, the
 //             caller's next Montgomery product).
-// Phase 1: each CTA reads a range of positions of all deg_L' rows of its slab from global memory
-// (coalesced along dimension 3), runs the column transforms in registers and stores every output
-// into the shared memory of the CTA that owns that row (or row block). A cluster barrier makes
-// the stores visible. Phase 2: every CTA runs the line transform of its row (block) in its own
-// shared memory and stores it. The slab is read once and written once per launch, so a transform
-// moves half the bytes of the four-call form and launches half the kernels. Butterflies, their
-// order and the reduction / skip / fused-final schedule are exactly those of the single-dimension
-// kernels (ntt_fast.cuh), so the results are bit-identical.
-//
-//   field_36864: rows [4, 3] (12), lines [2, 3, 8, 64] (3072). CTA k of the cluster owns row k;
-//     phase 1 covers 256 positions per CTA; phase 2 is the line kernel's programme.
-//   field_49152: rows [4] (4), lines [3, 64, 64] (12288). CTA 3k + b owns block b (4096 residues)
-//     of row k. Phase 1 takes positions p, p + 4096, p + 8192 of all four rows (12 residues), runs
-//     the four-point column transforms and then the leading radix-3 stage of each row (which
-//     couples exactly those three positions), so phase 2 - the twelve radix-2 stages - stays
-//     inside each CTA's block.
+// Phase 1: the cluster's threads read positions p, p + 4096, p + 8192 of all four rows (12
+// residues; coalesced along dimension 3), run the four-point column transforms and then the
+// leading radix-3 stage of each row, which couples exactly those three positions, and store each
+// result into the shared memory of the CTA owning its (row, block). A cluster barrier makes the
+// stores visible. Phase 2: every CTA runs the remaining twelve radix-2 stages of its block in its
+// own shared memory and stores it. The slab is read once and written once per launch, so a
+// transform moves half the bytes of the four-call form and launches half the kernels.
+// Butterflies, their order and the reduction / skip / fused-final schedule are exactly those of
+// the single-dimension kernels (ntt_fast.cuh), so the results are bit-identical.
 #include <cooperative_groups.h>
 
 #include <map>
@@ -46,8 +40,7 @@ namespace {
 
 constexpr int CLUSTER = 12;  // CTAs per slab
 constexpr int THREADS = 128;
-constexpr size_t SMEM3072 = (size_t)line_tile_words(HC_SHAPE_L3072) * 8;  // one padded line
-constexpr size_t SMEM12288 = 4608 * 8;                                    // one padded 4096-residue block
+constexpr size_t SMEM12288 = 4608 * 8;  // one padded 4096-residue block
 
 /// Split cluster barrier: every CTA arrives when it starts and waits before its first store into
 /// another CTA's shared memory, which is then known to be running (the loads and arithmetic of
@@ -55,67 +48,59 @@ constexpr size_t SMEM12288 = 4608 * 8;                                    // one
 __device__ __forceinline__ void cluster_arrive_relaxed() { asm volatile("barrier.cluster.arrive.relaxed;\n" ::: "memory"); }
 __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait;\n" ::: "memory"); }
 
-/// Fused pass of a field_36864 slab (DIR 0: launch A, DIR 1: launch B). src: read in phase 1
-/// (t itself for an in-place call). m2: the dimension-2 multiplier [1, r, 12, 1] (DIR 0); m3: the
-/// dimension-3 multiplier, [1, r, 1, 3072] (DIR 0) or a broadcast factor (DIR 1 with POST).
-template <int DIR, bool POST>
-__global__ void __launch_bounds__(THREADS, 8)
-    crt_slab3072_kernel(KView t, KView src, PlanPtrs p2, PlanPtrs p3, KView m2, KView m3, KMods mods) {
-    extern __shared__ int64_t smem[];
-    cg::cluster_group cluster = cg::this_cluster();
-    const int rank = (int)cluster.block_rank();  // the row this CTA owns
-    const int64_t slab = blockIdx.x / CLUSTER;
-    const int64_t j = slab % t.n1, i = slab / t.n1;
-    const DevPlanHeader* P2 = p2.p[j];
-    const DevPlanHeader* P3 = p3.p[j];
-    const int64_t n = mods.n[j], ninv = mods.ninv[j];
-    constexpr bool inv = DIR == 1;
-    cluster_arrive_relaxed();
-    // ---- phase 1: 12-residue columns at positions [256 rank, 256 rank + 256)
-    {
-        const fast::Ctx c2 = make_ctx(P2, reinterpret_cast<const int64_t*>(P2 + 1));
-        const FixedSched<HC_SHAPE_C12, inv> sch{inv ? P2->inv : P2->fwd};
-        fast::SF f[3];
-#pragma unroll
-        for (int q = 0; q < 3; q++) f[q] = fast::sflags(sch, q);
-        const int64_t* gs = reinterpret_cast<const int64_t*>(src.p) + i * src.s0 + j * src.s1;
-        bool first = true;
-        for (int l = 256 * rank + threadIdx.x; l < 256 * rank + 256; l += THREADS) {
-            int64_t x[4][3];
-#pragma unroll
-            for (int a = 0; a < 4; a++)
-#pragma unroll
-                for (int b = 0; b < 3; b++) x[a][b] = gs[(3 * a + b) * src.s2 + l];
-            fast::col12(c2, f, inv, false, x);
-            if (first) {  // every thread runs the first iteration (256 positions, 128 threads)
-                cluster_wait();
-                first = false;
-            }
-#pragma unroll
-            for (int a = 0; a < 4; a++)
-#pragma unroll
-                for (int b = 0; b < 3; b++) {
-                    int64_t v = x[a][b];
-                    if (DIR == 0) v = mul_mont(v, *kat<int64_t>(m2, i, j, 3 * a + b, 0), n, ninv);
-                    cluster.map_shared_rank(smem, 3 * a + b)[fast::pad8(l)] = v;
-                }
-        }
+
+
+/// The four-point factor of a dimension-2 column ([4] or the [4] of [4, 3]: its two radix-2
+/// stages f0, f1) for the two output rows {2h, 2h + 1} only, from the four inputs x0..x3: the
+/// same integers as ntt_fast.cuh's col12 / col4 (and the reference's butterflies,
+/// src/hal/ntt.rs:338-349, :465-476). Two warps share a column, one per h, so that each keeps
+/// six of the twelve values of a [4, 3] column (or of three [4] columns) in registers; the
+/// duplicated work is the four-point factor's one Barrett product per column.
+template <bool INV>
+__device__ __forceinline__ void four_half(const fast::Ctx& c, const fast::SF& f0, const fast::SF& f1, int h,
+                                          int64_t x0, int64_t x1, int64_t x2, int64_t x3, int64_t& o0, int64_t& o1) {
+    if (f0.red) {
+        x0 = fast::red1(c, x0), x1 = fast::red1(c, x1), x2 = fast::red1(c, x2), x3 = fast::red1(c, x3);
     }
-    cluster.sync();  // every row of the slab is in its owner's shared memory
-    // ---- phase 2: the line of row `rank`
-    {
-        const fast::Ctx c3 = make_ctx(P3, reinterpret_cast<const int64_t*>(P3 + 1));
-        const FixedSched<HC_SHAPE_L3072, inv> sch{inv ? P3->inv : P3->fwd};
-        int64_t* g = reinterpret_cast<int64_t*>(t.p) + i * t.s0 + j * t.s1 + rank * t.s2;
-        const int64_t* mulp = nullptr;
-        int64_t me = 0;
-        if (DIR == 0 || POST) {
-            mulp = kat<int64_t>(m3, i, j, rank, 0);
-            me = m3.b3 ? 0 : 1;
+    if (!INV) {
+        // stage 0 (length 4, block 0): pairs (0, 2), (1, 3)
+        int64_t t02 = x2, t13 = x3;
+        if (!f0.skip_ok) {
+            int64_t z, u;
+            fast::twl(c, f0.tw_off, z, u);
+            t02 = bmul(z, u, x2, c.n), t13 = bmul(z, u, x3, c.n);
         }
-        if (DIR == 0) fast::line3072<2, decltype(sch), true>(sch, c3, smem, g, mulp, me, n, ninv);
-        else if (POST) fast::line3072<3, decltype(sch), true>(sch, c3, smem, g, mulp, me, n, ninv);
-        else fast::line3072<1, decltype(sch), true>(sch, c3, smem, g, mulp, me, n, ninv);
+        int64_t p = h ? wsub(x0, t02) : wadd(x0, t02), q = h ? wsub(x1, t13) : wadd(x1, t13);
+        if (f1.red) p = fast::red1(c, p), q = fast::red1(c, q);
+        // stage 1 (length 2): block 0 = rows (0, 1), block 1 = rows (2, 3)
+        int64_t t = q;
+        if (h) {
+            int64_t z, u;
+            fast::twl(c, f1.tw_off + 1, z, u);
+            t = bmul(z, u, q, c.n);
+        } else if (!f1.skip_ok) {
+            int64_t z, u;
+            fast::twl(c, f1.tw_off, z, u);
+            t = bmul(z, u, q, c.n);
+        }
+        o0 = wadd(p, t), o1 = wsub(p, t);
+    } else {
+        // stage 0 (length 2): block 0 = (0, 1), block 1 = (2, 3)
+        int64_t y0 = wadd(x0, x1), y1 = wsub(x0, x1), y2 = wadd(x2, x3), y3 = wsub(x2, x3);
+        if (f0.last) {
+            y0 = bmul(c.il_z, c.il_u, y0, c.n), y1 = bmul(c.il_z, c.il_u, y1, c.n);
+            y2 = bmul(c.il_z, c.il_u, y2, c.n), y3 = bmul(c.il_z, c.il_u, y3, c.n);
+        } else {
+            int64_t z, u;
+            fast::twl(c, f0.tw_off + 1, z, u);
+            if (z != 1) y3 = bmul(z, u, y3, c.n);
+        }
+        if (f1.red) {
+            y0 = fast::red1(c, y0), y1 = fast::red1(c, y1), y2 = fast::red1(c, y2), y3 = fast::red1(c, y3);
+        }
+        // stage 1 (length 4): pairs (0, 2), (1, 3)
+        o0 = h ? wsub(y0, y2) : wadd(y0, y2), o1 = h ? wsub(y1, y3) : wadd(y1, y3);
+        if (f1.last) o0 = bmul(c.il_z, c.il_u, o0, c.n), o1 = bmul(c.il_z, c.il_u, o1, c.n);
     }
 }
 
@@ -136,50 +121,42 @@ __global__ void __launch_bounds__(THREADS, 6)
     const fast::Ctx c3 = make_ctx(P3, reinterpret_cast<const int64_t*>(P3 + 1));
     const FixedSched<HC_SHAPE_L12288, inv> sch3{inv ? P3->inv : P3->fwd};
     cluster_arrive_relaxed();
-    // ---- phase 1: positions p, p + 4096, p + 8192 of the four rows, over the cluster's threads
+    // ---- phase 1: positions p, p + 4096, p + 8192 of the four rows, over the cluster's threads;
+    // warp w keeps rows 2h, 2h + 1 (h = w & 1) of 64 positions per CTA and step
     {
         const fast::Ctx c2 = make_ctx(P2, reinterpret_cast<const int64_t*>(P2 + 1));
         const FixedSched<HC_SHAPE_C4, inv> sch2{inv ? P2->inv : P2->fwd};
-        fast::SF f2[2];
-        f2[0] = fast::sflags(sch2, 0), f2[1] = fast::sflags(sch2, 1);
+        const fast::SF f0 = fast::sflags(sch2, 0), f1 = fast::sflags(sch2, 1);
         const fast::SF f30 = fast::sflags(sch3, 0);
-        int64_t m2v[4] = {0, 0, 0, 0};
-        if (DIR == 0) {
-#pragma unroll
-            for (int k = 0; k < 4; k++) m2v[k] = *kat<int64_t>(m2, i, j, k, 0);
-        }
+        const int warp = threadIdx.x >> 5, h = warp & 1;
+        int64_t m2a = 0, m2b = 0;  // the dimension-2 multipliers of rows 2h, 2h + 1
+        if (DIR == 0) m2a = *kat<int64_t>(m2, i, j, 2 * h, 0), m2b = *kat<int64_t>(m2, i, j, 2 * h + 1, 0);
         const int64_t* gs = reinterpret_cast<const int64_t*>(src.p) + i * src.s0 + j * src.s1;
-        bool first = true;
-        for (int p = rank * THREADS + threadIdx.x; p < 4096; p += CLUSTER * THREADS) {
-            int64_t x[4][3];  // [row][block]
-#pragma unroll
-            for (int k = 0; k < 4; k++)
-#pragma unroll
-                for (int b = 0; b < 3; b++) x[k][b] = gs[k * src.s2 + 4096 * b + p];
+#pragma unroll 1
+        for (int q = 0;; q++) {
+            const int p = 768 * q + 64 * rank + 32 * (warp >> 1) + (threadIdx.x & 31);
+            if (p >= 4096) break;  // warp-uniform (4096 and 768 are multiples of 32)
+            int64_t y[2][3];  // rows 2h, 2h + 1 by block b
 #pragma unroll
             for (int b = 0; b < 3; b++) {
-                int64_t col[4] = {x[0][b], x[1][b], x[2][b], x[3][b]};
-                fast::col4(c2, f2, inv, false, col);
-#pragma unroll
-                for (int k = 0; k < 4; k++) x[k][b] = DIR == 0 ? mul_mont(col[k], m2v[k], n, ninv) : col[k];
+                const int64_t* col = gs + 4096 * b + p;
+                four_half<inv>(c2, f0, f1, h, col[0], col[src.s2], col[2 * src.s2], col[3 * src.s2], y[0][b], y[1][b]);
+                if (DIR == 0) y[0][b] = mul_mont(y[0][b], m2a, n, ninv), y[1][b] = mul_mont(y[1][b], m2b, n, ninv);
             }
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
+            for (int a = 0; a < 2; a++) {
                 if (f30.red) {
 #pragma unroll
-                    for (int b = 0; b < 3; b++) x[k][b] = fast::red1(c3, x[k][b]);
+                    for (int b = 0; b < 3; b++) y[a][b] = fast::red1(c3, y[a][b]);
                 }
-                if (inv) fast::inv3(c3, f30, 0, x[k][0], x[k][1], x[k][2]);
-                else fast::fwd3<true>(c3, f30, false, 0, x[k][0], x[k][1], x[k][2]);
+                if (inv) fast::inv3(c3, f30, 0, y[a][0], y[a][1], y[a][2]);
+                else fast::fwd3<true>(c3, f30, false, 0, y[a][0], y[a][1], y[a][2]);
             }
-            if (first) {  // every thread runs the first iteration (4096 positions, 1536 threads)
-                cluster_wait();
-                first = false;
-            }
+            if (q == 0) cluster_wait();  // every thread runs q = 0 (p < 768)
 #pragma unroll
-            for (int k = 0; k < 4; k++)
+            for (int a = 0; a < 2; a++)
 #pragma unroll
-                for (int b = 0; b < 3; b++) cluster.map_shared_rank(smem, 3 * k + b)[fast::pad8(p)] = x[k][b];
+                for (int b = 0; b < 3; b++) cluster.map_shared_rank(smem, 3 * (2 * h + a) + b)[fast::pad8(p)] = y[a][b];
         }
     }
     cluster.sync();
@@ -267,25 +244,23 @@ bool cluster_ready(K kern, size_t smem) {
 }
 
 template <int DIR, bool POST>
-hc_status launch_shape(hc_context ctx, int shape3, int64_t slabs, const KView& t, const KView& src,
-                       const PlanPtrs& p2, const PlanPtrs& p3, const KView& m2, const KView& m3, const KMods& mods) {
-    if (shape3 == HC_SHAPE_L3072)
-        return cluster_launch(ctx, crt_slab3072_kernel<DIR, POST>, slabs, SMEM3072, t, src, p2, p3, m2, m3, mods);
+hc_status launch_fused(hc_context ctx, int64_t slabs, const KView& t, const KView& src, const PlanPtrs& p2,
+                       const PlanPtrs& p3, const KView& m2, const KView& m3, const KMods& mods) {
     return cluster_launch(ctx, crt_slab12288_kernel<DIR, POST>, slabs, SMEM12288, t, src, p2, p3, m2, m3, mods);
 }
 
-/// The fused shape of a transform's plans (HC_SHAPE_L3072 or HC_SHAPE_L12288), or 0: both plan
-/// lists are the specialised shapes with their compiled-in schedules and t has their extents.
-int fused_shape(const hc_ntt_plan* plans2, const hc_ntt_plan* plans3, size_t r, const KView& t) {
-    if (r == 0 || r > HC_MAX_MODS || (int64_t)r != t.n1) return 0;
+/// Whether a transform's plans are field_49152's shapes ([4] along dimension 2, [3, 64, 64] along
+/// dimension 3) with their compiled-in schedules and t has their extents. (field_36864's [4, 3] x
+/// [2, 3, 8, 64] slabs run faster as separate column and line launches: there the column pass
+/// is a cheap HBM-bound kernel, and the fused form measured 0.92 ms per transform of a
+/// [24, 34, 12, 3072] tensor against 0.88 ms for the four launches.)
+bool fused_shape(const hc_ntt_plan* plans2, const hc_ntt_plan* plans3, size_t r, const KView& t) {
+    if (r == 0 || r > HC_MAX_MODS || (int64_t)r != t.n1) return false;
     const int s2 = hc::plan_shape(plans2[0]), s3 = hc::plan_shape(plans3[0]);
-    const bool f36864 = s2 == (HC_SHAPE_C12 | 0x100) && s3 == (HC_SHAPE_L3072 | 0x100) && t.n2 == 12 && t.n3 == 3072;
-    const bool f49152 = s2 == (HC_SHAPE_C4 | 0x100) && s3 == (HC_SHAPE_L12288 | 0x100) && t.n2 == 4 && t.n3 == 12288;
-    if (!f36864 && !f49152) return 0;
+    if (s2 != (HC_SHAPE_C4 | 0x100) || s3 != (HC_SHAPE_L12288 | 0x100) || t.n2 != 4 || t.n3 != 12288) return false;
     for (size_t j = 1; j < r; j++)
-        if (hc::plan_shape(plans2[j]) != s2 || hc::plan_shape(plans3[j]) != s3) return 0;
-    if (t.n0 * t.n1 * CLUSTER > 0x7fffffff) return 0;
-    return s3 & 0xff;
+        if (hc::plan_shape(plans2[j]) != s2 || hc::plan_shape(plans3[j]) != s3) return false;
+    return t.n0 * t.n1 * CLUSTER <= 0x7fffffff;
 }
 
 }  // namespace
@@ -296,16 +271,9 @@ namespace hc {
 /// and the device runs the 12-CTA clusters of all three kernels of that shape.
 bool crt_pass_ready(hc_context ctx, const hc_ntt_plan* plans2, const hc_ntt_plan* plans3, size_t r, const KView& t) {
     (void)ctx;
-    const int shape3 = fused_shape(plans2, plans3, r, t);
-    if (shape3 == HC_SHAPE_L3072)
-        return cluster_ready(crt_slab3072_kernel<0, false>, SMEM3072) &&
-               cluster_ready(crt_slab3072_kernel<1, false>, SMEM3072) &&
-               cluster_ready(crt_slab3072_kernel<1, true>, SMEM3072);
-    if (shape3 == HC_SHAPE_L12288)
-        return cluster_ready(crt_slab12288_kernel<0, false>, SMEM12288) &&
-               cluster_ready(crt_slab12288_kernel<1, false>, SMEM12288) &&
-               cluster_ready(crt_slab12288_kernel<1, true>, SMEM12288);
-    return false;
+    return fused_shape(plans2, plans3, r, t) && cluster_ready(crt_slab12288_kernel<0, false>, SMEM12288) &&
+           cluster_ready(crt_slab12288_kernel<1, false>, SMEM12288) &&
+           cluster_ready(crt_slab12288_kernel<1, true>, SMEM12288);
 }
 
 /// One fused half of a CRT transform over t [count, r, deg_L', deg_K] (dimension 3 contiguous):
@@ -316,8 +284,7 @@ bool crt_pass_ready(hc_context ctx, const hc_ntt_plan* plans2, const hc_ntt_plan
 hc_status launch_crt_pass(hc_context ctx, int dir, const KView& t, const KView* src, const hc_ntt_plan* plans2,
                           const hc_ntt_plan* plans3, size_t r, const KView& m2, const KView& m3, bool post,
                           const KMods& mods) {
-    const int shape3 = fused_shape(plans2, plans3, r, t);
-    if (!shape3) return fail(HC_ERR_UNSUPPORTED, "fused CRT pass: plans are not a fused shape");
+    if (!fused_shape(plans2, plans3, r, t)) return fail(HC_ERR_UNSUPPORTED, "fused CRT pass: plans are not a fused shape");
     PlanPtrs p2, p3;
     for (size_t j = 0; j < r; j++) {
         p2.p[j] = reinterpret_cast<const DevPlanHeader*>(plan_device(plans2[j]));
@@ -326,9 +293,9 @@ hc_status launch_crt_pass(hc_context ctx, int dir, const KView& t, const KView* 
     const int64_t slabs = t.n0 * t.n1;
     if (slabs == 0) return HC_OK;
     const KView& s = src ? *src : t;
-    if (dir == 0) return launch_shape<0, false>(ctx, shape3, slabs, t, s, p2, p3, m2, m3, mods);
-    if (post) return launch_shape<1, true>(ctx, shape3, slabs, t, s, p2, p3, m2, m3, mods);
-    return launch_shape<1, false>(ctx, shape3, slabs, t, s, p2, p3, m2, m3, mods);
+    if (dir == 0) return launch_fused<0, false>(ctx, slabs, t, s, p2, p3, m2, m3, mods);
+    if (post) return launch_fused<1, true>(ctx, slabs, t, s, p2, p3, m2, m3, mods);
+    return launch_fused<1, false>(ctx, slabs, t, s, p2, p3, m2, m3, mods);
 }
 
 }  // namespace hc

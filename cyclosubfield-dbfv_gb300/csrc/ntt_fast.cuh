@@ -276,9 +276,8 @@ __device__ __forceinline__ void red_all(const Ctx& c, bool red, int64_t* x) {
 /// [2, 3, 8, 64] line (3072 residues): g -> g, via the padded tile s (3456 words). MODE as the
 /// tile kernel (0 forward, 1 inverse, 2 forward + product, 3 inverse + product); the schedule
 /// SCH is that of the programme of MODE's direction. Stages: 0 = factor 2, 1 = factor 3,
-/// 2..4 = factor 8, 5..10 = factor 64. SRC_SMEM: the line is already in the tile (its first pass
-/// reads the tile instead of g); the result still goes to g.
-template <int MODE, class SCH, bool SRC_SMEM = false>
+/// 2..4 = factor 8, 5..10 = factor 64.
+template <int MODE, class SCH>
 __device__ __forceinline__ void line3072(const SCH& sch, const Ctx& c, int64_t* s, int64_t* g, const int64_t* mulp,
                                          int64_t me, int64_t mn, int64_t mi) {
     constexpr bool inv = MODE & 1, reduce_output = MODE == 0;
@@ -291,8 +290,7 @@ __device__ __forceinline__ void line3072(const SCH& sch, const Ctx& c, int64_t* 
 #pragma unroll
             for (int b = 0; b < 2; b++)
 #pragma unroll
-                for (int a = 0; a < 3; a++)
-                    x[b][a] = SRC_SMEM ? s[pad8(o + 512 * a + 1536 * b)] : g[o + 512 * a + 1536 * b];
+                for (int a = 0; a < 3; a++) x[b][a] = g[o + 512 * a + 1536 * b];
             red_all<6>(c, f0.red, &x[0][0]);
             if (!inv) {
 #pragma unroll
