@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(THREADS, 6)
 #pragma unroll
                     for (int b = 0; b < 3; b++) y[a][b] = fast::red1(c3, y[a][b]);
                 }
-                if (inv) fast::inv3(c3, f30, 0, y[a][0], y[a][1], y[a][2]);
+                if (inv) fast::inv3(c3, f30, y[a][0], y[a][1], y[a][2]);
                 else fast::fwd3<true>(c3, f30, false, 0, y[a][0], y[a][1], y[a][2]);
             }
             if (q == 0) cluster_wait();  // every thread runs q = 0 (p < 768)

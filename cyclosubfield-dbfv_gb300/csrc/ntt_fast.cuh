@@ -136,8 +136,11 @@ __device__ __forceinline__ void fwd3(const Ctx& c, const SF& f, bool fuse, int b
     d = o2;
 }
 
-/// Inverse radix-3 butterfly of block `blk` (src/hal/ntt.rs:511-530).
-__device__ __forceinline__ void inv3(const Ctx& c, const SF& f, int blk, int64_t& a, int64_t& b, int64_t& d) {
+/// Inverse radix-3 butterfly of a factor-3 stage (src/hal/ntt.rs:511-530). Every radix-3 stage
+/// of the specialised shapes is the single stage of a factor of length 3: it has one block, whose
+/// twiddles are v^0 = 1, so the reference's twiddle-1 skip always applies and the outputs take
+/// no block-twiddle product (only the fused len^-1 scaling when the stage is the last one).
+__device__ __forceinline__ void inv3(const Ctx& c, const SF& f, int64_t& a, int64_t& b, int64_t& d) {
     int64_t zz0, zu0, zz1, zu1;
     twl(c, f.zeta_off, zz0, zu0);
     twl(c, f.zeta_off + 1, zz1, zu1);
@@ -151,13 +154,9 @@ __device__ __forceinline__ void inv3(const Ctx& c, const SF& f, int blk, int64_t
         d = bmul(c.il_z, c.il_u, sz, c.n);
         return;
     }
-    int64_t yz, yu, zz, zu;
-    twl(c, f.tw_off + 2 * blk, yz, yu);
-    twl(c, f.tw_off + 2 * blk + 1, zz, zu);
-    const bool skip = yz == 1;
     a = s0;
-    b = skip ? sy : bmul(yz, yu, sy, c.n);
-    d = skip ? sz : bmul(zz, zu, sz, c.n);
+    b = sy;
+    d = sz;
 }
 
 // ---------------------------------------------------------------- register groups of radix-2 stages
@@ -313,7 +312,7 @@ __device__ __forceinline__ void line3072(const SCH& sch, const Ctx& c, int64_t* 
                 }
                 red_all<6>(c, f1.red, &x[0][0]);
 #pragma unroll
-                for (int b = 0; b < 2; b++) inv3(c, f1, 0, x[b][0], x[b][1], x[b][2]);
+                for (int b = 0; b < 2; b++) inv3(c, f1, x[b][0], x[b][1], x[b][2]);
             }
 #pragma unroll
             for (int b = 0; b < 2; b++)
@@ -372,7 +371,7 @@ __device__ __forceinline__ void line12288(const SCH& sch, const Ctx& c, int64_t*
                 for (int a = 0; a < 3; a++) fwd_group<3, true>(c, f + 1, fz + 1, 0, x[a]);
             } else {
 #pragma unroll
-                for (int m = 0; m < 8; m++) inv3(c, f[0], 0, x[0][m], x[1][m], x[2][m]);
+                for (int m = 0; m < 8; m++) inv3(c, f[0], x[0][m], x[1][m], x[2][m]);
 #pragma unroll
                 for (int a = 0; a < 3; a++) inv_group<3, false>(c, f + 1, gg >> 6, x[a]);
             }
@@ -419,19 +418,16 @@ __device__ __forceinline__ void line12288_block(const SCH& sch, const Ctx& c, in
             f[q] = sflags(sch, q);
             fz[q] = f[q].last && reduce_output;
         }
-        // twiddles of the factor-3 stage (one block)
-        int64_t wz0, wu0, wz1, wu1, wz2, wu2, wz3, wu3;  // forward: the two products of output blk
+        // twiddles of the factor-3 stage (one block, whose block twiddles are 1: the inverse
+        // outputs take no block-twiddle product, as inv3 explains)
+        int64_t wz0, wu0, wz1, wu1;  // forward: the two products of output blk; inverse: zeta, zeta^2
         if (!inv) {
             const int i0 = blk == 0 ? 0 : (blk == 1 ? 1 : 2), i1 = blk == 0 ? 3 : (blk == 1 ? 5 : 4);
             twl(c, f[0].tw_off + i0, wz0, wu0);
             twl(c, f[0].tw_off + i1, wz1, wu1);
-            wz2 = wu2 = wz3 = wu3 = 0;
         } else {
-            twl(c, f[0].zeta_off, wz0, wu0);       // zeta
-            twl(c, f[0].zeta_off + 1, wz1, wu1);   // zeta^2
-            twl(c, f[0].tw_off + (blk == 2 ? 1 : 0), wz2, wu2);  // block twiddle of output blk (1, 2)
-            twl(c, f[0].tw_off, wz3, wu3);                       // its first entry decides the skip
-            (void)wu3;
+            twl(c, f[0].zeta_off, wz0, wu0);
+            twl(c, f[0].zeta_off + 1, wz1, wu1);
         }
         constexpr int span = inv ? 64 : 512;
         for (int gg = threadIdx.x; gg < 512; gg += blockDim.x) {
@@ -469,7 +465,6 @@ __device__ __forceinline__ void line12288_block(const SCH& sch, const Ctx& c, in
                         o = wadd(wadd(a, bmul(wz0, wu0, b, c.n)), bmul(wz1, wu1, d, c.n));
                     }
                     if (f[0].last) o = bmul(c.il_z, c.il_u, o, c.n);
-                    else if (blk != 0 && wz3 != 1) o = bmul(wz2, wu2, o, c.n);
                 }
                 x[m] = o;
             }
@@ -593,7 +588,7 @@ __device__ __forceinline__ void col12(const Ctx& c, const SF* f, bool inv, bool 
 #pragma unroll
                 for (int b = 0; b < 3; b++) x[a][b] = red1(c, x[a][b]);
 #pragma unroll
-        for (int a = 0; a < 4; a++) inv3(c, f[2], 0, x[a][0], x[a][1], x[a][2]);
+        for (int a = 0; a < 4; a++) inv3(c, f[2], x[a][0], x[a][1], x[a][2]);
     }
 }
 

@@ -2091,6 +2091,7 @@ hc_status hc_crt_batch_destroy(hc_crt_batch b) {
 /// of the next key running on a copy stream while the current key switch computes.
 struct hc_keyset_s {
     hc_ring R = nullptr;
+    hc_context ctx = nullptr;  // the ring's context: a keyset may be destroyed after its ring
     Digits digits;
     size_t r_key = 0, key_words = 0, budget = 0, resident_bytes = 0;
     struct Entry {
@@ -2187,6 +2188,8 @@ void hom_gal_keyset(hc_ring R, const hc_view& ct, const Base& b, const std::vect
     for (auto& o : outs) REQUIRE(o.shape[0] == 2 * B, HC_ERR_SHAPE, "one output row pair per ciphertext");
     Digits dg = clip(ks->digits, b.size());
     REQUIRE(ks->r_key >= b.size(), HC_ERR_SHAPE, "keyset keys cover fewer RNS factors than the ciphertext");
+    for (uint64_t g : gs)  // refused before any work is queued
+        REQUIRE(ks->keys.count(g), HC_ERR_ARG, "keyset: no Galois key for automorphism " + std::to_string(g));
     Tensor c1(R->ctx, B, rr, R->dl(), R->dk());
     const hc_view c1_crt = vstep(ct, 1, 2, B);
     R->transform(c1.view(), b, true, nullptr, &c1_crt);
@@ -2245,6 +2248,7 @@ hc_status hc_keyset_create(hc_ring R, const size_t* digits, size_t d, size_t r_k
         REQUIRE(d > 0 && r_key > 0, HC_ERR_ARG, "keyset: digits and key RNS length");
         auto ks = std::make_unique<hc_keyset_s>();
         ks->R = R;
+        ks->ctx = R->ctx;
         ks->digits = digits_of(digits, d);
         ks->r_key = r_key;
         ks->key_words = 2 * d * r_key * (size_t)R->dl() * (size_t)R->dk();
@@ -2298,7 +2302,7 @@ hc_status hc_keyset_stats(hc_keyset ks, size_t* resident, size_t* streamed, uint
 }
 
 hc_status hc_keyset_destroy(hc_keyset ks) {
-    if (ks) cudaStreamSynchronize(stream_of(ks->R->ctx));
+    if (ks) cudaStreamSynchronize(stream_of(ks->ctx));
     delete ks;
     return HC_OK;
 }
@@ -2315,6 +2319,18 @@ hc_status hc_bfv_hom_gal_keyset(hc_ring R, hc_view ct, const size_t* base, size_
         std::vector<hc_view> outs;
         for (size_t i = 0; i < ngs; i++) outs.push_back(vrows(out, 2 * (int64_t)i, 2 * (int64_t)i + 2));
         hom_gal_keyset(R, ct, b, std::vector<uint64_t>(gs, gs + ngs), ks, outs);
+    });
+}
+
+hc_status hc_bfv_hom_gal_batch_keyset(hc_ring R, hc_view ct, const size_t* base, size_t r, uint64_t g, hc_keyset ks,
+                                      hc_view out) {
+    return guard([&] {
+        REQUIRE(R && ks, HC_ERR_ARG, "null argument");
+        Base b = base_of(base, r);
+        REQUIRE(ct.shape[0] >= 2 && ct.shape[0] % 2 == 0, HC_ERR_SHAPE, "ciphertexts must have 2 rows each");
+        check_view(ct, ct.shape[0], (int64_t)r, R->dl(), R->dk(), "ciphertexts");
+        check_view(out, ct.shape[0], (int64_t)r, R->dl(), R->dk(), "output");
+        hom_gal_keyset(R, ct, b, std::vector<uint64_t>{g}, ks, std::vector<hc_view>{out});
     });
 }
 

@@ -394,6 +394,14 @@ def barrett_peak(be):
     return float(v.value)
 
 
+def int8_mma_peak(be):
+    """The GPU's int8 tensor-core rate (multiply-adds/s) of warp-level s8 x s8 -> s32 MMAs, measured
+    by a register-only kernel (hc_int8_mma_peak)."""
+    v = ctypes.c_double()
+    check(lib().hc_int8_mma_peak(be.h, ctypes.byref(v)))
+    return float(v.value)
+
+
 class PinnedBuffer:
     """Page-locked host memory viewed as a numpy int64 array."""
 

@@ -370,6 +370,14 @@ def hom_gal_keyset(ring, ct, base, gs, ks):
     return out
 
 
+def hom_gal_batch_keyset(ring, ct, base, g, ks, out=None):
+    """hc_bfv_hom_gal_batch_keyset: B ciphertexts [2B, r] under automorphism g, key from a keyset."""
+    out = out if out is not None else ring.allocate(ct.shape[0], len(base))
+    check(lib().hc_bfv_hom_gal_batch_keyset(ring.h, ct.view(), _sz(base), ctypes.c_size_t(len(base)),
+                                            ctypes.c_uint64(g), ks.h, out.view()))
+    return out
+
+
 def dbfv_hom_cyclic_transform(ring, log2_b, log2_t, g, coeffs, ct, base, ks):
     """hom_cyclic_transform_dbfv on the GPU; returns a [rows, r, ...] device tensor."""
     digits = (log2_t - 1) // log2_b + 1

@@ -203,6 +203,11 @@ hc_status hc_memory_stats(hc_context ctx, int reset_high, uint64_t out[3]);
  * Barrett product, from a register-only kernel on the context's stream (about a millisecond;
  * synchronises the stream). The integer-pipe roofline denominator of the compute-bound NTTs. */
 hc_status hc_barrett_peak(hc_context ctx, double* products_per_s);
+/* Measurement utility (no reference counterpart): the GPU's int8 tensor-core rate in
+ * multiply-adds per second, from a register-only kernel of warp-level s8 x s8 -> s32 MMAs (the only
+ * int8 tensor instruction sm_103a has; about a millisecond; synchronises the stream). The
+ * denominator an int8 limb-split base conversion would be measured against. */
+hc_status hc_int8_mma_peak(hc_context ctx, double* macs_per_s);
 
 /* CUDA-graph capture of a sequence of calls on the context's stream (for launch-bound loops):
  * every call between begin and end is recorded, not executed; hc_graph_launch replays it. The

@@ -163,6 +163,12 @@ hc_status hc_keyset_destroy(hc_keyset ks);
 /* bfv_hom_gal (src/bfv.rs:783-841) with the keys of a keyset: ct [2, r] CRT -> out [ngs * 2, r] */
 hc_status hc_bfv_hom_gal_keyset(hc_ring ring, hc_view ct, const size_t* base, size_t r, const uint64_t* gs, size_t ngs,
                                 hc_keyset ks, hc_view out);
+/* bfv_hom_gal (src/bfv.rs:783-841) of B ciphertexts ct [2B, r] (rows 2i, 2i + 1) under one
+ * automorphism g whose key comes from a keyset (streamed in when it is over the HBM budget):
+ * one gadget decomposition and one key-switch launch for the batch -> out [2B, r]. A keyset
+ * without a key for g is refused (HC_ERR_ARG) before any work is queued. */
+hc_status hc_bfv_hom_gal_batch_keyset(hc_ring ring, hc_view ct, const size_t* base, size_t r, uint64_t g, hc_keyset ks,
+                                      hc_view out);
 /* hom_cyclic_transform_dbfv (src/bootstrap/homcrt.rs:369-429): the dBFV ciphertext ct [2 d, r]
  * (CRT basis, almost reduced) is mapped to sum_i coeffs[i] sigma_g^i(ct) by baby-step giant-step:
  * the baby steps share one gadget decomposition per digit, every giant step applies one unhoisted

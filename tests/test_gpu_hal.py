@@ -363,3 +363,13 @@ def test_runtime_stream_wait_and_barrett_peak(be):
     s.close()
     rate = halcuda.barrett_peak(be)
     assert math.isfinite(rate) and rate > 1e9
+
+
+def test_int8_mma_peak(be):
+    """hc_int8_mma_peak returns a positive finite multiply-add rate."""
+    import math
+
+    import halcuda
+
+    rate = halcuda.int8_mma_peak(be)
+    assert math.isfinite(rate) and rate > 1e11
