@@ -48,7 +48,8 @@ def parse():
     ap.add_argument("--no-crt-batch", action="store_true", help="skip the batched CRT-transform workload")
     ap.add_argument("--no-homcrt", action="store_true", help="skip the homomorphic CRT transform workload")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
-    ap.add_argument("--only", choices=["crt_batch", "homcrt", "serving"],
+    ap.add_argument("--no-trait-path", action="store_true", help="skip the trait-level ct-mult")
+    ap.add_argument("--only", choices=["crt_batch", "homcrt", "serving", "trait_path"],
                     help="run just this workload and print its result (for profiling it alone)")
     ap.add_argument("--roofline-only", action="store_true",
                     help="time only the dominant NTT kernel (the launches a profile of it captures)")
@@ -86,8 +87,50 @@ class Dist:
 
 
 # ------------------------------------------------------------------------------ clocks
+class _Nvml:
+    """Read-only NVML queries through ctypes (libnvidia-ml.so.1): the SM clock, its maximum and
+    the clock-event (throttle) reasons of one GPU."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, ordinal):
+        """`ordinal`: the CUDA device ordinal; its PCI bus id (from the CUDA driver, which applies
+        CUDA_VISIBLE_DEVICES) selects the NVML device."""
+        import ctypes
+
+        cu = ctypes.CDLL("libcuda.so.1")
+        dev = ctypes.c_int()
+        bus = ctypes.create_string_buffer(32)
+        if cu.cuInit(0) != 0 or cu.cuDeviceGet(ctypes.byref(dev), ctypes.c_int(ordinal)) != 0 or \
+                cu.cuDeviceGetPCIBusId(bus, ctypes.c_int(32), dev) != 0:
+            raise OSError("no CUDA device")
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        if self.lib.nvmlDeviceGetHandleByPciBusId_v2(bus, ctypes.byref(self.h)) != 0:
+            raise OSError("no NVML handle")
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        self._u = ctypes.c_uint()
+        self._r = ctypes.c_ulonglong()
+        self.ctypes = ctypes
+
+    def sample(self):
+        """(SM MHz, max SM MHz, reason bits)"""
+        c = self.ctypes
+        self.lib.nvmlDeviceGetClockInfo(self.h, c.c_int(1), c.byref(self._u))  # NVML_CLOCK_SM
+        sm = self._u.value
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, c.c_int(1), c.byref(self._u))
+        mx = self._u.value
+        self.reasons_fn(self.h, c.byref(self._r))
+        return sm, mx, self._r.value
+
+
 class ClockSampler:
-    """nvidia-smi samples of SM clocks and throttle reasons during the timed region."""
+    """SM clocks and throttle reasons sampled during the timed region: NVML every millisecond from a
+    host thread where the library loads (so that even a region of a few milliseconds holds
+    samples), else nvidia-smi every 20 ms."""
 
     Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -96,9 +139,36 @@ class ClockSampler:
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
+        self.nvml = None
+        self.thread = None
+        self.rows = []  # NVML: (perf_counter, sm, max, reason bits)
+        self.running = False
         self.begin = self.end = None
+        self.begin_pc = self.end_pc = None
 
     def start(self):
+        import threading
+
+        try:
+            self.nvml = _Nvml(self.gpu)
+            self.nvml.sample()
+        except Exception:
+            self.nvml = None
+        if self.nvml:
+            self.running = True
+
+            def loop():
+                while self.running:
+                    try:
+                        self.rows.append((time.perf_counter(),) + self.nvml.sample())
+                    except Exception:
+                        pass
+                    time.sleep(0.001)
+
+            self.thread = threading.Thread(target=loop, daemon=True)
+            self.thread.start()
+            time.sleep(0.02)
+            return
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
                                           "--format=csv,noheader,nounits", "-lms", "20"],
@@ -108,17 +178,33 @@ class ClockSampler:
         time.sleep(0.1)  # the sampler's first query precedes the timed region
 
     def mark(self, begin):
-        """Host wall-clock bounds of the timed region (the samples inside them are the ones reported)."""
+        """Host bounds of the timed region (the samples inside them are the ones reported)."""
         import datetime
 
         if begin:
-            self.begin = datetime.datetime.now()
+            self.begin, self.begin_pc = datetime.datetime.now(), time.perf_counter()
         else:
-            self.end = datetime.datetime.now()
+            self.end, self.end_pc = datetime.datetime.now(), time.perf_counter()
+
+    def _summary(self, use, inside, reasons, source):
+        sm = [r[0] for r in use]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": use[-1][1] if use else None,
+                "samples": len(use), "samples_in_timed_region": len(inside), "reasons": sorted(reasons),
+                "source": source}
 
     def stop(self):
         import datetime
 
+        if self.nvml:
+            time.sleep(0.005)
+            self.running = False
+            self.thread.join(timeout=1)
+            rows = [(r[1], r[2], r[3]) for r in self.rows]
+            inside = [(r[1], r[2], r[3]) for r in self.rows
+                      if self.begin_pc is not None and self.begin_pc <= r[0] <= self.end_pc]
+            use = inside or rows
+            reasons = {name for r in use for bit, name in _Nvml.REASONS.items() if r[2] & bit}
+            return self._summary(use, inside, reasons, "NVML, 1 ms")
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         time.sleep(0.05)
@@ -146,9 +232,7 @@ class ClockSampler:
             for name, val in zip(names, r[3]):
                 if val.lower() == "active":
                     reasons.add(name)
-        sm = [r[1] for r in use]
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": use[-1][2] if use else None,
-                "samples": len(use), "samples_in_timed_region": len(inside), "reasons": sorted(reasons)}
+        return self._summary([(r[1], r[2]) for r in use], inside, reasons, "nvidia-smi, 20 ms")
 
 
 # ------------------------------------------------------------------------------ workload
@@ -264,9 +348,13 @@ class CrtWorkload:
         R.crt_to_pb(xi, base)
 
 
-def crt_batch_bench(be, steps, warmup):
+def crt_batch_bench(be, steps, warmup, bpeak=None, peaks=None):
     """CRT transforms/s (2 per element: forward and inverse) batched (graph replay of the persistent
-    launch) and plain (one element at a time); inputs ~2.5 GB, larger than L2."""
+    launch) and plain (one element at a time); inputs ~2.5 GB, larger than L2. After the timing a
+    seeded sample of elements is run once more through the batch and compared with the plain form
+    (per-element ring and HAL calls, each bit-exact against the oracle in the tests)."""
+    import numpy as np
+
     import halcuda
 
     w = CrtWorkload(be)
@@ -292,9 +380,39 @@ def crt_batch_bench(be, steps, warmup):
     ev1.record(be)
     plain_ms = ev0.elapsed_ms(ev1)
     n = w.elements
+    # sample check: 8 seeded (item, element) pairs, the batch's result vs the plain form on a copy
+    rng = np.random.default_rng(17)
+    picks = [(int(k), int(rng.integers(0, w.items[int(k)][1].shape[0])))
+             for k in rng.integers(0, len(w.items), size=8)]
+    before = [w.items[k][1].rows(i, i + 1).to_numpy() for k, i in picks]
+    w.graph.launch()
+    be.synchronize()
+    for (k, i), x0 in zip(picks, before):
+        R, x, op, base = w.items[k]
+        y = be.tensor(x0)
+        R.pb_to_crt(y, base)
+        be.hal_mul_mont64(y, op.rows(i, i + 1), R.mods_for(base))
+        R.crt_to_pb(y, base)
+        if not np.array_equal(y.to_numpy(), x.rows(i, i + 1).to_numpy()):
+            raise RuntimeError("crt_batch: element %d of item %d differs from the plain form" % (i, k))
+    # roofline: exact 64-bit products (two transforms and the operand product per residue) and
+    # algorithmic bytes (read x and the operand, write x: 24 B per residue)
+    products = sum(x.shape[0] * len(base) * R.n * (2 * TRANSFORM_PRODUCTS["field_%d" % R.n] + 1)
+                   for R, x, op, base in w.items)
+    roof = None
+    if bpeak:
+        hbm = (peaks or {}).get("hbm_gbs")
+        ach = products / (ms * 1e-3)
+        roof = {"int_roofline": {"achieved": round(ach / 1e9, 1), "peak": round(bpeak / 1e9, 1), "unit": "G products/s",
+                                 "frac": round(ach / bpeak, 4),
+                                 "plain_frac": round(products / (plain_ms * 1e-3) / bpeak, 4),
+                                 "products_per_batch": products},
+                "hbm": {"achieved": round(24 * w.residues / (ms * 1e-3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
+                        "frac": round(24 * w.residues / (ms * 1e-3) / 1e9 / hbm, 4) if hbm else None}}
     return {"workload": "%d elements, field uniform in {field_36864, field_49152}, RNS length uniform in 4..24; "
                         "each pb->crt, mul_mont64 by an operand, crt->pb" % n,
-            "elements": n, "slabs": w.batch.num_slabs, "residues": w.residues,
+            "elements": n, "slabs": w.batch.num_slabs, "residues": w.residues, "roofline": roof,
+            "checked": "8 seeded elements re-run after the timing: equal to the plain form",
             "crt_transforms_per_s": round(2 * n / (ms * 1e-3), 1),
             "plain_crt_transforms_per_s": round(2 * n / (plain_ms * 1e-3), 1),
             "ms_per_batch": round(ms, 4), "plain_ms_per_batch": round(plain_ms, 4),
@@ -357,6 +475,11 @@ def homcrt_bench(be, reps=3):
                       "streamed_GB_per_transform": round((s1["streamed_bytes"] - s0["streamed_bytes"]) / reps / 1e9, 3)}
         ks.close()
     out["key_switches_per_transform"] = 3 * (baby - 1) + 3 * (giant - 1)
+    # every baby-step key is read once per step for all three digits (one key-switch launch), the
+    # giant-step key once per giant rotation (one launch for all output digits)
+    kb = (baby - 1 + giant - 1) * key_bytes
+    out["key_GB_read_per_transform"] = round(kb / 1e9, 3)
+    out["key_read_GBps_resident"] = round(kb / (out["resident"]["ms_per_transform"] * 1e-3) / 1e9, 1)
     R.close()
     return out
 
@@ -383,8 +506,84 @@ def serving_bench(be, n=4000, rate=2000.0):
     reqs = serving.make_stream(n, 1e9, [0.5, 0.35, 0.15], sorted(fields), (4, 20), 2, seed=7)
     out["capacity_batched"] = serving.Engine(be, fields, 16 << 30).run(reqs, batched=True)
     for f in fields.values():
-        f.ring.close()
+        f.close()
+    # over-budget keys: rotations by four automorphisms per field (g, g^2, g^3, g^4) with an HBM
+    # key budget of two keys per field, so that half of the Galois keys are streamed in from
+    # pinned host memory by the rotations that need them
+    gens = {"field_36864": (3283177, 8536255), "field_49152": (20965738, 35297665)}
+    fields = {}
+    for seed, (name, (g, m)) in enumerate(sorted(gens.items()), start=11):
+        fields[name] = serving.FieldState(be, name, (1100, 1140), 256, range(4, 21), 2,
+                                          [pow(g, k, m) for k in range(1, 5)], seed=seed, resident_keys=2)
+    serving.Engine(be, fields, 16 << 30).warm()
+    s0 = {n_: f.keys.stats() for n_, f in fields.items()}
+    reqs = serving.make_stream(n, rate, [0.5, 0.35, 0.15], sorted(fields), (4, 20), 2, seed=7, n_galois=4)
+    res = serving.Engine(be, fields, 16 << 30).run(reqs, batched=True)
+    s1 = {n_: f.keys.stats() for n_, f in fields.items()}
+    res["keys"] = {n_: {"resident": s1[n_]["resident"], "streamed": s1[n_]["streamed"],
+                        "key_MB": round(fields[n_].key_bytes / 1e6, 1),
+                        "streamed_copies": s1[n_]["streamed_copies"] - s0[n_]["streamed_copies"],
+                        "streamed_GB": round((s1[n_]["streamed_bytes"] - s0[n_]["streamed_bytes"]) / 1e9, 2)}
+                   for n_ in fields}
+    out["batched_streamed_keys"] = res
+    for f in fields.values():
+        f.close()
     return out
+
+
+def trait_path_bench(be, work, reps=20):
+    """The reference crate's own bfv_hom_mul call sequence issued through the hal::Backend trait
+    entry points only (trait_ring.py: what the unchanged crate runs above a hal::cuda backend), on
+    the headline workload's first ciphertext pair: direct calls (one ctypes call per trait method,
+    host-issued like the crate's) and a CUDA-graph replay of the same sequence. Its result is
+    compared with the fused path's (hc_bfv_hom_mul), which the tests pin to the oracle."""
+    import numpy as np
+
+    import halcuda
+    import trait_ring
+
+    R = work.ring
+    bfv = trait_ring.TraitBfv(trait_ring.TraitRing(R))
+    c1, c2 = work.ct1.rows(0, 2), work.ct2.rows(0, 2)
+    out = R.allocate(2, work.r)
+
+    def call():
+        bfv.hom_mul(T, c1, c2, work.base, work.rk, work.digits, out=out)
+
+    call()  # builds the crate-side caches (imports of its constant tensors)
+    be.synchronize()
+    exp = R.hom_mul(T, c1, c2, work.base, work.rk, work.digits).to_numpy()
+    if not np.array_equal(out.to_numpy(), exp):
+        raise RuntimeError("trait path: result differs from hc_bfv_hom_mul")
+    ev0, ev1 = halcuda.Event(), halcuda.Event()
+    l0 = be.launch_count()
+    call()
+    launches = be.launch_count() - l0
+    be.synchronize()
+    t0 = time.perf_counter()
+    ev0.record(be)
+    for _ in range(reps):
+        call()
+    ev1.record(be)
+    direct_ms = ev0.elapsed_ms(ev1) / reps
+    host_ms = 1e3 * (time.perf_counter() - t0) / reps
+    graph = halcuda.Graph(be, call)
+    graph.launch()
+    be.synchronize()
+    ev0.record(be)
+    for _ in range(reps):
+        graph.launch()
+    ev1.record(be)
+    graph_ms = ev0.elapsed_ms(ev1) / reps
+    be.synchronize()
+    if not np.array_equal(out.to_numpy(), exp):
+        raise RuntimeError("trait path: graph replay differs from hc_bfv_hom_mul")
+    return {"workload": "bfv_hom_mul %s r=%d t=%d d=%d through the trait entry points only, in the crate's call "
+                        "order (src/bfv.rs:747-775, src/ring.rs)" % (FIELD, work.r, T, len(work.digits)),
+            "launches_per_ct_mult": launches, "checked": "equal to hc_bfv_hom_mul (bit-exact)",
+            "direct": {"ct_mults_per_s": round(1e3 / direct_ms, 1), "ms_per_ct_mult": round(direct_ms, 4),
+                       "host_ms_per_ct_mult": round(host_ms, 4)},
+            "graph": {"ct_mults_per_s": round(1e3 / graph_ms, 1), "ms_per_ct_mult": round(graph_ms, 4)}}
 
 
 def flush_l2(be, scratch):
@@ -560,13 +759,23 @@ def kernel_roofline(be, R, base, reps, peaks):
 TRANSFORM_PRODUCTS = {"field_36864": 22, "field_49152": 20}
 
 
-def transform_roofline(be, R, base, reps, peaks, rows=ROOF_ROWS):
-    """The fused CRT transform passes (csrc/crt_fused.cu): pb_to_crt of a [rows, r + e, 12, 3072]
-    tensor of lifted products (240 MB, larger than L2) in its two cluster launches, timed with
-    CUDA events on the library's stream. Algorithmic bytes: one read and one write of every
-    residue per launch (32 B per residue per transform); algorithmic products: 22 per residue."""
+# (field, log2 q range, t bits, rows of the timed tensor): lifted bases of 34 and 48 factors; 241 MB
+# and 151 MB tensors, larger than L2
+TRANSFORM_CASES = (("field_36864", (900, 930), 8, 24), ("field_49152", (1280, 1310), 2, 8))
+
+
+def transform_roofline(be, R, field, rows, reps, bpeak, peaks):
+    """CRT transforms as the ring runs them: pb_to_crt of a [rows, r + e, deg_L', deg_K] tensor of
+    lifted residues (larger than L2), timed with CUDA events on the library's stream, beside the
+    same transform as the reference's four HAL calls (one launch per dimension and direction).
+    field_49152 runs as two fused cluster launches (csrc/crt_fused.cu), field_36864 as the four
+    column / line launches. Algorithmic bytes: one read and one write of every residue per
+    launch; algorithmic products: TRANSFORM_PRODUCTS per residue."""
+    import numpy as np
+
     import halcuda
 
+    base = R.initial_base()
     lifted = base + R.extension_base(base)
     t = R.allocate(rows, len(lifted))
     ev0, ev1 = halcuda.Event(), halcuda.Event()
@@ -580,14 +789,12 @@ def transform_roofline(be, R, base, reps, peaks, rows=ROOF_ROWS):
     ev1.record(be)
     ms = ev0.elapsed_ms(ev1) / reps
     launches = (be.launch_count() - l0) // reps
-    # the same transform as the reference's four HAL calls, one launch per dimension and direction
-    import numpy as np
-
     ker = [R.crt_kernels(i) for i in lifted]
     kl = be.tensor(np.stack([k[0] for k in ker]).reshape(1, len(lifted), R.dl, 1))
     kk = be.tensor(np.stack([k[1] for k in ker]).reshape(1, len(lifted), 1, R.dk))
-    p2 = [be.hal_create_ntt_plan(R.modulus(i), [4, 3]) for i in lifted]
-    p3 = _k_plans(R, lifted)
+    shape2, shape3 = ([4, 3], [2, 3, 8, 64]) if field == "field_36864" else ([4], [3, 64, 64])
+    p2 = [be.hal_create_ntt_plan(R.modulus(i), shape2) for i in lifted]
+    p3 = [be.hal_create_ntt_plan(R.modulus(i), shape3) for i in lifted]
     mods = R.mods_for(lifted)
 
     def four_calls():
@@ -605,18 +812,31 @@ def transform_roofline(be, R, base, reps, peaks, rows=ROOF_ROWS):
     ms4 = ev0.elapsed_ms(ev1) / reps
     residues = rows * len(lifted) * R.n
     bytes_alg = 16 * launches * residues
-    products = TRANSFORM_PRODUCTS[FIELD] * residues
-    bpeak = halcuda.barrett_peak(be)
+    products = TRANSFORM_PRODUCTS[field] * residues
     peak = peaks.get("hbm_gbs")
     achieved = bytes_alg / (ms * 1e-3) / 1e9
-    return {"kernel": "crt_slab3072_kernel (fused CRT passes, pb_to_crt of [%d, %d, 12, 3072])" % (rows, len(lifted)),
+    return {"workload": "pb_to_crt of [%d, %d, %d, %d] (%d MB)" % (rows, len(lifted), R.dl, R.dk, residues * 8 >> 20),
             "launches_per_transform": launches, "ms_per_transform": round(ms, 5),
             "four_hal_calls_ms_per_transform": round(ms4, 5),
-            "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4) if peak else None, "bytes_per_transform": bytes_alg,
+            "hbm": {"achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(achieved / peak, 4) if peak else None, "bytes_per_transform": bytes_alg},
             "int_roofline": {"achieved": round(products / (ms * 1e-3) / 1e9, 1), "peak": round(bpeak / 1e9, 1),
                              "unit": "G products/s", "frac": round(products / (ms * 1e-3) / bpeak, 4),
-                             "products_per_transform": products}}
+                             "products_per_transform": products,
+                             "four_hal_calls_frac": round(products / (ms4 * 1e-3) / bpeak, 4)}}
+
+
+def transform_rooflines(be, reps, peaks):
+    import halcuda
+    import ringcuda
+
+    bpeak = halcuda.barrett_peak(be)
+    out = {}
+    for field, (lo, hi), tb, rows in TRANSFORM_CASES:
+        R = ringcuda.RingContext(field, lo, hi, tb, backend=be)
+        out[field] = transform_roofline(be, R, field, rows, reps, bpeak, peaks)
+        R.close()
+    return out
 
 
 _PLAN_CACHE = {}
@@ -654,6 +874,181 @@ def cpu_baseline(seconds_budget=12.0):
             "sample": "%d bfv_hom_mul on %s r=%d (oracle C++ restatement of hal::cpu, g++ -O3 without CPU "
                       "tuning, 1 thread, %.1f s)"
                       % (n, FIELD, len(base), el)}
+
+
+# ------------------------------------------------------------------------------ CPU baselines
+# The oracle (single-threaded C++ restatement of the reference's hal::cpu path, test
+# infrastructure) timed on bounded samples of configurations 3, 4 and 5: one host core each, in a
+# spawned process pool that runs beside the GPU measurements, then every host core at once after
+# them.
+
+def cpu_crt_batch_sample():
+    """Configuration 3 on one core: six elements of the batch's mix (both fields, RNS lengths 4, 14
+    and 24), each pb->crt, Montgomery product with an operand, crt->pb, for about 8 s."""
+    import numpy as np
+
+    from oracle import pyoracle as po
+
+    g = np.random.default_rng(3)
+    rings = {f: po.Ring(f, lo, hi, tb) for f, lo, hi, tb in CrtWorkload.FIELDS}
+    work = []
+    for f, o in rings.items():
+        for r in (4, 14, 24):
+            x = g.integers(-(1 << 56), 1 << 56, size=o.shape(1, r), dtype=np.int64)
+            op = g.integers(-(1 << 56), 1 << 56, size=o.shape(1, r), dtype=np.int64)
+            work.append((o, list(range(r)), x, op))
+
+    def run(o, base, x, op):
+        y = np.ascontiguousarray(o.pb_to_crt(x, base)).copy()
+        po.mul_mont64(y, op, [o.primes[i] for i in base])
+        return o.crt_to_pb(y, base)
+
+    for item in work:  # first use builds each prime's CRT kernels: outside the timing
+        run(*item)
+    done, t0 = 0, time.perf_counter()
+    while True:
+        for item in work:
+            run(*item)
+        done += len(work)
+        el = time.perf_counter() - t0
+        if el > 8.0:
+            break
+    return {"value": round(2 * done / el, 2), "unit": "CRT transforms/s", "cores": 1, "kind": "port",
+            "sample": "%d elements cycling over field_36864 and field_49152 at RNS lengths 4, 14, 24, pb->crt, "
+                      "product, crt->pb, %.1f s on one core" % (done, el)}
+
+
+def cpu_homcrt_sample():
+    """Configuration 4 on one core: one full homomorphic CRT step at field_49152 r = 23, len 64,
+    with the benchmark's keys and seeds (key generation untimed)."""
+    import numpy as np
+
+    from oracle import pyoracle as po
+
+    o = po.Ring("field_49152", 1280, 1310, 2)
+    base = o.initial_base()
+    r = len(base)
+    digits = po.select_digits(math.ceil(r / 4), r)
+    la = o.log2_alpha_for_sigma(base, 3.2)
+    st = [99]
+    sk = o.gen_sk(st)
+    m, gen, length = o.info["m"], 20965738, 64
+    baby = min(range(1, length + 1), key=lambda c: (c + 3 * ((length - 1) // c + 1), c))
+    gs = sorted(set([pow(gen, j, m) for j in range(1, baby)] + [pow(gen, baby, m)]))
+    keys = {gg: o.gen_gk(st, sk, gg, digits, la) for gg in gs}
+    t = 1 << 24
+    rng = np.random.default_rng(5)
+    ct = np.zeros(o.shape(6, r), dtype=np.int64)
+    ct[0:2] = o.enc(st, base, t, [int(v) for v in rng.integers(0, t, size=o.n)], sk, la)
+    for dd in (1, 2):
+        ct[2 * dd:2 * dd + 2] = o.enc(st, base, t, [0] * o.n, sk, la)
+    coeffs = [[int(v) for v in rng.integers(-t // 2, t // 2, size=o.dl)] for _ in range(length)]
+    t0 = time.perf_counter()
+    o.dbfv_hom_cyclic_transform(8, 24, gen, coeffs, ct, base, keys, digits)
+    el = time.perf_counter() - t0
+    return {"value": round(1e3 * el, 1), "unit": "ms per transform step", "higher_is_better": False, "cores": 1,
+            "kind": "port", "sample": "one full step (13 baby x 5 giant steps, 48 key switches) on one core"}
+
+
+def cpu_serving_sample(n=24):
+    """Configuration 5 on one core: the first n requests of the benchmark's stream served one after
+    another by the oracle (multiplications, rotations, transforms at their fields and levels)."""
+    import numpy as np
+
+    import serving
+    from oracle import pyoracle as po
+
+    g = np.random.default_rng(11)
+    fields = {}
+    for name, gal in (("field_36864", 3283177), ("field_49152", 20965738)):
+        o = po.Ring(name, 1100, 1140, 8)
+        full = o.initial_base()
+        digits = po.select_digits(math.ceil(len(full) / 4), len(full))
+        la = o.log2_alpha_for_sigma(full, 3.2)
+        st = [5]
+        sk = o.gen_sk(st)
+        fields[name] = (o, digits, o.gen_rk(st, sk, digits, la), o.gen_gk(st, sk, gal, digits, la)[None], gal)
+    reqs = serving.make_stream(n, 2000.0, [0.5, 0.35, 0.15], sorted(fields), (4, 20), 2, seed=7)
+
+    def residues(o, rows, lv):
+        x = np.empty(o.shape(rows, lv), dtype=np.int64)
+        for j in range(lv):
+            x[:, j] = g.integers(0, o.primes[j], size=x[:, j].shape)
+        return x
+
+    inputs = [(q, residues(fields[q.field][0], 2, q.level), residues(fields[q.field][0], 2, q.level)) for q in reqs]
+    for name, (o, *_rest) in fields.items():  # CRT kernels of every prime: outside the timing
+        o.pb_to_crt(residues(o, 1, 20), list(range(20)))
+    lat = []
+    t0 = time.perf_counter()
+    for q, a, b in inputs:
+        o, digits, rk, gk, gal = fields[q.field]
+        base = list(range(q.level))
+        s0 = time.perf_counter()
+        if q.op == "mul":
+            o.hom_mul(256, a, b, base, rk, digits)
+        elif q.op == "rot":
+            o.hom_gal(a, base, [gal], gk, digits)
+        else:
+            o.pb_to_crt(a[0:1], base)
+        lat.append(1e3 * (time.perf_counter() - s0))
+    el = time.perf_counter() - t0
+    lat.sort()
+    return {"value": round(n / el, 2), "unit": "req/s", "cores": 1, "kind": "port",
+            "p50_ms": round(lat[len(lat) // 2], 1), "p99_ms": round(lat[-1], 1),
+            "sample": "the first %d requests of the stream, served one after another on one core (%.1f s)" % (n, el)}
+
+
+CPU_SAMPLES = {"headline": cpu_baseline, "crt_batch": cpu_crt_batch_sample, "homcrt": cpu_homcrt_sample,
+               "serving": cpu_serving_sample}
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu), or the machine type."""
+    import platform
+
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return platform.machine()
+
+
+def _sample_task(name):
+    return CPU_SAMPLES[name]()
+
+
+def cpu_all_cores(name):
+    """The one-core sample `name` run at the same time in one spawned process per host core; the
+    throughputs add up (a homcrt step's time becomes steps per second)."""
+    import multiprocessing as mp
+
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(_sample_task, [name] * cores)
+    el = time.perf_counter() - t0
+    if name == "homcrt":
+        value, unit = sum(1e3 / r["value"] for r in res), "transform steps/s"
+    else:
+        value, unit = sum(r["value"] for r in res), res[0]["unit"]
+    return {"value": round(value, 3), "unit": unit, "cores": cores, "kind": "port", "cpu": cpu_model(),
+            "sample": "the one-core sample in %d concurrent processes (%.0f s wall)" % (cores, el)}
+
+
+def start_cpu_baselines(names):
+    """Starts the one-core oracle samples in a spawned process pool (one process per sample,
+    before the first GPU call); returns (pool, {name: async result})."""
+    import multiprocessing as mp
+
+    from oracle import build as oracle_build
+
+    oracle_build.build()
+    pool = mp.get_context("spawn").Pool(len(names))
+    return pool, {n: pool.apply_async(_sample_task, (n,)) for n in names}
 
 
 def load_peaks():
@@ -730,22 +1125,25 @@ def main():
     if args.impl == "reference":
         reference_arm(args, dist)
         return
+    cpu_jobs = None
+    if dist.rank == 0 and not args.no_cpu_baseline and not (args.only or args.transform_only or args.roofline_only):
+        names = ["headline"] + [n for n, off in (("crt_batch", args.no_crt_batch), ("homcrt", args.no_homcrt),
+                                                  ("serving", args.no_serving)) if not off]
+        cpu_jobs = start_cpu_baselines(names)  # before the first GPU call
     import halcuda
 
     halcuda.lib()
     be = halcuda.CudaBackend(dist.local_rank)
     if args.only:
-        fn = {"crt_batch": lambda: crt_batch_bench(be, max(3, args.steps // 2), args.warmup),
+        fn = {"crt_batch": lambda: crt_batch_bench(be, max(3, args.steps // 2), args.warmup,
+                                                   halcuda.barrett_peak(be), load_peaks()),
               "homcrt": lambda: homcrt_bench(be, reps=max(1, args.steps // 3)),
-              "serving": lambda: serving_bench(be)}[args.only]
+              "serving": lambda: serving_bench(be),
+              "trait_path": lambda: trait_path_bench(be, Workload(be, 1))}[args.only]
         print(json.dumps({args.only: fn()}), flush=True)
         return
     if args.transform_only:
-        import ringcuda
-
-        ring = ringcuda.RingContext(FIELD, LOG2_Q[0], LOG2_Q[1], T_BITS, backend=be)
-        print(json.dumps(transform_roofline(be, ring, ring.initial_base(), max(1, args.steps), load_peaks())),
-              flush=True)
+        print(json.dumps(transform_rooflines(be, max(1, args.steps), load_peaks())), flush=True)
         return
     if args.roofline_only:
         import ringcuda
@@ -797,13 +1195,32 @@ def main():
     e2e_ms, h2d, d2h, _ = e2e_steps(be, work, e2e_n, args.e2e_slots)
     e2e_val = dist.world * e2e_n / (e2e_ms * 1e-3)
     roof = kernel_roofline(be, work.ring, work.base, 20, peaks)
-    crt = None if args.no_crt_batch else crt_batch_bench(be, min(20, max(3, args.steps // 2)), args.warmup)
+    trait = None if args.no_trait_path else trait_path_bench(be, work)
+    bpeak = halcuda.barrett_peak(be)
+    int8 = halcuda.int8_mma_peak(be)
+    transforms = transform_rooflines(be, 10, peaks)
+    crt = None if args.no_crt_batch else crt_batch_bench(be, min(20, max(3, args.steps // 2)), args.warmup, bpeak,
+                                                          peaks)
     hcrt = None if args.no_homcrt else homcrt_bench(be)
     srv = None if args.no_serving else serving_bench(be)
 
     if dist.rank != 0:
         return
-    cpu = None if args.no_cpu_baseline else cpu_baseline()
+    cpu, cpu_more = None, {}
+    if cpu_jobs:
+        pool, jobs = cpu_jobs
+        for name, job in jobs.items():
+            res = job.get(timeout=900)
+            if name == "headline":
+                cpu = dict(res, cpu=cpu_model())
+            else:
+                cpu_more[name] = dict(res, cpu=cpu_model())
+        pool.close()
+        pool.join()
+    for name, res in (("crt_batch", crt), ("homcrt", hcrt), ("serving", srv)):
+        if res and name in cpu_more:
+            res["cpu_baseline"] = cpu_more[name]
+            res["cpu_baseline_all_cores"] = cpu_all_cores(name)  # after the GPU work: no contention
     line = {
         "metric": METRIC,
         "value": round(value, 3),
@@ -831,8 +1248,12 @@ def main():
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": roof,
+        "transform_rooflines": transforms,
+        "peaks_measured_here": {"barrett_products_per_s": round(bpeak, -6), "int8_mma_macs_per_s": round(int8, -9)},
         "clocks": clk,
     }
+    if trait:
+        line["trait_path"] = trait
     if crt:
         line["crt_batch"] = crt
     if hcrt:
