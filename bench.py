@@ -878,9 +878,9 @@ def cpu_baseline(seconds_budget=12.0):
 
 # ------------------------------------------------------------------------------ CPU baselines
 # The oracle (single-threaded C++ restatement of the reference's hal::cpu path, test
-# infrastructure) timed on bounded samples of configurations 3, 4 and 5: one host core each, in a
-# spawned process pool that runs beside the GPU measurements, then every host core at once after
-# them.
+# infrastructure) timed on bounded samples of configurations 3, 4 and 5 after the GPU
+# measurements: one host core each (spawned processes, one per sample), then every host core at
+# once.
 
 def cpu_crt_batch_sample():
     """Configuration 3 on one core: six elements of the batch's mix (both fields, RNS lengths 4, 14
@@ -1040,8 +1040,8 @@ def cpu_all_cores(name):
 
 
 def start_cpu_baselines(names):
-    """Starts the one-core oracle samples in a spawned process pool (one process per sample,
-    before the first GPU call); returns (pool, {name: async result})."""
+    """Starts the one-core oracle samples in a spawned process pool (one process per sample);
+    returns (pool, {name: async result})."""
     import multiprocessing as mp
 
     from oracle import build as oracle_build
@@ -1125,11 +1125,6 @@ def main():
     if args.impl == "reference":
         reference_arm(args, dist)
         return
-    cpu_jobs = None
-    if dist.rank == 0 and not args.no_cpu_baseline and not (args.only or args.transform_only or args.roofline_only):
-        names = ["headline"] + [n for n, off in (("crt_batch", args.no_crt_batch), ("homcrt", args.no_homcrt),
-                                                  ("serving", args.no_serving)) if not off]
-        cpu_jobs = start_cpu_baselines(names)  # before the first GPU call
     import halcuda
 
     halcuda.lib()
@@ -1206,9 +1201,12 @@ def main():
 
     if dist.rank != 0:
         return
+    # the oracle's samples run after the GPU work (spawned processes), so that their host memory
+    # traffic does not slow the GPU's copies from pinned host memory (the streamed keys)
     cpu, cpu_more = None, {}
-    if cpu_jobs:
-        pool, jobs = cpu_jobs
+    if not args.no_cpu_baseline:
+        names = ["headline"] + [n for n, r_ in (("crt_batch", crt), ("homcrt", hcrt), ("serving", srv)) if r_]
+        pool, jobs = start_cpu_baselines(names)
         for name, job in jobs.items():
             res = job.get(timeout=900)
             if name == "headline":
