@@ -2,7 +2,9 @@
 
 Workload (BFV ciphertext multiplication at full size): field_36864 (n = 36864 = 12 x 3072), an
 initial RNS base of r = 16 primes of 57 bits (log2 q in 900..930), plaintext modulus t = 256,
-secret key sparse ternary, error sigma = 3.2, relinearisation key with ceil(r/4) = 4 gadget digits.
+secret key uniform ternary (every coefficient uniform in {-1, 0, 1}; the parity tests use the
+reference's sparse generator as well), error sigma = 3.2, relinearisation key with ceil(r/4) = 4
+gadget digits.
 The plain GPU form: one step is one ciphertext multiplication per launch (bfv_hom_mul incl.
 lifting, tensoring, rescaling and relinearisation, replayed from a CUDA graph of the call), the
 steps cycling over B = 8 seeded synthetic ciphertext pairs (larger than L2 together) on two
@@ -249,7 +251,7 @@ class Workload:
         self.digits = ringcuda.select_digits(math.ceil(self.r / 4), self.r)
         la = R.log2_alpha_for_sigma(self.base, 3.2)
         st = [seed]
-        self.sk = R.gen_sk(st)
+        self.sk = R.gen_sk_uniform_ternary(st)  # the configuration's key: coefficients uniform in {-1, 0, 1}
         self.rk = R.gen_rk(st, self.sk, self.digits, la)
         self.batch = batch
         # B ciphertext pairs stacked along dimension 0: rows 2b, 2b + 1 hold pair b
@@ -1237,6 +1239,7 @@ def main():
                    "field": FIELD, "rns_len": work.r,
                    "extension_len": len(work.ring.extension_base(work.base)), "gadget_digits": len(work.digits),
                    "ct_mults_per_step": 1, "streams": len(streams),
+                   "secret_key": "uniform ternary", "error_sigma": 3.2,
                    "l2": "steps cycle over %d ciphertext pairs (%d MB of operands and results, larger than L2); "
                          "no flush" % (work.batch, 3 * work.ct_bytes * work.batch // 2**20)},
         "batched": batched,

@@ -1524,6 +1524,20 @@ hc_status hc_bfv_gen_sk(hc_ring R, uint64_t* st, hc_view sk) {
     });
 }
 
+hc_status hc_bfv_gen_sk_uniform_ternary(hc_ring R, uint64_t* st, hc_view sk) {
+    return guard([&] {
+        REQUIRE(R && st, HC_ERR_ARG, "null argument");
+        Base b = prefix(R->initial_len);
+        check_view(sk, 1, (int64_t)b.size(), R->dl(), R->dk(), "sk");
+        std::vector<i128> c(R->n(), 0);
+        for (size_t j = 0; j < R->n(); j++) c[j] = (i128)(splitmix(st) % 3) - 1;
+        Tensor t = element_from_coeffs(R, b, c);
+        R->transform(t.view(), b, false);
+        CK(hc_assign(R->ctx, sk, t.view()));
+        CK(hc_synchronize(R->ctx));
+    });
+}
+
 double hc_bfv_log2_alpha_for_sigma(hc_ring R, const size_t* base, size_t r, double sigma) {
     return R->log2_q(Base(base, base + r)) - std::log2(sigma);
 }

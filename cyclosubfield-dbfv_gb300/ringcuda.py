@@ -148,6 +148,14 @@ class RingContext:
         state[0] = int(st[0])
         return sk
 
+    def gen_sk_uniform_ternary(self, state):
+        """hc_bfv_gen_sk_uniform_ternary: every coefficient uniform in {-1, 0, 1}."""
+        st = self._state(state)
+        sk = self.allocate(1, self.initial_len)
+        check(lib().hc_bfv_gen_sk_uniform_ternary(self.h, st, sk.view()))
+        state[0] = int(st[0])
+        return sk
+
     def enc(self, state, base, t, ptxt, sk, log2_alpha):
         st = self._state(state)
         words = np.zeros((self.n, 2), dtype=np.int64)

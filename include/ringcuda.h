@@ -70,6 +70,11 @@ hc_status hc_ring_apply_galois(hc_ring ring, hc_view dst, hc_view src, const siz
 /* ---------------------------------------------------------------- BFV (src/bfv.rs) */
 /* gen_sk (:180-190): sk [1, r0, ...] over the initial base, CRT basis */
 hc_status hc_bfv_gen_sk(hc_ring ring, uint64_t* rng_state, hc_view sk);
+/* No counterpart in the reference (whose gen_sk, src/bfv.rs:180-190, is sparse with Hamming weight
+ * 128): a secret key with every coefficient uniform in {-1, 0, 1}, coefficient j = (splitmix64
+ * draw j mod 3) - 1, the distribution the benchmark's configuration names; CRT basis, initial
+ * base, like hc_bfv_gen_sk. The kernels do not depend on the key's distribution. */
+hc_status hc_bfv_gen_sk_uniform_ternary(hc_ring ring, uint64_t* rng_state, hc_view sk);
 /* bfv_enc (:294-307): ptxt holds n i128 coefficients (2 words each); ct [2, r, ...] */
 hc_status hc_bfv_enc(hc_ring ring, uint64_t* rng_state, const size_t* base, size_t r, const int64_t t[2],
                      const int64_t* ptxt, hc_view sk, double log2_alpha, hc_view ct);

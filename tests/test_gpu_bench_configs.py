@@ -122,3 +122,43 @@ def test_hom_mul_config2_rns_lengths(po, be, lo, hi, r):
     got = d.hom_mul(t, d.tensor(ct1), d.tensor(ct2), base, rk_d, digits).to_numpy()
     assert (got == exp).all()
     assert o.decrypt(got, base, sk, t) == [po.cmod(7 * v, t) for v in m1]
+
+
+def test_uniform_ternary_secret_key(po, be):
+    """The benchmark's secret key (hc_bfv_gen_sk_uniform_ternary, no reference counterpart):
+    coefficient j is (splitmix64 draw j mod 3) - 1, returned in CRT basis over the initial base; a
+    field_36864 r = 16 ct-mult of encryptions under it equals the oracle's and decrypts to the
+    product."""
+    import ringcuda
+
+    R = ringcuda.RingContext("field_36864", 120, 140, 8, backend=be)
+    o = po.Ring("field_36864", 120, 140, 8)
+    base = R.initial_base()
+    st, st2 = [77], [77]
+    sk = R.gen_sk_uniform_ternary(st)
+    exp = [po.splitmix64(st2) % 3 - 1 for _ in range(R.n)]
+    assert st[0] == st2[0]
+    pb = R.allocate(1, len(base))
+    be.hal_assign(pb, sk)
+    R.crt_to_pb(pb, base)
+    lifts, _ = o.element_lifts(pb.to_numpy(), base)
+    assert lifts == exp
+    assert all(abs(exp.count(v) - R.n / 3) < 0.02 * R.n for v in (-1, 0, 1))
+    R.close()
+
+    R = ringcuda.RingContext("field_36864", 900, 930, 8, backend=be)
+    o = po.Ring("field_36864", 900, 930, 8)
+    base = R.initial_base()
+    st = [2026]
+    sk = R.gen_sk_uniform_ternary(st)
+    digits = po.select_digits(math.ceil(len(base) / 4), len(base))
+    la = R.log2_alpha_for_sigma(base, 3.2)
+    rk = R.gen_rk(st, sk, digits, la)
+    g = np.random.default_rng(12)
+    m1 = [int(v) for v in g.integers(0, 256, size=R.n)]
+    ct1, ct2 = R.enc(st, base, 256, m1, sk, la), R.enc(st, base, 256, o.encode_scalar(5), sk, la)
+    got = R.hom_mul(256, ct1, ct2, base, rk, digits).to_numpy()
+    rk_o = rk.to_numpy().reshape(len(digits), 2, len(base), R.dl, R.dk)
+    assert (got == o.hom_mul(256, ct1.to_numpy(), ct2.to_numpy(), base, rk_o, digits)).all()
+    assert o.decrypt(got, base, sk.to_numpy(), 256) == [po.cmod(5 * v, 256) for v in m1]
+    R.close()
