@@ -98,6 +98,32 @@ __global__ void __launch_bounds__(256) matmul_kernel(KView d, KView lhs, KView r
     }
 }
 
+/// matmul_kernel with the position's U <= KMAX right-hand values read once into registers: all
+/// output rows j are formed from them (the naive form re-reads rhs[i,u,k,l] for every j); the lhs
+/// entries are warp-uniform loads. Same products in the same order, so the same wrapping sums.
+template <int KMAX>
+__global__ void __launch_bounds__(128, 4) matmul_reg_kernel(KView d, KView lhs, KView rhs, int U, int64_t lines,
+                                                         int chunks) {
+    const int64_t tiles = lines * chunks;
+    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        int64_t line = tile / chunks;  // (i, k)
+        int64_t l = (tile - line * chunks) * blockDim.x + threadIdx.x;
+        if (l >= d.n3) continue;
+        int64_t k = line % d.n2, i = line / d.n2;
+        int64_t x[KMAX];
+#pragma unroll
+        for (int u = 0; u < KMAX; u++) x[u] = u < U ? *kat<int64_t>(rhs, i, u, k, l) : 0;
+        for (int64_t j = 0; j < d.n1; j++) {
+            const int64_t* c = kat<int64_t>(lhs, i, j, 0, 0);
+            i128 acc = 0;
+#pragma unroll
+            for (int u = 0; u < KMAX; u++)
+                if (u < U) acc = (i128)((u128)acc + (u128)((i128)c[u * lhs.s2] * (i128)x[u]));
+            st128(kat<longlong2>(d, i, j, k, l), acc);
+        }
+    }
+}
+
 struct Terms {
     KView l[HC_MAX_TERMS];
     KView r[HC_MAX_TERMS];
@@ -242,8 +268,19 @@ hc_status launch_matmul(hc_context ctx, const KView& d, const KView& lhs, const 
     if (lines == 0 || d.n3 == 0 || d.n1 == 0) return HC_OK;
     int chunks;
     unsigned blocks;
-    grid_for(ctx, d, lines, &chunks, &blocks);
-    matmul_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(d, lhs, rhs, U, lines, chunks);
+    cudaStream_t s = stream_of(ctx);
+    if (U <= 24) {
+        // 128-thread CTAs: up to 24 register-resident right-hand values per thread
+        chunks = (int)((d.n3 + 127) / 128);
+        const int64_t tiles = lines * chunks, cap = (int64_t)num_sms(ctx) * 32;
+        blocks = (unsigned)(tiles < cap ? tiles : cap);
+        if (U <= 8) matmul_reg_kernel<8><<<blocks, 128, 0, s>>>(d, lhs, rhs, (int)U, lines, chunks);
+        else if (U <= 16) matmul_reg_kernel<16><<<blocks, 128, 0, s>>>(d, lhs, rhs, (int)U, lines, chunks);
+        else matmul_reg_kernel<24><<<blocks, 128, 0, s>>>(d, lhs, rhs, (int)U, lines, chunks);
+    } else {
+        grid_for(ctx, d, lines, &chunks, &blocks);
+        matmul_kernel<<<blocks, 256, 0, s>>>(d, lhs, rhs, U, lines, chunks);
+    }
     count_launch(ctx);
     return cuda_check(cudaGetLastError(), "matmul kernel launch");
 }
