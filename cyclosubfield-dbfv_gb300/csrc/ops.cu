@@ -77,6 +77,22 @@ __global__ void __launch_bounds__(256) pw_kernel(KView d, KView a, KView b, KMod
     }
 }
 
+/// pw_kernel over a 2-D grid: blockIdx.y is the destination line (i, j, k), decomposed once per
+/// thread with 32-bit arithmetic, and each thread walks LINE_SPAN / 256 positions of it, so that
+/// the per-element work is the operation itself (the tile form pays several 64-bit divisions per
+/// element). Used while the line count fits the grid's y dimension.
+constexpr int LINE_SPAN = 1024;
+
+template <int OP>
+__global__ void __launch_bounds__(256) pw_line_kernel(KView d, KView a, KView b, KMods m) {
+    const int line = (int)blockIdx.y;
+    const int k = line % (int)d.n2, r = line / (int)d.n2;
+    const int j = r % (int)d.n1, i = r / (int)d.n1;
+    const int64_t l0 = (int64_t)blockIdx.x * LINE_SPAN;
+    const int64_t l1 = l0 + LINE_SPAN < d.n3 ? l0 + LINE_SPAN : d.n3;
+    for (int64_t l = l0 + threadIdx.x; l < l1; l += 256) pw_apply<OP>(d, a, b, m, i, j, k, l);
+}
+
 /// dst[i,j,k,l] = sum_u lhs[li,j,u,0] * rhs[ri,u,k,l] (src/hal/cpu.rs:791-818), i128 wrapping.
 __global__ void __launch_bounds__(256) matmul_kernel(KView d, KView lhs, KView rhs, int64_t U, int64_t lines,
                                                      int chunks) {
@@ -148,6 +164,23 @@ __global__ void __launch_bounds__(256) inner_product_kernel(KView d, Terms terms
     }
 }
 
+/// inner_product_kernel over the line grid of pw_line_kernel.
+__global__ void __launch_bounds__(256) inner_product_line_kernel(KView d, Terms terms) {
+    const int line = (int)blockIdx.y;
+    const int k = line % (int)d.n2, r = line / (int)d.n2;
+    const int j = r % (int)d.n1, i = r / (int)d.n1;
+    const int64_t l0 = (int64_t)blockIdx.x * LINE_SPAN;
+    const int64_t l1 = l0 + LINE_SPAN < d.n3 ? l0 + LINE_SPAN : d.n3;
+    for (int64_t l = l0 + threadIdx.x; l < l1; l += 256) {
+        i128 acc = 0;
+        for (int t = 0; t < terms.n; t++) {
+            i128 prod = (i128)*kat<int64_t>(terms.l[t], i, j, k, l) * (i128)*kat<int64_t>(terms.r[t], i, j, k, l);
+            acc = (i128)((u128)acc + (u128)prod);
+        }
+        st128(kat<longlong2>(d, i, j, k, l), acc);
+    }
+}
+
 /// dst[i,j,k,l] += red(((lhs[i,0,k,l] + 2^(shift-1)) >> shift) * rhs[ri,j,0,0])
 /// (src/hal/cpu.rs:950-980)
 __global__ void __launch_bounds__(256) bconv_correct_kernel(KView d, KView lhs, KView rhs, KMods m, int shift,
@@ -165,6 +198,24 @@ __global__ void __launch_bounds__(256) bconv_correct_kernel(KView d, KView lhs, 
         int64_t c = *kat<int64_t>(rhs, i, j, 0, 0);
         int64_t* p = kat<int64_t>(d, i, j, k, l);
         *p = wadd(*p, mul_mont(q, c, m.n[j], m.ninv[j]));
+    }
+}
+
+/// bconv_correct_kernel over the line grid of pw_line_kernel.
+__global__ void __launch_bounds__(256) bconv_correct_line_kernel(KView d, KView lhs, KView rhs, KMods m, int shift) {
+    const i128 half = (i128)1 << (shift - 1);
+    const int line = (int)blockIdx.y;
+    const int k = line % (int)d.n2, r = line / (int)d.n2;
+    const int j = r % (int)d.n1, i = r / (int)d.n1;
+    const int64_t c = *kat<int64_t>(rhs, i, j, 0, 0);
+    const int64_t n = m.n[j], ninv = m.ninv[j];
+    const int64_t l0 = (int64_t)blockIdx.x * LINE_SPAN;
+    const int64_t l1 = l0 + LINE_SPAN < d.n3 ? l0 + LINE_SPAN : d.n3;
+    for (int64_t l = l0 + threadIdx.x; l < l1; l += 256) {
+        i128 x = ld128(kat<longlong2>(lhs, i, 0, k, l));
+        int64_t q = (int64_t)((i128)((u128)x + (u128)half) >> shift);
+        int64_t* p = kat<int64_t>(d, i, j, k, l);
+        *p = wadd(*p, mul_mont(q, c, n, ninv));
     }
 }
 
@@ -220,6 +271,13 @@ __global__ void __launch_bounds__(256) permute_kernel(KView d, KView s, const ui
     }
 }
 
+/// Grid of the line kernels, or false when the line count exceeds the grid's y dimension.
+bool line_grid(const KView& d, int64_t lines, dim3* grid) {
+    if (lines > 65535 || d.n1 > INT32_MAX || d.n2 > INT32_MAX) return false;
+    *grid = dim3((unsigned)((d.n3 + LINE_SPAN - 1) / LINE_SPAN), (unsigned)lines, 1);
+    return true;
+}
+
 void grid_for(hc_context ctx, const KView& d, int64_t lines, int* chunks, unsigned* blocks) {
     *chunks = (int)((d.n3 + 255) / 256);
     int64_t tiles = lines * *chunks;
@@ -238,8 +296,13 @@ hc_status launch_pointwise(hc_context ctx, int op, const KView& d, const KView& 
     unsigned blocks;
     grid_for(ctx, d, lines, &chunks, &blocks);
     cudaStream_t s = stream_of(ctx);
-#define HC_PW(OPV) \
-    case OPV: pw_kernel<OPV><<<blocks, 256, 0, s>>>(d, a, b, m, lines, chunks); break;
+    dim3 lg;
+    const bool by_line = line_grid(d, lines, &lg);
+#define HC_PW(OPV)                                                      \
+    case OPV:                                                           \
+        if (by_line) pw_line_kernel<OPV><<<lg, 256, 0, s>>>(d, a, b, m); \
+        else pw_kernel<OPV><<<blocks, 256, 0, s>>>(d, a, b, m, lines, chunks); \
+        break;
     switch (op) {
         HC_PW(OP_ASSIGN)
         HC_PW(OP_ASSIGN_NARROW)
@@ -293,8 +356,13 @@ hc_status launch_inner_product(hc_context ctx, const KView& d, const KView* l, c
     t.n = n;
     int chunks;
     unsigned blocks;
-    grid_for(ctx, d, lines, &chunks, &blocks);
-    inner_product_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(d, t, lines, chunks);
+    dim3 lg;
+    if (line_grid(d, lines, &lg)) {
+        inner_product_line_kernel<<<lg, 256, 0, stream_of(ctx)>>>(d, t);
+    } else {
+        grid_for(ctx, d, lines, &chunks, &blocks);
+        inner_product_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(d, t, lines, chunks);
+    }
     count_launch(ctx);
     return cuda_check(cudaGetLastError(), "inner product kernel launch");
 }
@@ -305,8 +373,13 @@ hc_status launch_bconv_correct(hc_context ctx, const KView& d, const KView& lhs,
     if (lines == 0 || d.n3 == 0) return HC_OK;
     int chunks;
     unsigned blocks;
-    grid_for(ctx, d, lines, &chunks, &blocks);
-    bconv_correct_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(d, lhs, rhs, m, shift, lines, chunks);
+    dim3 lg;
+    if (line_grid(d, lines, &lg)) {
+        bconv_correct_line_kernel<<<lg, 256, 0, stream_of(ctx)>>>(d, lhs, rhs, m, shift);
+    } else {
+        grid_for(ctx, d, lines, &chunks, &blocks);
+        bconv_correct_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(d, lhs, rhs, m, shift, lines, chunks);
+    }
     count_launch(ctx);
     return cuda_check(cudaGetLastError(), "bconv correction kernel launch");
 }
