@@ -94,6 +94,9 @@ __global__ void __launch_bounds__(256) pw_line_kernel(KView d, KView a, KView b,
 }
 
 /// dst[i,j,k,l] = sum_u lhs[li,j,u,0] * rhs[ri,u,k,l] (src/hal/cpu.rs:791-818), i128 wrapping.
+/// Four output rows j per pass share each rhs load (the matrix entries are warp-uniform loads),
+/// and columns whose four entries are zero are skipped (a gadget conversion matrix is zero outside
+/// each digit's columns); the sums are the same wrapping sums.
 __global__ void __launch_bounds__(256) matmul_kernel(KView d, KView lhs, KView rhs, int64_t U, int64_t lines,
                                                      int chunks) {
     const int64_t tiles = lines * chunks;
@@ -102,39 +105,28 @@ __global__ void __launch_bounds__(256) matmul_kernel(KView d, KView lhs, KView r
         int64_t l = (tile - line * chunks) * blockDim.x + threadIdx.x;
         if (l >= d.n3) continue;
         int64_t k = line % d.n2, i = line / d.n2;
-        for (int64_t j = 0; j < d.n1; j++) {
+        int64_t j = 0;
+        for (; j + 4 <= d.n1; j += 4) {
+            i128 acc[4] = {0, 0, 0, 0};
+            for (int64_t u = 0; u < U; u++) {
+                int64_t c[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) c[q] = *kat<int64_t>(lhs, i, j + q, u, 0);
+                if ((c[0] | c[1] | c[2] | c[3]) == 0) continue;  // zero columns (a gadget matrix's) add nothing
+                const int64_t x = *kat<int64_t>(rhs, i, u, k, l);
+#pragma unroll
+                for (int q = 0; q < 4; q++) acc[q] = (i128)((u128)acc[q] + (u128)((i128)c[q] * (i128)x));
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) st128(kat<longlong2>(d, i, j + q, k, l), acc[q]);
+        }
+        for (; j < d.n1; j++) {
             i128 acc = 0;
             for (int64_t u = 0; u < U; u++) {
                 int64_t c = *kat<int64_t>(lhs, i, j, u, 0);
                 int64_t x = *kat<int64_t>(rhs, i, u, k, l);
                 acc = (i128)((u128)acc + (u128)((i128)c * (i128)x));
             }
-            st128(kat<longlong2>(d, i, j, k, l), acc);
-        }
-    }
-}
-
-/// matmul_kernel with the position's U <= KMAX right-hand values read once into registers: all
-/// output rows j are formed from them (the naive form re-reads rhs[i,u,k,l] for every j); the lhs
-/// entries are warp-uniform loads. Same products in the same order, so the same wrapping sums.
-template <int KMAX>
-__global__ void __launch_bounds__(128, 4) matmul_reg_kernel(KView d, KView lhs, KView rhs, int U, int64_t lines,
-                                                         int chunks) {
-    const int64_t tiles = lines * chunks;
-    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        int64_t line = tile / chunks;  // (i, k)
-        int64_t l = (tile - line * chunks) * blockDim.x + threadIdx.x;
-        if (l >= d.n3) continue;
-        int64_t k = line % d.n2, i = line / d.n2;
-        int64_t x[KMAX];
-#pragma unroll
-        for (int u = 0; u < KMAX; u++) x[u] = u < U ? *kat<int64_t>(rhs, i, u, k, l) : 0;
-        for (int64_t j = 0; j < d.n1; j++) {
-            const int64_t* c = kat<int64_t>(lhs, i, j, 0, 0);
-            i128 acc = 0;
-#pragma unroll
-            for (int u = 0; u < KMAX; u++)
-                if (u < U) acc = (i128)((u128)acc + (u128)((i128)c[u * lhs.s2] * (i128)x[u]));
             st128(kat<longlong2>(d, i, j, k, l), acc);
         }
     }
@@ -331,19 +323,8 @@ hc_status launch_matmul(hc_context ctx, const KView& d, const KView& lhs, const 
     if (lines == 0 || d.n3 == 0 || d.n1 == 0) return HC_OK;
     int chunks;
     unsigned blocks;
-    cudaStream_t s = stream_of(ctx);
-    if (U <= 24) {
-        // 128-thread CTAs: up to 24 register-resident right-hand values per thread
-        chunks = (int)((d.n3 + 127) / 128);
-        const int64_t tiles = lines * chunks, cap = (int64_t)num_sms(ctx) * 32;
-        blocks = (unsigned)(tiles < cap ? tiles : cap);
-        if (U <= 8) matmul_reg_kernel<8><<<blocks, 128, 0, s>>>(d, lhs, rhs, (int)U, lines, chunks);
-        else if (U <= 16) matmul_reg_kernel<16><<<blocks, 128, 0, s>>>(d, lhs, rhs, (int)U, lines, chunks);
-        else matmul_reg_kernel<24><<<blocks, 128, 0, s>>>(d, lhs, rhs, (int)U, lines, chunks);
-    } else {
-        grid_for(ctx, d, lines, &chunks, &blocks);
-        matmul_kernel<<<blocks, 256, 0, s>>>(d, lhs, rhs, U, lines, chunks);
-    }
+    grid_for(ctx, d, lines, &chunks, &blocks);
+    matmul_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(d, lhs, rhs, U, lines, chunks);
     count_launch(ctx);
     return cuda_check(cudaGetLastError(), "matmul kernel launch");
 }

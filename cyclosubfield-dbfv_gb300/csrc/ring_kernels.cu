@@ -6,7 +6,7 @@
 //    the double reduction, the q~-scaled correction and the conversion to Montgomery form, without
 //    the i128 `tmp` / `correction` tensors ever reaching HBM.
 //  - galois_kernel: both permutation passes of apply_galois (src/ring.rs:1212-1222) as one gather.
-//  - keyswitch_kernel: the key-switch inner product, the addition of c0 / c1 through mont(1)
+//  - keyswitch_async_kernel (keyswitch1_kernel for odd or unaligned views): the key-switch inner product, the addition of c0 / c1 through mont(1)
 //    and reduce_wide (src/bfv.rs:498-556, src/ring.rs:460-485, :503-509, :846-865).
 //  - tensor_kernel: hom_mul_raw_acc + reduce_wide (src/bfv.rs:667-683).
 //  - giant_kernel: one giant step of the homomorphic CRT transform for up to four output digits:
@@ -270,52 +270,15 @@ __global__ void __launch_bounds__(256) keyswitch1_kernel(KsArgs a, KMods m, cons
     }
 }
 
-__global__ void __launch_bounds__(256) keyswitch_kernel(KsArgs a, KMods m, const int64_t* one, int64_t lines,
-                                                        int chunks) {
-    // two adjacent positions l, l + 1 per thread: the keys and the output are read and written as
-    // 16-byte pairs (dimension 3 is contiguous and even), the parts and summands gathered singly.
-    // Tiles run as ((j, k), chunk, i) with the ciphertext index innermost: the B tiles that read
-    // one block of the key are adjacent, so the key comes from DRAM once and B - 1 reads hit L2.
-    const int64_t tiles = lines * chunks;
-    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const int64_t i = tile % a.batch, u = tile / a.batch;
-        const int64_t line = u / chunks;  // (j, k)
-        const int64_t l = 2 * ((u - line * chunks) * blockDim.x + threadIdx.x);
-        if (l >= a.dst.n3) continue;
-        const int64_t k = line % a.dst.n2, j = line / a.dst.n2;
-        const int64_t sk = a.p2 ? (int64_t)a.p2[k] : k;
-        const int64_t sl0 = a.p3 ? (int64_t)a.p3[l] : l, sl1 = a.p3 ? (int64_t)a.p3[l + 1] : l + 1;
-        i128 acc00 = 0, acc01 = 0, acc10 = 0, acc11 = 0;  // acc<row><position>
-        for (int t = 0; t < a.nterms; t++) {
-            const int64_t x0 = *kat<int64_t>(a.parts[t], i, j, sk, sl0), x1 = *kat<int64_t>(a.parts[t], i, j, sk, sl1);
-            const longlong2 k0 = *reinterpret_cast<const longlong2*>(kat<int64_t>(a.keys[t], 0, j, k, l));
-            const longlong2 k1 = *reinterpret_cast<const longlong2*>(kat<int64_t>(a.keys[t], 1, j, k, l));
-            acc00 = (i128)((u128)acc00 + (u128)((i128)x0 * (i128)k0.x));
-            acc01 = (i128)((u128)acc01 + (u128)((i128)x1 * (i128)k0.y));
-            acc10 = (i128)((u128)acc10 + (u128)((i128)x0 * (i128)k1.x));
-            acc11 = (i128)((u128)acc11 + (u128)((i128)x1 * (i128)k1.y));
-        }
-        const int64_t o = one[j];
-        if (a.has_add0) {
-            acc00 = (i128)((u128)acc00 + (u128)((i128)*kat<int64_t>(a.add0, i, j, sk, sl0) * (i128)o));
-            acc01 = (i128)((u128)acc01 + (u128)((i128)*kat<int64_t>(a.add0, i, j, sk, sl1) * (i128)o));
-        }
-        if (a.has_add1) {
-            acc10 = (i128)((u128)acc10 + (u128)((i128)*kat<int64_t>(a.add1, i, j, sk, sl0) * (i128)o));
-            acc11 = (i128)((u128)acc11 + (u128)((i128)*kat<int64_t>(a.add1, i, j, sk, sl1) * (i128)o));
-        }
-        longlong2 w0, w1;
-        w0.x = finish_wide(acc00, a.full0, m, (int)j), w0.y = finish_wide(acc01, a.full0, m, (int)j);
-        w1.x = finish_wide(acc10, a.full1, m, (int)j), w1.y = finish_wide(acc11, a.full1, m, (int)j);
-        *reinterpret_cast<longlong2*>(kat<int64_t>(a.dst, 2 * i, j, k, l)) = w0;
-        *reinterpret_cast<longlong2*>(kat<int64_t>(a.dst, 2 * i + 1, j, k, l)) = w1;
-    }
-}
-
-/// keyswitch_kernel with the terms' reads (the two gathered digit words and the two 16-byte key
-/// pairs of each gadget digit) staged through shared memory by asynchronous copies, KS_STAGES
-/// digits ahead of the products, so that the reads in flight do not occupy registers. Each
-/// thread copies and reads only its own slots (no barrier). Same products, same wrapping sums.
+/// The key-switch inner product with two adjacent positions l, l + 1 per thread: the keys and the
+/// output are read and written as 16-byte pairs (dimension 3 is contiguous and even), the parts
+/// and summands gathered singly (through the automorphism's permutation when one is fused). The
+/// terms' reads (the two digit words and the two key pairs of each gadget digit) are staged
+/// through shared memory by asynchronous copies, KS_STAGES digits ahead of the products, so that
+/// the reads in flight do not occupy registers; each thread copies and reads only its own slots
+/// (no barrier). Tiles run as ((j, k), chunk, i) with the ciphertext index innermost: the B tiles
+/// that read one block of the key are adjacent, so the key comes from DRAM once and B - 1 reads
+/// hit L2.
 constexpr int KS_STAGES = 3;
 
 __global__ void __launch_bounds__(256, 4) keyswitch_async_kernel(KsArgs a, KMods m, const int64_t* one,
@@ -500,81 +463,6 @@ __global__ void __launch_bounds__(256) giant_kernel(GiantArgs a, KMods m, const 
     }
 }
 
-/// giant_kernel with its baby-step reads staged through shared memory by asynchronous copies
-/// (cp.async), GA_STAGES (baby step, input digit) units ahead of the products: the loads in
-/// flight no longer occupy registers, so a thread keeps several units' reads outstanding at the
-/// occupancy its accumulators allow. Each thread copies and reads only its own positions' words,
-/// so no barrier is needed between the copies and their use. `units` lists the (baby step, input
-/// digit) pairs that feed an output digit of the launch, in the order of giant_kernel's loops;
-/// the sums are the same wrapping i128 sums.
-constexpr int GA_STAGES = 6;
-constexpr int GA_MAX_UNITS = 1024;
-
-struct GiantUnits {
-    unsigned short u[GA_MAX_UNITS];  // (baby step << 6) | input digit
-    int n;
-};
-
-
-__global__ void __launch_bounds__(256, 4) giant_async_kernel(GiantArgs a, GiantUnits un, KMods m, const int64_t* one,
-                                                          int64_t lines, int chunks) {
-    __shared__ int64_t stage[GA_STAGES][2][256];
-    const int64_t tiles = lines * chunks;
-    const int tid = threadIdx.x;
-    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        int64_t line = tile / chunks;  // (j, k)
-        int64_t l = (tile - line * chunks) * blockDim.x + tid;
-        if (l >= a.dst.n3) continue;
-        int64_t k = line % a.dst.n2, j = line / a.dst.n2;
-        auto issue = [&](int u) {
-            if (u < un.n) {
-                const int bj = un.u[u] >> 6, i = un.u[u] & 63;
-                const int64_t row = (int64_t)bj * 2 * a.d + 2 * i;
-                const int sl = u % GA_STAGES;
-                cp_async8(&stage[sl][0][tid], kat<int64_t>(a.babies, row, j, k, l));
-                cp_async8(&stage[sl][1][tid], kat<int64_t>(a.babies, row + 1, j, k, l));
-            }
-            cp_async_commit();  // an empty group past the end keeps the count uniform
-        };
-#pragma unroll
-        for (int u = 0; u < GA_STAGES - 1; u++) issue(u);
-        i128 acc0[GIANT_OUT], acc1[GIANT_OUT];
-#pragma unroll
-        for (int o = 0; o < GIANT_OUT; o++) acc0[o] = acc1[o] = 0;
-        for (int u = 0; u < un.n; u++) {
-            issue(u + GA_STAGES - 1);
-            cp_async_wait<GA_STAGES - 1>();  // unit u's group has landed
-            const int bj = un.u[u] >> 6, i = un.u[u] & 63;
-            const int lf = a.lfirst[bj], lc = a.lcount[bj];
-            const int sl = u % GA_STAGES;
-            const int64_t x0 = stage[sl][0][tid], x1 = stage[sl][1][tid];
-#pragma unroll
-            for (int o = 0; o < GIANT_OUT; o++) {
-                const int jj = a.out0 + o - i;
-                if (o < a.nout && jj >= 0 && jj < lc) {
-                    const int64_t f = *kat<int64_t>(a.lcoef, lf + jj, j, k, 0);
-                    acc0[o] = (i128)((u128)acc0[o] + (u128)((i128)x0 * (i128)f));
-                    acc1[o] = (i128)((u128)acc1[o] + (u128)((i128)x1 * (i128)f));
-                }
-            }
-        }
-        cp_async_wait<0>();
-#pragma unroll
-        for (int o = 0; o < GIANT_OUT; o++) {
-            if (o >= a.nout) break;
-            const int od = a.out0 + o;
-            if (od < a.nadd) {
-                const int64_t on = one[j];
-                acc0[o] = (i128)((u128)acc0[o] + (u128)((i128)*kat<int64_t>(a.add, 2 * od, j, k, l) * (i128)on));
-                acc1[o] = (i128)((u128)acc1[o] + (u128)((i128)*kat<int64_t>(a.add, 2 * od + 1, j, k, l) * (i128)on));
-            }
-            const bool full = (a.full >> o) & 1;
-            *kat<int64_t>(a.dst, 2 * od, j, k, l) = finish_wide(acc0[o], full, m, (int)j);
-            *kat<int64_t>(a.dst, 2 * od + 1, j, k, l) = finish_wide(acc1[o], full, m, (int)j);
-        }
-    }
-}
-
 void grid_lines(hc_context ctx, int64_t n3, int64_t lines, int* chunks, unsigned* blocks) {
     *chunks = (int)((n3 + 255) / 256);
     int64_t tiles = lines * *chunks;
@@ -697,18 +585,7 @@ hc_status launch_giant(hc_context ctx, const KView& babies, const KView& lcoef, 
         a.nout = std::min(GIANT_OUT, used - o0);
         a.full = 0;
         for (int o = 0; o < a.nout; o++) a.full |= (unsigned)(full[o0 + o] != 0) << o;
-        // the (baby step, input digit) units that feed an output digit of this launch
-        GiantUnits un;
-        un.n = 0;
-        bool fits = d < 64 && nbaby < 1024;
-        for (int bj = 0; bj < nbaby && fits; bj++)
-            for (int i = 0; i < d && fits; i++) {
-                if (i + lcount[bj] <= a.out0 || i >= a.out0 + a.nout) continue;
-                if (un.n == GA_MAX_UNITS) fits = false;
-                else un.u[un.n++] = (unsigned short)((bj << 6) | i);
-            }
-        if (fits) giant_async_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(a, un, m, one_dev, lines, chunks);
-        else giant_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(a, m, one_dev, lines, chunks);
+        giant_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(a, m, one_dev, lines, chunks);
         count_launch(ctx);
         hc_status st = cuda_check(cudaGetLastError(), "giant-step kernel launch");
         if (st) return st;
