@@ -6,8 +6,9 @@
 //    the double reduction, the q~-scaled correction and the conversion to Montgomery form, without
 //    the i128 `tmp` / `correction` tensors ever reaching HBM.
 //  - galois_kernel: both permutation passes of apply_galois (src/ring.rs:1212-1222) as one gather.
-//  - keyswitch_async_kernel (keyswitch1_kernel for odd or unaligned views): the key-switch inner product, the addition of c0 / c1 through mont(1)
-//    and reduce_wide (src/bfv.rs:498-556, src/ring.rs:460-485, :503-509, :846-865).
+//  - keyswitch_async_kernel (keyswitch1_kernel for odd or unaligned views): the key-switch inner
+//    product, the addition of c0 / c1 through mont(1) and reduce_wide (src/bfv.rs:498-556,
+//    src/ring.rs:460-485, :503-509, :846-865).
 //  - tensor_kernel: hom_mul_raw_acc + reduce_wide (src/bfv.rs:667-683).
 //  - giant_kernel: one giant step of the homomorphic CRT transform for up to four output digits:
 //    the baby-step inner product over the digit convolution (dbfv_acc_inner_product_element_lprime,
