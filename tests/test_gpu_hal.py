@@ -373,3 +373,53 @@ def test_int8_mma_peak(be):
 
     rate = halcuda.int8_mma_peak(be)
     assert math.isfinite(rate) and rate > 1e11
+
+
+def test_matmul_zero_columns_and_row_remainders(be, po):
+    """A gadget-style conversion matrix [d, r + 1, r, 1], zero outside each digit's columns (the
+    kernel skips all-zero column groups), with output row counts that are not multiples of four,
+    against the oracle."""
+    g = rng(41)
+    d, r = 4, 16
+    for rows in (r + 1, 6, 3):
+        lhs = np.zeros((d, rows, r, 1), dtype=np.int64)
+        for i in range(d):
+            lhs[i, :, 4 * i:4 * i + 4, 0] = rand_i64(g, (rows, 4), -(1 << 56), 1 << 56)
+        rhs = rand_i64(g, (1, r, 12, 64), -(1 << 57), 1 << 57)
+        exp = rand_i128(g, (d, rows, 12, 64))
+        po.matmul_i64(exp, lhs, rhs)
+        out = be.tensor(rand_i128(g, (d, rows, 12, 64)), wide=True)
+        be.hal_matmul_i64(out, be.tensor(lhs), be.tensor(rhs))
+        assert (out.to_numpy() == exp).all(), rows
+
+
+def test_line_grid_and_tile_paths_agree(be, po, primes36864):
+    """The pointwise, inner-product and correction kernels run over a grid of destination lines
+    while the line count fits the grid, and over tiles beyond it: both forms against the oracle
+    (70000 lines of 4 positions, and 200 lines of 3072)."""
+    g = rng(42)
+    for shape in ((1, 70000, 1, 4), (2, 4, 25, 3072)):
+        a, b = rand_i64(g, shape), rand_i64(g, shape)
+        exp = a.copy()
+        po.sub_i64(exp, b)
+        da = be.tensor(a)
+        be.hal_sub_i64(da, be.tensor(b))
+        assert (da.to_numpy() == exp).all(), shape
+        ls = [rand_i64(g, shape, -(1 << 57), 1 << 57) for _ in range(3)]
+        rs = [rand_i64(g, shape, -(1 << 57), 1 << 57) for _ in range(3)]
+        wexp = rand_i128(g, shape)
+        po.inner_product_i64(wexp, ls, rs)
+        dw = be.tensor(rand_i128(g, shape), wide=True)
+        be.hal_inner_product_i64(dw, [be.tensor(x) for x in ls], [be.tensor(x) for x in rs])
+        assert (dw.to_numpy() == wexp).all(), shape
+    # the base-conversion correction over > 65535 destination lines
+    pr = primes36864[:2]
+    shape = (35000, 2, 1, 4)
+    lhs = rand_i128(g, (35000, 1, 1, 4))
+    rhs = residues(g, (1, 2, 1, 1), pr)
+    dst = residues(g, shape, pr)
+    exp = dst.copy()
+    po.bconv_correct_mont64(exp, lhs, rhs, pr, 70)
+    d = be.tensor(dst)
+    be.hal_bconv_correct_mont64(d, be.tensor(lhs, wide=True), be.tensor(rhs), mods(be, pr), 70)
+    assert (d.to_numpy() == exp).all()

@@ -158,3 +158,43 @@ def test_host_side_failures_do_not_stop_the_stream(be, fields, po):
             alone = serving.Request(q.rid, q.op, q.field, q.level, 0.0, q.slot)
             eng.submit([alone])
             assert (alone.out.to_numpy() == q.out.to_numpy()).all(), (q.op, q.field, q.level)
+
+
+@pytest.mark.slow
+def test_benchmark_parameters_against_the_oracle(be, po):
+    """Serving at the benchmark's parameters (log2 q in 1100..1140, t = 256) at its largest level,
+    20 factors, on both fields: one multiplication, one rotation and one transform each, served
+    together in one stream, every result equal to the oracle's with the same seeded keys."""
+    import math
+
+    import serving
+
+    fields, seeds = {}, {"field_36864": 31, "field_49152": 32}
+    for name, gen in GENERATORS.items():
+        fields[name] = serving.FieldState(be, name, (1100, 1140), 256, [20], 1, gen, seed=seeds[name])
+    reqs = [serving.Request(k, op, name, 20, 0.0, 0) for k, (op, name) in
+            enumerate((op, name) for name in sorted(fields) for op in serving.OPS)]
+    stats = serving.Engine(be, fields, 16 << 30, max_batch=8).run(reqs, batched=True, keep_outputs=True)
+    assert stats["requests"] == 6 and stats["failed"] == 0
+    for q in reqs:
+        F = fields[q.field]
+        o = po.Ring(q.field, 1100, 1140, 8)
+        full = o.initial_base()
+        digits = po.select_digits(math.ceil(len(full) / 4), len(full))
+        la = o.log2_alpha_for_sigma(full, 3.2)
+        st = [seeds[q.field]]
+        sk = o.gen_sk(st)
+        rk = o.gen_rk(st, sk, digits, la)
+        gk = o.gen_gk(st, sk, F.g, digits, la)
+        base = list(range(20))
+        c1, c2 = (x.to_numpy() for x in F.pool[20][0])
+        if q.op == "mul":
+            exp = o.hom_mul(F.t, c1, c2, base, rk, digits)
+        elif q.op == "rot":
+            exp = o.hom_gal(c1, base, [F.g], gk[None], digits)[0]
+        else:
+            exp = o.pb_to_crt(c1[0:1], base)
+        got = q.out.to_numpy()
+        assert (got == np.asarray(exp).reshape(got.shape)).all(), (q.op, q.field)
+    for F in fields.values():
+        F.close()
