@@ -1109,7 +1109,9 @@ def reference_arm(args, dist):
             "ms_per_step": round(1e3 * el / args.steps, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int64", "data": "synthetic",
             "config": {"workload": "bfv_hom_mul %s r=16 t=256, %d ct-mults per step (one per host core)"
-                                   % (FIELD, cores), "field": FIELD, "rns_len": 16},
+                                   % (FIELD, cores), "field": FIELD, "rns_len": 16,
+                       "secret_key": "the reference's sparse ternary generator (a ct-mult's work does not depend "
+                                     "on the key)"},
             "cpu_baseline": {"value": round(value, 4), "unit": "ct-mults/s", "cores": cores, "kind": "port",
                              "sample": "%d ct-mults per step on %d processes; oracle C++ restatement of the "
                                        "reference's hal::cpu path, g++ -O3 without CPU tuning (the Rust crate is not "
