@@ -280,8 +280,12 @@ __global__ void __launch_bounds__(256) keyswitch1_kernel(KsArgs a, KMods m, cons
 /// (no barrier). Tiles run as ((j, k), chunk, i) with the ciphertext index innermost: the B tiles
 /// that read one block of the key are adjacent, so the key comes from DRAM once and B - 1 reads
 /// hit L2.
+/// COMMON: every term's digit view shares the strides of parts[0] and every key view those of
+/// keys[0] (the layouts the ring layer passes), so each thread forms its offsets once and a term's
+/// addresses are one addition each.
 constexpr int KS_STAGES = 3;
 
+template <bool COMMON>
 __global__ void __launch_bounds__(256, 4) keyswitch_async_kernel(KsArgs a, KMods m, const int64_t* one,
                                                                  int64_t lines, int chunks) {
     __shared__ int64_t sx[KS_STAGES][2][256];
@@ -296,13 +300,27 @@ __global__ void __launch_bounds__(256, 4) keyswitch_async_kernel(KsArgs a, KMods
         const int64_t k = line % a.dst.n2, j = line / a.dst.n2;
         const int64_t sk = a.p2 ? (int64_t)a.p2[k] : k;
         const int64_t sl0 = a.p3 ? (int64_t)a.p3[l] : l, sl1 = a.p3 ? (int64_t)a.p3[l + 1] : l + 1;
+        // COMMON offsets (in words) of this thread's digit words and key pairs within every term
+        const KView& P = a.parts[0];
+        const KView& K = a.keys[0];
+        const int64_t po = i * P.s0 + j * P.s1 + sk * P.s2, po0 = po + (P.b3 ? 0 : sl0), po1 = po + (P.b3 ? 0 : sl1);
+        const int64_t ko0 = j * K.s1 + k * K.s2 + l, ko1 = ko0 + K.s0;
         auto issue = [&](int t) {
             if (t < a.nterms) {
                 const int s = t % KS_STAGES;
-                cp_async8(&sx[s][0][tid], kat<int64_t>(a.parts[t], i, j, sk, sl0));
-                cp_async8(&sx[s][1][tid], kat<int64_t>(a.parts[t], i, j, sk, sl1));
-                cp_async16(&skey[s][0][tid], kat<int64_t>(a.keys[t], 0, j, k, l));
-                cp_async16(&skey[s][1][tid], kat<int64_t>(a.keys[t], 1, j, k, l));
+                if (COMMON) {
+                    const int64_t* pp = reinterpret_cast<const int64_t*>(a.parts[t].p);
+                    const int64_t* kp = reinterpret_cast<const int64_t*>(a.keys[t].p);
+                    cp_async8(&sx[s][0][tid], pp + po0);
+                    cp_async8(&sx[s][1][tid], pp + po1);
+                    cp_async16(&skey[s][0][tid], kp + ko0);
+                    cp_async16(&skey[s][1][tid], kp + ko1);
+                } else {
+                    cp_async8(&sx[s][0][tid], kat<int64_t>(a.parts[t], i, j, sk, sl0));
+                    cp_async8(&sx[s][1][tid], kat<int64_t>(a.parts[t], i, j, sk, sl1));
+                    cp_async16(&skey[s][0][tid], kat<int64_t>(a.keys[t], 0, j, k, l));
+                    cp_async16(&skey[s][1][tid], kat<int64_t>(a.keys[t], 1, j, k, l));
+                }
             }
             cp_async_commit();  // an empty group past the end keeps the count uniform
         };
@@ -419,29 +437,40 @@ struct GiantArgs {
     KView dst;                     // [2 used, ...]
 };
 
+/// The lcoef values of a tile's line (j, k) are the same for all its positions: the CTA stages
+/// them in shared memory once per tile (nt words, dynamic shared memory), and each thread forms
+/// its baby-step addresses from one base offset and the row stride, so that the loop spends its
+/// issue slots on the products rather than on 64-bit address arithmetic and uniform loads.
 __global__ void __launch_bounds__(256) giant_kernel(GiantArgs a, KMods m, const int64_t* one, int64_t lines,
                                                     int chunks) {
+    extern __shared__ int64_t slc[];  // lcoef[t, j, k] for the tile's (j, k), t < a.lcoef.n0
     const int64_t tiles = lines * chunks;
+    const int nt = (int)a.lcoef.n0;
     for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        int64_t line = tile / chunks;  // (j, k)
-        int64_t l = (tile - line * chunks) * blockDim.x + threadIdx.x;
+        const int64_t line = tile / chunks;  // (j, k)
+        const int64_t l = (tile - line * chunks) * blockDim.x + threadIdx.x;
+        const int64_t k = line % a.dst.n2, j = line / a.dst.n2;
+        __syncthreads();  // the previous tile's readers of slc are done
+        for (int t = threadIdx.x; t < nt; t += blockDim.x) slc[t] = *kat<int64_t>(a.lcoef, t, j, k, 0);
+        __syncthreads();
         if (l >= a.dst.n3) continue;
-        int64_t k = line % a.dst.n2, j = line / a.dst.n2;
+        const int64_t rs = a.babies.s0;  // row stride of the baby-step tensor
+        const int64_t* xb = kat<int64_t>(a.babies, 0, j, k, l);
         i128 acc0[GIANT_OUT], acc1[GIANT_OUT];
 #pragma unroll
         for (int o = 0; o < GIANT_OUT; o++) acc0[o] = acc1[o] = 0;
         for (int bj = 0; bj < a.nbaby; bj++) {
             const int lf = a.lfirst[bj], lc = a.lcount[bj];
-            for (int i = 0; i < a.d; i++) {
+            const int64_t* xr = xb + (int64_t)bj * 2 * a.d * rs;
+            for (int i = 0; i < a.d; i++, xr += 2 * rs) {
                 // input digit i feeds output digits i + jj, jj < lc; skip it when none is in range
                 if (i + lc <= a.out0 || i >= a.out0 + a.nout) continue;
-                const int64_t row = (int64_t)bj * 2 * a.d + 2 * i;
-                const int64_t x0 = *kat<int64_t>(a.babies, row, j, k, l), x1 = *kat<int64_t>(a.babies, row + 1, j, k, l);
+                const int64_t x0 = xr[0], x1 = xr[rs];
 #pragma unroll
                 for (int o = 0; o < GIANT_OUT; o++) {
                     const int jj = a.out0 + o - i;
                     if (o < a.nout && jj >= 0 && jj < lc) {
-                        const int64_t f = *kat<int64_t>(a.lcoef, lf + jj, j, k, 0);
+                        const int64_t f = slc[lf + jj];
                         acc0[o] = (i128)((u128)acc0[o] + (u128)((i128)x0 * (i128)f));
                         acc1[o] = (i128)((u128)acc1[o] + (u128)((i128)x1 * (i128)f));
                     }
@@ -555,7 +584,14 @@ hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys
         return cuda_check(cudaGetLastError(), "keyswitch kernel launch");
     }
     grid_lines(ctx, dst.n3 / 2, lines, &chunks, &blocks);
-    keyswitch_async_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(a, m, one_dev, lines, chunks);
+    bool common = true;
+    for (int t = 1; t < nterms; t++) {
+        const KView &p = parts[t], &p0 = parts[0], &k = keys[t], &k0 = keys[0];
+        common = common && p.s0 == p0.s0 && p.s1 == p0.s1 && p.s2 == p0.s2 && p.b3 == p0.b3 && k.s0 == k0.s0 &&
+                 k.s1 == k0.s1 && k.s2 == k0.s2;
+    }
+    if (common) keyswitch_async_kernel<true><<<blocks, 256, 0, stream_of(ctx)>>>(a, m, one_dev, lines, chunks);
+    else keyswitch_async_kernel<false><<<blocks, 256, 0, stream_of(ctx)>>>(a, m, one_dev, lines, chunks);
     count_launch(ctx);
     return cuda_check(cudaGetLastError(), "keyswitch kernel launch");
 }
@@ -581,12 +617,14 @@ hc_status launch_giant(hc_context ctx, const KView& babies, const KView& lcoef, 
     int chunks;
     unsigned blocks;
     grid_lines(ctx, dst.n3, lines, &chunks, &blocks);
+    const size_t smem = (size_t)std::max<int64_t>(lcoef.n0, 1) * 8;  // the tile's lcoef words
+    if (smem > 49152) return fail(HC_ERR_UNSUPPORTED, "too many coefficient digits");
     for (int o0 = 0; o0 < used; o0 += GIANT_OUT) {
         a.out0 = o0;
         a.nout = std::min(GIANT_OUT, used - o0);
         a.full = 0;
         for (int o = 0; o < a.nout; o++) a.full |= (unsigned)(full[o0 + o] != 0) << o;
-        giant_kernel<<<blocks, 256, 0, stream_of(ctx)>>>(a, m, one_dev, lines, chunks);
+        giant_kernel<<<blocks, 256, smem, stream_of(ctx)>>>(a, m, one_dev, lines, chunks);
         count_launch(ctx);
         hc_status st = cuda_check(cudaGetLastError(), "giant-step kernel launch");
         if (st) return st;
