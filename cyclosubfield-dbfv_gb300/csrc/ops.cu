@@ -93,76 +93,38 @@ __global__ void __launch_bounds__(256) pw_line_kernel(KView d, KView a, KView b,
     for (int64_t l = l0 + threadIdx.x; l < l1; l += 256) pw_apply<OP>(d, a, b, m, i, j, k, l);
 }
 
-/// acc += s0 + (s2 - s0 - s1) 2^29 + s1 2^58: the Karatsuba column sums of 29-bit limb products.
-__device__ __forceinline__ i128 fold29(i128 acc, int64_t s0, int64_t s1, int64_t s2) {
-    const u128 mid = (u128)((i128)s2 - (i128)s0 - (i128)s1);
-    return (i128)((u128)acc + (u128)(i128)s0 + (mid << 29) + ((u128)(i128)s1 << 58));
-}
-
 /// dst[i,j,k,l] = sum_u lhs[li,j,u,0] * rhs[ri,u,k,l] (src/hal/cpu.rs:791-818), i128 wrapping.
 /// Four output rows j per pass share each rhs load (the matrix entries are warp-uniform loads),
 /// and columns whose four entries are zero are skipped (a gadget conversion matrix is zero outside
-/// each digit's columns). Products whose operands fit (|x| < 2^57, |c| < 2^56: lifts of 57-bit
-/// residues times centred matrix entries, as the base conversions pass them) are formed from
-/// 29-bit limbs (x = x1 2^29 + x0, 0 <= x0 < 2^29): three 32 x 32 -> 64-bit products per term into
-/// int64 column sums (Karatsuba middle column), which stay below 2^63 over 16 terms and are then
-/// folded into the i128 sum; other products are formed whole. Every product is exact either way,
-/// so the wrapping sums are the same.
+/// each digit's columns); the sums are the same wrapping sums.
 __global__ void __launch_bounds__(256) matmul_kernel(KView d, KView lhs, KView rhs, int64_t U, int64_t lines,
                                                      int chunks) {
     const int64_t tiles = lines * chunks;
-    constexpr int64_t M29 = ((int64_t)1 << 29) - 1;
     for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         int64_t line = tile / chunks;  // (i, k)
         int64_t l = (tile - line * chunks) * blockDim.x + threadIdx.x;
         if (l >= d.n3) continue;
         int64_t k = line % d.n2, i = line / d.n2;
-        const int64_t* rp = kat<int64_t>(rhs, i, 0, k, l);  // rhs row u at u * rhs.s1
         int64_t j = 0;
         for (; j + 4 <= d.n1; j += 4) {
-            const int64_t* cp = kat<int64_t>(lhs, i, j, 0, 0);  // entry (q, u) at q * s1 + u * s2
             i128 acc[4] = {0, 0, 0, 0};
-            int64_t sm[4][3] = {};
-            int pending = 0;
             for (int64_t u = 0; u < U; u++) {
                 int64_t c[4];
 #pragma unroll
-                for (int q = 0; q < 4; q++) c[q] = cp[q * lhs.s1 + u * lhs.s2];
-                if ((c[0] | c[1] | c[2] | c[3]) == 0) continue;  // zero columns add nothing
-                const int64_t x = rp[u * rhs.s1];
-                bool fit = x >= -((int64_t)1 << 57) && x < ((int64_t)1 << 57);
+                for (int q = 0; q < 4; q++) c[q] = *kat<int64_t>(lhs, i, j + q, u, 0);
+                if ((c[0] | c[1] | c[2] | c[3]) == 0) continue;  // zero columns (a gadget matrix's) add nothing
+                const int64_t x = *kat<int64_t>(rhs, i, u, k, l);
 #pragma unroll
-                for (int q = 0; q < 4; q++) fit = fit && c[q] >= -((int64_t)1 << 56) && c[q] < ((int64_t)1 << 56);
-                if (fit) {
-                    const int x0 = (int)(x & M29), x1 = (int)(x >> 29), xs = x0 + x1;
-#pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        const int c0 = (int)(c[q] & M29), c1 = (int)(c[q] >> 29);
-                        sm[q][0] += (int64_t)x0 * c0;
-                        sm[q][1] += (int64_t)x1 * c1;
-                        sm[q][2] += (int64_t)xs * (c0 + c1);
-                    }
-                    if (++pending == 16) {
-#pragma unroll
-                        for (int q = 0; q < 4; q++) {
-                            acc[q] = fold29(acc[q], sm[q][0], sm[q][1], sm[q][2]);
-                            sm[q][0] = sm[q][1] = sm[q][2] = 0;
-                        }
-                        pending = 0;
-                    }
-                } else {
-#pragma unroll
-                    for (int q = 0; q < 4; q++) acc[q] = (i128)((u128)acc[q] + (u128)((i128)c[q] * (i128)x));
-                }
+                for (int q = 0; q < 4; q++) acc[q] = (i128)((u128)acc[q] + (u128)((i128)c[q] * (i128)x));
             }
 #pragma unroll
-            for (int q = 0; q < 4; q++) st128(kat<longlong2>(d, i, j + q, k, l), fold29(acc[q], sm[q][0], sm[q][1], sm[q][2]));
+            for (int q = 0; q < 4; q++) st128(kat<longlong2>(d, i, j + q, k, l), acc[q]);
         }
         for (; j < d.n1; j++) {
             i128 acc = 0;
             for (int64_t u = 0; u < U; u++) {
                 int64_t c = *kat<int64_t>(lhs, i, j, u, 0);
-                int64_t x = rp[u * rhs.s1];
+                int64_t x = *kat<int64_t>(rhs, i, u, k, l);
                 acc = (i128)((u128)acc + (u128)((i128)c * (i128)x));
             }
             st128(kat<longlong2>(d, i, j, k, l), acc);
