@@ -378,15 +378,13 @@ def test_int8_mma_peak(be):
 def test_matmul_zero_columns_and_row_remainders(be, po):
     """A gadget-style conversion matrix [d, r + 1, r, 1], zero outside each digit's columns (the
     kernel skips all-zero column groups), with output row counts that are not multiples of four,
-    right-hand values that fit the kernel's 29-bit limb products and values that do not, against
-    the oracle."""
+    57-bit and 63-bit right-hand values, against the oracle."""
     g = rng(41)
     d, r = 4, 16
     for rows, xbits in ((r + 1, 57), (6, 57), (3, 57), (r + 1, 63)):
         lhs = np.zeros((d, rows, r, 1), dtype=np.int64)
         for i in range(d):
             lhs[i, :, 4 * i:4 * i + 4, 0] = rand_i64(g, (rows, 4), -(1 << 56), (1 << 56) - 1)
-        # 57-bit right-hand values take the limb products; 63-bit ones (some lanes) the whole ones
         rhs = rand_i64(g, (1, r, 12, 64), -(1 << xbits), (1 << xbits) - 1)
         exp = rand_i128(g, (d, rows, 12, 64))
         po.matmul_i64(exp, lhs, rhs)
