@@ -438,45 +438,70 @@ struct GiantArgs {
 };
 
 /// The lcoef values of a tile's line (j, k) are the same for all its positions: the CTA stages
-/// them in shared memory once per tile (nt words, dynamic shared memory), and each thread forms
-/// its baby-step addresses from one base offset and the row stride, so that the loop spends its
-/// issue slots on the products rather than on 64-bit address arithmetic and uniform loads.
-__global__ void __launch_bounds__(256) giant_kernel(GiantArgs a, KMods m, const int64_t* one, int64_t lines,
-                                                    int chunks) {
-    extern __shared__ int64_t slc[];  // lcoef[t, j, k] for the tile's (j, k), t < a.lcoef.n0
+/// them in shared memory once per tile (nt words, dynamic shared memory, after the staging
+/// buffers). The (baby step, input digit) units that feed an output digit of the launch are listed
+/// by the host (`units`, in giant step order); each thread copies its positions' two words of the
+/// next GIANT_STAGES - 1 units into shared memory with cp.async while it multiplies the current
+/// one, so that its loads in flight take no registers, and forms every address from one base
+/// offset and the row stride. Each thread copies and reads only its own slots.
+constexpr int GIANT_STAGES = 4;
+constexpr int GIANT_MAX_UNITS = 1024;
+
+struct GiantUnits {
+    unsigned short u[GIANT_MAX_UNITS];  // (baby step << 6) | input digit
+    int n;
+};
+
+__global__ void __launch_bounds__(256) giant_kernel(GiantArgs a, GiantUnits un, KMods m, const int64_t* one,
+                                                    int64_t lines, int chunks) {
+    extern __shared__ int64_t gsm[];  // [GIANT_STAGES][2][256] staging, then the tile's lcoef
+    int64_t* slc = gsm + GIANT_STAGES * 2 * 256;
     const int64_t tiles = lines * chunks;
     const int nt = (int)a.lcoef.n0;
+    const int tid = threadIdx.x;
     for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const int64_t line = tile / chunks;  // (j, k)
-        const int64_t l = (tile - line * chunks) * blockDim.x + threadIdx.x;
+        const int64_t l = (tile - line * chunks) * blockDim.x + tid;
         const int64_t k = line % a.dst.n2, j = line / a.dst.n2;
         __syncthreads();  // the previous tile's readers of slc are done
-        for (int t = threadIdx.x; t < nt; t += blockDim.x) slc[t] = *kat<int64_t>(a.lcoef, t, j, k, 0);
+        for (int t = tid; t < nt; t += blockDim.x) slc[t] = *kat<int64_t>(a.lcoef, t, j, k, 0);
         __syncthreads();
         if (l >= a.dst.n3) continue;
         const int64_t rs = a.babies.s0;  // row stride of the baby-step tensor
         const int64_t* xb = kat<int64_t>(a.babies, 0, j, k, l);
+        auto issue = [&](int u) {
+            if (u < un.n) {
+                const int bj = un.u[u] >> 6, i = un.u[u] & 63;
+                const int64_t* xr = xb + ((int64_t)bj * 2 * a.d + 2 * i) * rs;
+                int64_t* slot = gsm + (u % GIANT_STAGES) * 512;
+                cp_async8(slot + tid, xr);
+                cp_async8(slot + 256 + tid, xr + rs);
+            }
+            cp_async_commit();  // an empty group past the end keeps the count uniform
+        };
+#pragma unroll
+        for (int u = 0; u < GIANT_STAGES - 1; u++) issue(u);
         i128 acc0[GIANT_OUT], acc1[GIANT_OUT];
 #pragma unroll
         for (int o = 0; o < GIANT_OUT; o++) acc0[o] = acc1[o] = 0;
-        for (int bj = 0; bj < a.nbaby; bj++) {
+        for (int u = 0; u < un.n; u++) {
+            issue(u + GIANT_STAGES - 1);
+            cp_async_wait<GIANT_STAGES - 1>();  // unit u's words have landed
+            const int bj = un.u[u] >> 6, i = un.u[u] & 63;
             const int lf = a.lfirst[bj], lc = a.lcount[bj];
-            const int64_t* xr = xb + (int64_t)bj * 2 * a.d * rs;
-            for (int i = 0; i < a.d; i++, xr += 2 * rs) {
-                // input digit i feeds output digits i + jj, jj < lc; skip it when none is in range
-                if (i + lc <= a.out0 || i >= a.out0 + a.nout) continue;
-                const int64_t x0 = xr[0], x1 = xr[rs];
+            const int64_t* slot = gsm + (u % GIANT_STAGES) * 512;
+            const int64_t x0 = slot[tid], x1 = slot[256 + tid];
 #pragma unroll
-                for (int o = 0; o < GIANT_OUT; o++) {
-                    const int jj = a.out0 + o - i;
-                    if (o < a.nout && jj >= 0 && jj < lc) {
-                        const int64_t f = slc[lf + jj];
-                        acc0[o] = (i128)((u128)acc0[o] + (u128)((i128)x0 * (i128)f));
-                        acc1[o] = (i128)((u128)acc1[o] + (u128)((i128)x1 * (i128)f));
-                    }
+            for (int o = 0; o < GIANT_OUT; o++) {
+                const int jj = a.out0 + o - i;
+                if (o < a.nout && jj >= 0 && jj < lc) {
+                    const int64_t f = slc[lf + jj];
+                    acc0[o] = (i128)((u128)acc0[o] + (u128)((i128)x0 * (i128)f));
+                    acc1[o] = (i128)((u128)acc1[o] + (u128)((i128)x1 * (i128)f));
                 }
             }
         }
+        cp_async_wait<0>();
 #pragma unroll
         for (int o = 0; o < GIANT_OUT; o++) {
             if (o >= a.nout) break;
@@ -617,14 +642,24 @@ hc_status launch_giant(hc_context ctx, const KView& babies, const KView& lcoef, 
     int chunks;
     unsigned blocks;
     grid_lines(ctx, dst.n3, lines, &chunks, &blocks);
-    const size_t smem = (size_t)std::max<int64_t>(lcoef.n0, 1) * 8;  // the tile's lcoef words
+    // the staging buffers and the tile's lcoef words
+    const size_t smem = (size_t)(GIANT_STAGES * 2 * 256 + std::max<int64_t>(lcoef.n0, 1)) * 8;
     if (smem > 49152) return fail(HC_ERR_UNSUPPORTED, "too many coefficient digits");
+    if (d >= 64) return fail(HC_ERR_UNSUPPORTED, "too many dBFV digits");
     for (int o0 = 0; o0 < used; o0 += GIANT_OUT) {
         a.out0 = o0;
         a.nout = std::min(GIANT_OUT, used - o0);
         a.full = 0;
         for (int o = 0; o < a.nout; o++) a.full |= (unsigned)(full[o0 + o] != 0) << o;
-        giant_kernel<<<blocks, 256, smem, stream_of(ctx)>>>(a, m, one_dev, lines, chunks);
+        GiantUnits un;  // the (baby step, input digit) units that feed an output digit of this launch
+        un.n = 0;
+        for (int bj = 0; bj < nbaby; bj++)
+            for (int i = 0; i < d; i++) {
+                if (i + lcount[bj] <= a.out0 || i >= a.out0 + a.nout) continue;
+                if (un.n == GIANT_MAX_UNITS) return fail(HC_ERR_UNSUPPORTED, "too many baby-step units");
+                un.u[un.n++] = (unsigned short)((bj << 6) | i);
+            }
+        giant_kernel<<<blocks, 256, smem, stream_of(ctx)>>>(a, un, m, one_dev, lines, chunks);
         count_launch(ctx);
         hc_status st = cuda_check(cudaGetLastError(), "giant-step kernel launch");
         if (st) return st;
