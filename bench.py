@@ -533,6 +533,26 @@ def serving_bench(be, n=4000, rate=2000.0):
     return out
 
 
+def ct_mult_int_work(work, ms_per_ct_mult, bpeak):
+    """The exact integer work of one ct-mult: the CRT transforms' Barrett products (TRANSFORM_PRODUCTS
+    per residue of every transformed (row, prime) slab: both operands' crt_to_pb, the lifted
+    extension rows' pb_to_crt, the product's crt_to_pb over the lifted base, the relinearised
+    (c0, c1) rows' pb_to_crt and the gadget digits' pb_to_crt) and the base conversions' terms
+    (source x destination products plus the correction row: both lifts, rescale's two conversions,
+    the gadget decomposition). `ntt_time_frac` is the time those products would take at the
+    measured Barrett rate, as a fraction of the measured time per ct-mult."""
+    R, r, d = work.ring, work.r, len(work.digits)
+    e = len(R.extension_base(work.base))
+    slabs = 2 * 2 * r + 2 * 2 * e + 3 * (r + e) + 2 * r + d * r
+    products = slabs * R.n * TRANSFORM_PRODUCTS[FIELD]
+    per_digit = -(-r // d)
+    terms = (2 * 2 * (r * e + r) + 3 * (r * e + r) + 3 * (e * r + e) + d * (r * per_digit + per_digit)) * R.n
+    return {"transformed_slabs": slabs, "barrett_products": products, "conversion_terms": terms,
+            "ntt_time_frac": round(products / bpeak / (ms_per_ct_mult * 1e-3), 4),
+            "note": "the transforms' products at the measured Barrett rate take this fraction of a batched ct-mult; "
+                    "the conversions (29-bit limb products on the same pipe) and the key switch take most of the rest"}
+
+
 def trait_path_bench(be, work, reps=20):
     """The reference crate's own bfv_hom_mul call sequence issued through the hal::Backend trait
     entry points only (trait_ring.py: what the unchanged crate runs above a hal::cuda backend), on
@@ -1183,6 +1203,7 @@ def main():
     batched = {"ct_mults_per_s": round(work.batch * nb / (batched_ms * 1e-3), 3), "batch": work.batch,
                "ms_per_step": round(batched_ms / nb, 4), "steps": nb,
                "l2": "flushed before every step (512 MB memset, untimed)"}
+    batched["int_work"] = ct_mult_int_work(work, batched_ms / nb / work.batch, halcuda.barrett_peak(be))
 
     # plain form (one ct-mult per timed call) and its latency distribution
     per = plain_calls(be, work, min(20, max(2, args.steps // 2)), scratch)
