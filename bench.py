@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-homcrt", action="store_true", help="skip the homomorphic CRT transform workload")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--no-trait-path", action="store_true", help="skip the trait-level ct-mult")
+    ap.add_argument("--crt-elements", type=int, default=512,
+                    help="elements of the batched CRT workload with --only crt_batch (512: the configuration's)")
     ap.add_argument("--only", choices=["crt_batch", "homcrt", "serving", "trait_path"],
                     help="run just this workload and print its result (for profiling it alone)")
     ap.add_argument("--roofline-only", action="store_true",
@@ -350,7 +352,7 @@ class CrtWorkload:
         R.crt_to_pb(xi, base)
 
 
-def crt_batch_bench(be, steps, warmup, bpeak=None, peaks=None):
+def crt_batch_bench(be, steps, warmup, bpeak=None, peaks=None, elements=512):
     """CRT transforms/s (2 per element: forward and inverse) batched (graph replay of the persistent
     launch) and plain (one element at a time); inputs ~2.5 GB, larger than L2. After the timing a
     seeded sample of elements is run once more through the batch and compared with the plain form
@@ -359,7 +361,7 @@ def crt_batch_bench(be, steps, warmup, bpeak=None, peaks=None):
 
     import halcuda
 
-    w = CrtWorkload(be)
+    w = CrtWorkload(be, elements)
     ev0, ev1 = halcuda.Event(), halcuda.Event()
     for _ in range(warmup):
         w.graph.launch()
@@ -1155,7 +1157,7 @@ def main():
     be = halcuda.CudaBackend(dist.local_rank)
     if args.only:
         fn = {"crt_batch": lambda: crt_batch_bench(be, max(3, args.steps // 2), args.warmup,
-                                                   halcuda.barrett_peak(be), load_peaks()),
+                                                   halcuda.barrett_peak(be), load_peaks(), args.crt_elements),
               "homcrt": lambda: homcrt_bench(be, reps=max(1, args.steps // 3)),
               "serving": lambda: serving_bench(be),
               "trait_path": lambda: trait_path_bench(be, Workload(be, 1))}[args.only]
