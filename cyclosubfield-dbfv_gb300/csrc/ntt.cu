@@ -677,6 +677,7 @@ __global__ void __launch_bounds__(256, HC_NTT_MIN_BLOCKS) ntt_tile_kernel(KView 
 /// column blocks of 2^logv columns (dimension 2). Modes as tile_run; `mulrow` is the CRT kernel
 /// row of the pass (modes 2 and 3 along dimension 2, mode 2 along dimension 3), while mode 3
 /// along dimension 3 multiplies by the slab's operand.
+template <bool GENERIC>
 __device__ __forceinline__ void slab_pass(const CrtSlab& S, const DevPlanHeader* P, const int64_t* tw, int64_t* s,
                                           int dim, int mode, const int64_t* mulrow, int logv) {
     // specialised kernels for slabs whose plans have the fixed schedule (bit 16: dimension-3
@@ -693,9 +694,15 @@ __device__ __forceinline__ void slab_pass(const CrtSlab& S, const DevPlanHeader*
                 else if (mode == 3) run_line<HC_SHAPE_L3072, 3, true>(P, c, s, g, mulp, 1, S.n, S.ninv);
                 else run_line<HC_SHAPE_L3072, 1, true>(P, c, s, g, mulp, 1, S.n, S.ninv);
             } else {
-                if (mode == 2) run_line<HC_SHAPE_L12288, 2, true>(P, c, s, g, mulp, 1, S.n, S.ninv);
-                else if (mode == 3) run_line<HC_SHAPE_L12288, 3, true>(P, c, s, g, mulp, 1, S.n, S.ninv);
-                else run_line<HC_SHAPE_L12288, 1, true>(P, c, s, g, mulp, 1, S.n, S.ninv);
+                // one 4096-residue block in shared memory at a time (crt_slab_tile_words)
+                if (mode & 1) {
+                    const FixedSched<HC_SHAPE_L12288, true> sch{P->inv};
+                    fast::line12288_seq<1>(sch, c, s, g, mulp, 1, S.n, S.ninv);
+                } else {
+                    const FixedSched<HC_SHAPE_L12288, false> sch{P->fwd};
+                    if (mode == 2) fast::line12288_seq<2>(sch, c, s, g, mulp, 1, S.n, S.ninv);
+                    else fast::line12288_seq<3>(sch, c, s, g, mulp, 1, S.n, S.ninv);
+                }
             }
             __syncthreads();
         }
@@ -719,6 +726,7 @@ __device__ __forceinline__ void slab_pass(const CrtSlab& S, const DevPlanHeader*
         __syncthreads();
         return;
     }
+    if constexpr (!GENERIC) return;  // the launcher sends only specialised slabs to this form
     TileIO io;
     io.mn = S.n, io.mi = S.ninv;
     io.me = 1, io.mv = 0;
@@ -746,7 +754,12 @@ __device__ __forceinline__ void slab_pass(const CrtSlab& S, const DevPlanHeader*
 /// its `ops` say) before taking another. Slabs of different fields and RNS lengths mix freely;
 /// the passes are the HAL transforms' passes in the same order (src/ring.rs:1118-1161), the
 /// operand product fused into the epilogue of the forward transform's last pass.
-__global__ void __launch_bounds__(256, 2)
+/// GENERIC = false: every slab has the specialised line and column shapes with compiled-in
+/// schedules (both large fields' rings), so the generic tile programme is left out; MINB: the CTAs
+/// of 256 threads per SM the register allocation must allow (2: 128 registers; 3: 80, with some
+/// spilling), chosen through the autotuned CTAs per SM. GENERIC = true serves other slabs.
+template <bool GENERIC, int MINB>
+__global__ void __launch_bounds__(256, MINB)
     crt_batch_kernel(const CrtSlab* __restrict__ slabs, int nslabs, int* counter, int logv, int tile_words) {
     extern __shared__ int64_t smem[];
     __shared__ int s_next;
@@ -765,10 +778,10 @@ __global__ void __launch_bounds__(256, 2)
         stage_twiddles(P3, tw3);
         __syncthreads();
         if (S.ops & HC_CRT_FORWARD) {
-            slab_pass(S, P2, tw2, smem, 2, 2, S.kl, logv);
-            slab_pass(S, P3, tw3, smem, 3, 2, S.kk, logv);
-            slab_pass(S, P2, tw2, smem, 2, 1, nullptr, logv);
-            slab_pass(S, P3, tw3, smem, 3, (S.ops & HC_CRT_MUL) ? 3 : 1, nullptr, logv);
+            slab_pass<GENERIC>(S, P2, tw2, smem, 2, 2, S.kl, logv);
+            slab_pass<GENERIC>(S, P3, tw3, smem, 3, 2, S.kk, logv);
+            slab_pass<GENERIC>(S, P2, tw2, smem, 2, 1, nullptr, logv);
+            slab_pass<GENERIC>(S, P3, tw3, smem, 3, (S.ops & HC_CRT_MUL) ? 3 : 1, nullptr, logv);
         } else if (S.ops & HC_CRT_MUL) {
             const int total = S.dl * S.dk;
             for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
@@ -779,10 +792,10 @@ __global__ void __launch_bounds__(256, 2)
             __syncthreads();
         }
         if (S.ops & HC_CRT_INVERSE) {
-            slab_pass(S, P2, tw2, smem, 2, 2, S.ikl, logv);
-            slab_pass(S, P3, tw3, smem, 3, 2, S.ikk, logv);
-            slab_pass(S, P2, tw2, smem, 2, 1, nullptr, logv);
-            slab_pass(S, P3, tw3, smem, 3, 1, nullptr, logv);
+            slab_pass<GENERIC>(S, P2, tw2, smem, 2, 2, S.ikl, logv);
+            slab_pass<GENERIC>(S, P3, tw3, smem, 3, 2, S.ikk, logv);
+            slab_pass<GENERIC>(S, P2, tw2, smem, 2, 1, nullptr, logv);
+            slab_pass<GENERIC>(S, P3, tw3, smem, 3, 1, nullptr, logv);
         }
     }
 }
@@ -1016,6 +1029,20 @@ int32_t plan_len(hc_ntt_plan p) { return p->len; }
 const void* plan_device(hc_ntt_plan p) { return p->dev; }
 int32_t plan_ntw(hc_ntt_plan p) { return p->ntw; }
 int32_t plan_shape(hc_ntt_plan p) { return p->shape | (p->fixed ? 0x100 : 0); }
+/// Shared-memory words a slab of the batched transform needs: a padded 3072-residue line, one padded
+/// 4096-residue block of a 12288-residue line (line12288_seq), or the generic tile (the whole line,
+/// or deg_L' x 2^logv dimension-2 columns); the specialised column passes use none.
+size_t crt_slab_tile_words(int32_t shapes, int32_t dl, int32_t dk, int logv) {
+    const int s3 = shapes & 0xff, s2 = (shapes >> 8) & 0xff;
+    const bool f3 = (shapes >> 16) & 1, f2 = (shapes >> 17) & 1;
+    const size_t w3 = !f3 ? (size_t)dk
+                          : s3 == HC_SHAPE_L3072 ? (size_t)line_tile_words(HC_SHAPE_L3072)
+                          : s3 == HC_SHAPE_L12288 ? (size_t)(4096 + 4096 / 8) : (size_t)dk;
+    const size_t w2 = f2 && (s2 == HC_SHAPE_C12 || s2 == HC_SHAPE_C4) ? 0 : ((size_t)dl << logv);
+    const size_t w = std::max(w3, w2);
+    return (w + 1) & ~(size_t)1;
+}
+
 int32_t plan_tile_words(hc_ntt_plan p) {
     return p->shape == HC_SHAPE_L3072 || p->shape == HC_SHAPE_L12288 ? line_tile_words(p->shape) : 0;
 }
@@ -1023,17 +1050,26 @@ int32_t plan_tile_words(hc_ntt_plan p) {
 /// Launches the persistent batched-transform kernel over `nslabs` device slab descriptors.
 /// `tile_words`: largest tile (deg_K, or deg_L' x 2^logv); `tw_words`: largest pair of twiddle
 /// tables (dimension-2 + dimension-3 plan) of a slab. `counter` is reset on the stream first.
+/// Whether a slab runs entirely on the specialised line and column code (crt_batch_kernel<false>).
+bool crt_slab_specialised(int32_t shapes) {
+    const int s3 = shapes & 0xff, s2 = (shapes >> 8) & 0xff;
+    return ((shapes >> 16) & 1) && (s3 == HC_SHAPE_L3072 || s3 == HC_SHAPE_L12288) && ((shapes >> 17) & 1) &&
+           (s2 == HC_SHAPE_C12 || s2 == HC_SHAPE_C4);
+}
+
 hc_status launch_crt_batch(hc_context ctx, const CrtSlab* slabs, int nslabs, int* counter, size_t tile_words,
-                           size_t tw_words, const CrtLaunch& L) {
+                           size_t tw_words, const CrtLaunch& L, bool generic) {
     if (nslabs <= 0) return HC_OK;
+    auto kern = generic ? crt_batch_kernel<true, 2>
+                        : (L.ctas_per_sm >= 3 ? crt_batch_kernel<false, 3> : crt_batch_kernel<false, 2>);
     if (L.threads < 32 || L.threads > 256 || L.threads % 32) return fail(HC_ERR_ARG, "batched transform: threads per CTA");
     if (L.logv < 0 || L.logv > 6) return fail(HC_ERR_ARG, "batched transform: dimension-2 tile width");
     const size_t smem = (tile_words + tw_words) * 8;
     if (smem > max_smem_optin(ctx)) return fail(HC_ERR_UNSUPPORTED, "batched transform: slab tiles exceed shared memory");
-    cudaError_t e = cudaFuncSetAttribute(crt_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_check(e, "batched transform smem attribute");
     int occ = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, crt_batch_kernel, L.threads, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, L.threads, smem);
     if (e != cudaSuccess) return cuda_check(e, "batched transform occupancy");
     if (occ < 1) return fail(HC_ERR_UNSUPPORTED, "batched transform: launch shape does not fit an SM");
     int per = L.ctas_per_sm < 1 ? 1 : (L.ctas_per_sm < occ ? L.ctas_per_sm : occ);
@@ -1041,8 +1077,8 @@ hc_status launch_crt_batch(hc_context ctx, const CrtSlab* slabs, int nslabs, int
     if (grid > nslabs) grid = nslabs;
     hc_status st = cuda_check(cudaMemsetAsync(counter, 0, sizeof(int), stream_of(ctx)), "batched transform counter");
     if (st) return st;
-    crt_batch_kernel<<<(unsigned)grid, (unsigned)L.threads, smem, stream_of(ctx)>>>(slabs, nslabs, counter, L.logv,
-                                                                                  (int)tile_words);
+    kern<<<(unsigned)grid, (unsigned)L.threads, smem, stream_of(ctx)>>>(slabs, nslabs, counter, L.logv,
+                                                                      (int)tile_words);
     count_launch(ctx);
     return cuda_check(cudaGetLastError(), "batched transform launch");
 }

@@ -492,6 +492,68 @@ __device__ __forceinline__ void line12288_block(const SCH& sch, const Ctx& c, in
     line_store(s, g + 4096 * blk, 4096, MODE & 2, mulp + (me ? 4096 * blk : 0), me, mn, mi);
 }
 
+/// A [3, 64, 64] line with a tile of one 4096-residue block (for kernels that cannot give a CTA the
+/// whole 12288-residue line): stage 0, the factor-3 stage that couples the three blocks, runs in
+/// place in global memory, each thread owning whole position triples (the butterfly of line12288's
+/// first pass); stages 1..12, which act within a block, then run block by block exactly as
+/// line12288_block runs them. The first pass's global writes are the CTA's own, visible to its
+/// threads after the barrier.
+template <int MODE, class SCH>
+__device__ __forceinline__ void line12288_seq(const SCH& sch, const Ctx& c, int64_t* s, int64_t* g,
+                                              const int64_t* mulp, int64_t me, int64_t mn, int64_t mi) {
+    constexpr bool inv = MODE & 1, reduce_output = MODE == 0;
+    SF f[4];
+    bool fz[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        f[q] = sflags(sch, q);
+        fz[q] = f[q].last && reduce_output;
+    }
+    for (int p = threadIdx.x; p < 4096; p += blockDim.x) {
+        int64_t a = g[p], b = g[p + 4096], d = g[p + 8192];
+        if (f[0].red) {
+            a = red1(c, a);
+            b = red1(c, b);
+            d = red1(c, d);
+        }
+        if (!inv) fwd3<true>(c, f[0], fz[0], 0, a, b, d);
+        else inv3(c, f[0], a, b, d);
+        g[p] = a, g[p + 4096] = b, g[p + 8192] = d;
+    }
+    __syncthreads();
+    constexpr int span = inv ? 64 : 512;
+    for (int blk = 0; blk < 3; blk++) {
+        int64_t* gb = g + 4096 * blk;
+        for (int gg = threadIdx.x; gg < 512; gg += blockDim.x) {
+            const int base = inv ? ((gg >> 6) << 9) + (gg & 63) : gg;
+            int64_t x[8];
+#pragma unroll
+            for (int m = 0; m < 8; m++) x[m] = gb[base + span * m];
+            if (!inv) fwd_group<3, true>(c, f + 1, fz + 1, 0, x);
+            else inv_group<3, false>(c, f + 1, gg >> 6, x);
+#pragma unroll
+            for (int m = 0; m < 8; m++) s[pad8(base + span * m)] = x[m];
+        }
+        __syncthreads();
+        if (!inv) {
+            r2_pass<false, 3, 6, 9, 3>(c, s, 512, sch, 4, reduce_output);   // factor 64 (a): 256, 128, 64
+            __syncthreads();
+            r2_pass<false, 3, 3, 6, 0>(c, s, 512, sch, 7, reduce_output);   // factor 64 (b): 32, 16, 8
+            __syncthreads();
+            r2_pass<false, 3, 0, 3, 3>(c, s, 512, sch, 10, reduce_output);  // factor 64 (b): 4, 2, 1
+        } else {
+            r2_pass<true, 3, 9, 12, 0>(c, s, 512, sch, 4, false);  // factor 64 (a): 512, 1024, 2048
+            __syncthreads();
+            r2_pass<true, 3, 0, 3, 3>(c, s, 512, sch, 7, false);   // factor 64 (b): 1, 2, 4
+            __syncthreads();
+            r2_pass<true, 3, 3, 6, 0>(c, s, 512, sch, 10, false);  // factor 64 (b): 8, 16, 32
+        }
+        __syncthreads();
+        line_store(s, gb, 4096, MODE & 2, mulp + (me ? 4096 * blk : 0), me, mn, mi);
+        __syncthreads();  // the tile is refilled by the next block
+    }
+}
+
 // ---------------------------------------------------------------- columns
 
 /// [4, 3] column (12 residues at element stride ge): factor 4 (distance 3) then factor 3

@@ -40,6 +40,7 @@ hc_status launch_crt_pass(hc_context ctx, int dir, const KView& t, const KView* 
 hc_status launch_giant(hc_context ctx, const KView& babies, const KView& lcoef, int nbaby, int d, const int* lfirst,
                        const int* lcount, const KView* add, int nadd, const unsigned char* full, int used,
                        const KView& dst, const KMods& m, const int64_t* one_dev);
+size_t crt_slab_tile_words(int32_t shapes, int32_t dl, int32_t dk, int logv);
 }  // namespace hc
 
 using namespace hc;
@@ -1881,7 +1882,8 @@ extern "C" hc_status hc_bfv_key_switch_noalloc(hc_ring R, hc_view c0, hc_view c1
 
 namespace hc {
 hc_status launch_crt_batch(hc_context ctx, const CrtSlab* slabs, int nslabs, int* counter, size_t tile_words,
-                           size_t tw_words, const CrtLaunch& L);
+                           size_t tw_words, const CrtLaunch& L, bool generic);
+bool crt_slab_specialised(int32_t shapes);
 const void* plan_device(hc_ntt_plan p);
 int32_t plan_ntw(hc_ntt_plan p);
 int32_t plan_shape(hc_ntt_plan p);
@@ -1920,10 +1922,13 @@ std::string crt_signature(const std::vector<CrtSlab>& v) {
 
 /// Shared-memory tile of a slab: a padded line for the specialised line kernels, else the
 /// larger of a line and a column block; rounded to an even word count (16-byte aligned twiddles).
-size_t crt_tile_words(const CrtSlab& s, int logv) {
-    size_t w = std::max<size_t>((size_t)s.dk, (size_t)s.dl << logv);
-    if ((s.shapes & 0xff) != 0 && ((s.shapes >> 16) & 1)) w = std::max<size_t>(w, (size_t)s.dk + (size_t)s.dk / 8);
-    return (w + 1) & ~(size_t)1;
+size_t crt_tile_words(const CrtSlab& s, int logv) { return crt_slab_tile_words(s.shapes, s.dl, s.dk, logv); }
+
+/// Whether some slab needs the generic tile programme (crt_batch_kernel<true>).
+bool crt_generic(const std::vector<CrtSlab>& slabs) {
+    for (const CrtSlab& s : slabs)
+        if (!crt_slab_specialised(s.shapes)) return true;
+    return false;
 }
 
 }  // namespace
@@ -2003,7 +2008,7 @@ hc_status hc_crt_batch_run(hc_crt_batch b) {
         size_t tile = 0;
         for (const CrtSlab& s : b->host) tile = std::max(tile, crt_tile_words(s, b->launch.logv));
         CK(launch_crt_batch(b->ctx, b->dev.as<CrtSlab>(), (int)b->host.size(), b->counter.as<int>(), tile, b->tw_words,
-                            b->launch));
+                            b->launch, crt_generic(b->host)));
     });
 }
 
@@ -2056,6 +2061,7 @@ hc_status hc_crt_batch_tune(hc_crt_batch b, int reps, hc_crt_launch* chosen) {
             CK(cuda_check(cudaEventCreate(&e1), "tuning event"));
             CrtLaunch best = b->launch;
             float best_ms = -1;
+            const bool generic = crt_generic(b->host);
             const int threads[] = {128, 256};
             const int per_sm[] = {1, 2, 3, 4};
             const int logvs[] = {4, 5, 6};
@@ -2066,13 +2072,13 @@ hc_status hc_crt_batch_tune(hc_crt_batch b, int reps, hc_crt_launch* chosen) {
                         size_t tile = 0;
                         for (const CrtSlab& s : sample) tile = std::max(tile, crt_tile_words(s, lv));
                         hc_status rc = launch_crt_batch(ctx, sdev.as<CrtSlab>(), (int)sample.size(), cnt.as<int>(),
-                                                        tile, b->tw_words, L);
+                                                        tile, b->tw_words, L, generic);
                         if (rc == HC_ERR_UNSUPPORTED) continue;  // shape does not fit an SM
                         CK(rc);
                         cudaEventRecord(e0, st);
                         for (int r = 0; r < reps; r++)
                             CK(launch_crt_batch(ctx, sdev.as<CrtSlab>(), (int)sample.size(), cnt.as<int>(), tile,
-                                                b->tw_words, L));
+                                                b->tw_words, L, generic));
                         cudaEventRecord(e1, st);
                         CK(cuda_check(cudaEventSynchronize(e1), "tuning run"));
                         float ms = 0;
