@@ -695,13 +695,13 @@ __device__ __forceinline__ void slab_pass(const CrtSlab& S, const DevPlanHeader*
                 else run_line<HC_SHAPE_L3072, 1, true>(P, c, s, g, mulp, 1, S.n, S.ninv);
             } else {
                 // one 4096-residue block in shared memory at a time (crt_slab_tile_words)
-                if (mode & 1) {
+                if (mode & 1) {  // modes 1 (inverse) and 3 (inverse, then the operand product)
                     const FixedSched<HC_SHAPE_L12288, true> sch{P->inv};
-                    fast::line12288_seq<1>(sch, c, s, g, mulp, 1, S.n, S.ninv);
-                } else {
+                    if (mode == 3) fast::line12288_seq<3>(sch, c, s, g, mulp, 1, S.n, S.ninv);
+                    else fast::line12288_seq<1>(sch, c, s, g, mulp, 1, S.n, S.ninv);
+                } else {  // mode 2: forward, then the kernel product
                     const FixedSched<HC_SHAPE_L12288, false> sch{P->fwd};
-                    if (mode == 2) fast::line12288_seq<2>(sch, c, s, g, mulp, 1, S.n, S.ninv);
-                    else fast::line12288_seq<3>(sch, c, s, g, mulp, 1, S.n, S.ninv);
+                    fast::line12288_seq<2>(sch, c, s, g, mulp, 1, S.n, S.ninv);
                 }
             }
             __syncthreads();
