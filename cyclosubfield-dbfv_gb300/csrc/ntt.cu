@@ -756,8 +756,9 @@ __device__ __forceinline__ void slab_pass(const CrtSlab& S, const DevPlanHeader*
 /// operand product fused into the epilogue of the forward transform's last pass.
 /// GENERIC = false: every slab has the specialised line and column shapes with compiled-in
 /// schedules (both large fields' rings), so the generic tile programme is left out; MINB: the CTAs
-/// of 256 threads per SM the register allocation must allow (2: 128 registers; 3: 80, with some
-/// spilling), chosen through the autotuned CTAs per SM. GENERIC = true serves other slabs.
+/// of 256 threads per SM the register allocation must allow (2: 128 registers; 3: 80 and 4: 64,
+/// with some spilling), chosen through the autotuned CTAs per SM. GENERIC = true serves other
+/// slabs.
 template <bool GENERIC, int MINB>
 __global__ void __launch_bounds__(256, MINB)
     crt_batch_kernel(const CrtSlab* __restrict__ slabs, int nslabs, int* counter, int logv, int tile_words) {
@@ -1060,8 +1061,10 @@ bool crt_slab_specialised(int32_t shapes) {
 hc_status launch_crt_batch(hc_context ctx, const CrtSlab* slabs, int nslabs, int* counter, size_t tile_words,
                            size_t tw_words, const CrtLaunch& L, bool generic) {
     if (nslabs <= 0) return HC_OK;
-    auto kern = generic ? crt_batch_kernel<true, 2>
-                        : (L.ctas_per_sm >= 3 ? crt_batch_kernel<false, 3> : crt_batch_kernel<false, 2>);
+    auto kern = generic                ? crt_batch_kernel<true, 2>
+                : L.ctas_per_sm >= 4 ? crt_batch_kernel<false, 4>
+                : L.ctas_per_sm == 3 ? crt_batch_kernel<false, 3>
+                                     : crt_batch_kernel<false, 2>;
     if (L.threads < 32 || L.threads > 256 || L.threads % 32) return fail(HC_ERR_ARG, "batched transform: threads per CTA");
     if (L.logv < 0 || L.logv > 6) return fail(HC_ERR_ARG, "batched transform: dimension-2 tile width");
     const size_t smem = (tile_words + tw_words) * 8;
