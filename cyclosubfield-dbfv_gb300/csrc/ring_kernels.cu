@@ -447,8 +447,13 @@ struct GiantArgs {
 constexpr int GIANT_STAGES = 4;
 constexpr int GIANT_MAX_UNITS = 1024;
 
+/// The (baby step j, input digit i) units of one launch, prepared on the host: the unit's first
+/// row in the baby-step tensor (2 d j + 2 i), the output digits o it feeds (bit o of the mask: 0 <=
+/// out0 + o - i < lcount[j]) and the coefficient-digit row of output 0 (lfirst[j] + out0 - i;
+/// output o reads row fb + o).
 struct GiantUnits {
-    unsigned short u[GIANT_MAX_UNITS];  // (baby step << 6) | input digit
+    unsigned int w[GIANT_MAX_UNITS];  // row | mask << 16
+    short fb[GIANT_MAX_UNITS];
     int n;
 };
 
@@ -471,8 +476,7 @@ __global__ void __launch_bounds__(256) giant_kernel(GiantArgs a, GiantUnits un, 
         const int64_t* xb = kat<int64_t>(a.babies, 0, j, k, l);
         auto issue = [&](int u) {
             if (u < un.n) {
-                const int bj = un.u[u] >> 6, i = un.u[u] & 63;
-                const int64_t* xr = xb + ((int64_t)bj * 2 * a.d + 2 * i) * rs;
+                const int64_t* xr = xb + (int64_t)(un.w[u] & 0xffff) * rs;
                 int64_t* slot = gsm + (u % GIANT_STAGES) * 512;
                 cp_async8(slot + tid, xr);
                 cp_async8(slot + 256 + tid, xr + rs);
@@ -487,15 +491,14 @@ __global__ void __launch_bounds__(256) giant_kernel(GiantArgs a, GiantUnits un, 
         for (int u = 0; u < un.n; u++) {
             issue(u + GIANT_STAGES - 1);
             cp_async_wait<GIANT_STAGES - 1>();  // unit u's words have landed
-            const int bj = un.u[u] >> 6, i = un.u[u] & 63;
-            const int lf = a.lfirst[bj], lc = a.lcount[bj];
+            const unsigned mask = un.w[u] >> 16;
+            const int fb = un.fb[u];
             const int64_t* slot = gsm + (u % GIANT_STAGES) * 512;
             const int64_t x0 = slot[tid], x1 = slot[256 + tid];
 #pragma unroll
             for (int o = 0; o < GIANT_OUT; o++) {
-                const int jj = a.out0 + o - i;
-                if (o < a.nout && jj >= 0 && jj < lc) {
-                    const int64_t f = slc[lf + jj];
+                if ((mask >> o) & 1) {
+                    const int64_t f = slc[fb + o];
                     acc0[o] = (i128)((u128)acc0[o] + (u128)((i128)x0 * (i128)f));
                     acc1[o] = (i128)((u128)acc1[o] + (u128)((i128)x1 * (i128)f));
                 }
@@ -655,9 +658,17 @@ hc_status launch_giant(hc_context ctx, const KView& babies, const KView& lcoef, 
         un.n = 0;
         for (int bj = 0; bj < nbaby; bj++)
             for (int i = 0; i < d; i++) {
-                if (i + lcount[bj] <= a.out0 || i >= a.out0 + a.nout) continue;
-                if (un.n == GIANT_MAX_UNITS) return fail(HC_ERR_UNSUPPORTED, "too many baby-step units");
-                un.u[un.n++] = (unsigned short)((bj << 6) | i);
+                unsigned mask = 0;
+                for (int o = 0; o < a.nout; o++) {
+                    const int jj = a.out0 + o - i;
+                    if (jj >= 0 && jj < lcount[bj]) mask |= 1u << o;
+                }
+                if (!mask) continue;
+                const int row = bj * 2 * d + 2 * i, fb = lfirst[bj] + a.out0 - i;
+                if (un.n == GIANT_MAX_UNITS || row > 0xffff || fb < -32768 || fb > 32767)
+                    return fail(HC_ERR_UNSUPPORTED, "too many baby-step units");
+                un.w[un.n] = (unsigned)row | (mask << 16);
+                un.fb[un.n++] = (short)fb;
             }
         giant_kernel<<<blocks, 256, smem, stream_of(ctx)>>>(a, un, m, one_dev, lines, chunks);
         count_launch(ctx);
