@@ -677,7 +677,7 @@ __global__ void __launch_bounds__(256, HC_NTT_MIN_BLOCKS) ntt_tile_kernel(KView 
 /// column blocks of 2^logv columns (dimension 2). Modes as tile_run; `mulrow` is the CRT kernel
 /// row of the pass (modes 2 and 3 along dimension 2, mode 2 along dimension 3), while mode 3
 /// along dimension 3 multiplies by the slab's operand.
-template <bool GENERIC>
+template <bool GENERIC, int CLS>
 __device__ __forceinline__ void slab_pass(const CrtSlab& S, const DevPlanHeader* P, const int64_t* tw, int64_t* s,
                                           int dim, int mode, const int64_t* mulrow, int logv) {
     // specialised kernels for slabs whose plans have the fixed schedule (bit 16: dimension-3
@@ -689,11 +689,11 @@ __device__ __forceinline__ void slab_pass(const CrtSlab& S, const DevPlanHeader*
         for (int k = 0; k < S.dl; k++) {
             int64_t* g = S.data + k * S.s2;
             const int64_t* mulp = mode == 3 ? S.op + k * S.op_s2 : mulrow;
-            if (shape == HC_SHAPE_L3072) {
+            if (CLS != 2 && (CLS == 1 || shape == HC_SHAPE_L3072)) {
                 if (mode == 2) run_line<HC_SHAPE_L3072, 2, true>(P, c, s, g, mulp, 1, S.n, S.ninv);
                 else if (mode == 3) run_line<HC_SHAPE_L3072, 3, true>(P, c, s, g, mulp, 1, S.n, S.ninv);
                 else run_line<HC_SHAPE_L3072, 1, true>(P, c, s, g, mulp, 1, S.n, S.ninv);
-            } else {
+            } else if (CLS != 1) {
                 // one 4096-residue block in shared memory at a time (crt_slab_tile_words)
                 if (mode & 1) {  // modes 1 (inverse) and 3 (inverse, then the operand product)
                     const FixedSched<HC_SHAPE_L12288, true> sch{P->inv};
@@ -711,12 +711,12 @@ __device__ __forceinline__ void slab_pass(const CrtSlab& S, const DevPlanHeader*
     if (fix && dim == 2 && (shape == HC_SHAPE_C12 || shape == HC_SHAPE_C4)) {
         const fast::Ctx c = make_ctx(P, tw);
         for (int l = threadIdx.x; l < S.dk; l += blockDim.x) {
-            if (shape == HC_SHAPE_C12) {
+            if (CLS != 2 && (CLS == 1 || shape == HC_SHAPE_C12)) {
                 if (mode == 2) run_column<HC_SHAPE_C12, 2, true>(P, c, S.data + l, S.s2, S.data + l, S.s2, mulrow, 1, S.n,
                                                              S.ninv);
                 else run_column<HC_SHAPE_C12, 1, true>(P, c, S.data + l, S.s2, S.data + l, S.s2, mulrow, 1, S.n,
                                                              S.ninv);
-            } else {
+            } else if (CLS != 1) {
                 if (mode == 2) run_column<HC_SHAPE_C4, 2, true>(P, c, S.data + l, S.s2, S.data + l, S.s2, mulrow, 1, S.n,
                                                              S.ninv);
                 else run_column<HC_SHAPE_C4, 1, true>(P, c, S.data + l, S.s2, S.data + l, S.s2, mulrow, 1, S.n,
@@ -756,11 +756,12 @@ __device__ __forceinline__ void slab_pass(const CrtSlab& S, const DevPlanHeader*
 /// operand product fused into the epilogue of the forward transform's last pass.
 /// GENERIC = false: every slab has the specialised line and column shapes with compiled-in
 /// schedules (both large fields' rings), so the generic tile programme is left out; MINB: the CTAs
-/// of 256 threads per SM the register allocation must allow (2: 128 registers; 3: 80 and 4: 64,
-/// with some spilling), chosen through the autotuned CTAs per SM. GENERIC = true serves other
-/// slabs.
-template <bool GENERIC, int MINB>
-__global__ void __launch_bounds__(256, MINB)
+/// of MAXT threads per SM the register allocation must allow (256 threads: 2 -> 128 registers,
+/// 3 -> 80, 4 -> 64 with some spilling), chosen through the autotuned launch shape. GENERIC = true serves other slabs. CLS: the slabs' shape class - 1 every slab has
+/// field_36864's [4, 3] x [2, 3, 8, 64] shapes, 2 field_49152's [4] x [3, 64, 64], 0 any - so that
+/// a launch carries only its class's code.
+template <bool GENERIC, int CLS, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
     crt_batch_kernel(const CrtSlab* __restrict__ slabs, int nslabs, int* counter, int logv, int tile_words) {
     extern __shared__ int64_t smem[];
     __shared__ int s_next;
@@ -779,10 +780,10 @@ __global__ void __launch_bounds__(256, MINB)
         stage_twiddles(P3, tw3);
         __syncthreads();
         if (S.ops & HC_CRT_FORWARD) {
-            slab_pass<GENERIC>(S, P2, tw2, smem, 2, 2, S.kl, logv);
-            slab_pass<GENERIC>(S, P3, tw3, smem, 3, 2, S.kk, logv);
-            slab_pass<GENERIC>(S, P2, tw2, smem, 2, 1, nullptr, logv);
-            slab_pass<GENERIC>(S, P3, tw3, smem, 3, (S.ops & HC_CRT_MUL) ? 3 : 1, nullptr, logv);
+            slab_pass<GENERIC, CLS>(S, P2, tw2, smem, 2, 2, S.kl, logv);
+            slab_pass<GENERIC, CLS>(S, P3, tw3, smem, 3, 2, S.kk, logv);
+            slab_pass<GENERIC, CLS>(S, P2, tw2, smem, 2, 1, nullptr, logv);
+            slab_pass<GENERIC, CLS>(S, P3, tw3, smem, 3, (S.ops & HC_CRT_MUL) ? 3 : 1, nullptr, logv);
         } else if (S.ops & HC_CRT_MUL) {
             const int total = S.dl * S.dk;
             for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
@@ -793,10 +794,10 @@ __global__ void __launch_bounds__(256, MINB)
             __syncthreads();
         }
         if (S.ops & HC_CRT_INVERSE) {
-            slab_pass<GENERIC>(S, P2, tw2, smem, 2, 2, S.ikl, logv);
-            slab_pass<GENERIC>(S, P3, tw3, smem, 3, 2, S.ikk, logv);
-            slab_pass<GENERIC>(S, P2, tw2, smem, 2, 1, nullptr, logv);
-            slab_pass<GENERIC>(S, P3, tw3, smem, 3, 1, nullptr, logv);
+            slab_pass<GENERIC, CLS>(S, P2, tw2, smem, 2, 2, S.ikl, logv);
+            slab_pass<GENERIC, CLS>(S, P3, tw3, smem, 3, 2, S.ikk, logv);
+            slab_pass<GENERIC, CLS>(S, P2, tw2, smem, 2, 1, nullptr, logv);
+            slab_pass<GENERIC, CLS>(S, P3, tw3, smem, 3, 1, nullptr, logv);
         }
     }
 }
@@ -1058,13 +1059,23 @@ bool crt_slab_specialised(int32_t shapes) {
            (s2 == HC_SHAPE_C12 || s2 == HC_SHAPE_C4);
 }
 
+/// The specialised kernel of class CLS for a launch shape.
+template <int CLS>
+auto crt_batch_variant(const CrtLaunch& L) {
+    return L.ctas_per_sm >= 4   ? crt_batch_kernel<false, CLS, 256, 4>
+           : L.ctas_per_sm == 3 ? crt_batch_kernel<false, CLS, 256, 3>
+                                : crt_batch_kernel<false, CLS, 256, 2>;
+}
+
+/// Shape class of specialised slab shapes (crt_batch_kernel's CLS): 1 field_36864, 2 field_49152.
+int crt_slab_kernel_class(int32_t shapes) { return (shapes & 0xff) == HC_SHAPE_L3072 ? 1 : 2; }
+
 hc_status launch_crt_batch(hc_context ctx, const CrtSlab* slabs, int nslabs, int* counter, size_t tile_words,
-                           size_t tw_words, const CrtLaunch& L, bool generic) {
+                           size_t tw_words, const CrtLaunch& L, bool generic, int cls) {
     if (nslabs <= 0) return HC_OK;
-    auto kern = generic                ? crt_batch_kernel<true, 2>
-                : L.ctas_per_sm >= 4 ? crt_batch_kernel<false, 4>
-                : L.ctas_per_sm == 3 ? crt_batch_kernel<false, 3>
-                                     : crt_batch_kernel<false, 2>;
+    auto kern = generic    ? crt_batch_kernel<true, 0, 256, 2>
+                : cls == 1 ? crt_batch_variant<1>(L)
+                           : crt_batch_variant<2>(L);
     if (L.threads < 32 || L.threads > 256 || L.threads % 32) return fail(HC_ERR_ARG, "batched transform: threads per CTA");
     if (L.logv < 0 || L.logv > 6) return fail(HC_ERR_ARG, "batched transform: dimension-2 tile width");
     const size_t smem = (tile_words + tw_words) * 8;

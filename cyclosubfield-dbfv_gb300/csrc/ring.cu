@@ -1882,21 +1882,28 @@ extern "C" hc_status hc_bfv_key_switch_noalloc(hc_ring R, hc_view c0, hc_view c1
 
 namespace hc {
 hc_status launch_crt_batch(hc_context ctx, const CrtSlab* slabs, int nslabs, int* counter, size_t tile_words,
-                           size_t tw_words, const CrtLaunch& L, bool generic);
+                           size_t tw_words, const CrtLaunch& L, bool generic, int cls);
+int crt_slab_kernel_class(int32_t shapes);
 bool crt_slab_specialised(int32_t shapes);
 const void* plan_device(hc_ntt_plan p);
 int32_t plan_ntw(hc_ntt_plan p);
 int32_t plan_shape(hc_ntt_plan p);
 }  // namespace hc
 
-struct hc_crt_batch_s {
-    hc_context ctx = nullptr;
+/// The slabs of one shape class (crt_slab_class): one persistent launch with its own tuned shape.
+struct CrtGroup {
     std::vector<CrtSlab> host;  // sorted: largest slabs first
     DBuf dev;                   // the descriptors on the device
     DBuf counter;               // next slab of the running launch
-    size_t tile_words = 0, tw_words = 0;
+    size_t tw_words = 0;
     CrtLaunch launch{256, 3, 6};
-    std::string signature;      // composition of the batch, key of the autotuner's memory
+    std::string signature;      // composition of the group, key of the autotuner's memory
+    int64_t residues = 0;
+};
+
+struct hc_crt_batch_s {
+    hc_context ctx = nullptr;
+    std::vector<CrtGroup> groups;  // by shape class; groups[0] holds the most residues
 };
 
 namespace {
@@ -1904,8 +1911,8 @@ namespace {
 std::mutex crt_tune_mu;
 std::map<std::string, CrtLaunch> crt_tuned;  // signature -> launch shape chosen by the autotuner
 
-/// The batch's slabs grouped by (deg_L', deg_K, ops), with their counts: batches with the same
-/// composition share a tuned launch shape.
+/// The group's slabs grouped by (deg_L', deg_K, ops), with their counts: groups of the same shape
+/// class and composition share a tuned launch shape.
 std::string crt_signature(const std::vector<CrtSlab>& v) {
     std::map<std::tuple<int, int, int>, size_t> m;
     for (const CrtSlab& s : v) m[std::make_tuple(s.dl, s.dk, s.ops)]++;
@@ -1920,6 +1927,11 @@ std::string crt_signature(const std::vector<CrtSlab>& v) {
     return out;
 }
 
+/// Shape class of a slab: its specialised (line, column) shapes when it has them, else 0 (the
+/// generic tile programme). Slabs of one class run the same code, so a launch per class keeps
+/// each kernel's working code small and lets each class have its own launch shape.
+int crt_slab_class(const CrtSlab& s) { return crt_slab_specialised(s.shapes) ? (s.shapes & 0xffff) : 0; }
+
 /// Shared-memory tile of a slab: a padded line for the specialised line kernels, else the
 /// larger of a line and a column block; rounded to an even word count (16-byte aligned twiddles).
 size_t crt_tile_words(const CrtSlab& s, int logv) { return crt_slab_tile_words(s.shapes, s.dl, s.dk, logv); }
@@ -1929,6 +1941,84 @@ bool crt_generic(const std::vector<CrtSlab>& slabs) {
     for (const CrtSlab& s : slabs)
         if (!crt_slab_specialised(s.shapes)) return true;
     return false;
+}
+
+hc_status crt_group_run(hc_context ctx, CrtGroup& g) {
+    size_t tile = 0;
+    for (const CrtSlab& s : g.host) tile = std::max(tile, crt_tile_words(s, g.launch.logv));
+    const bool generic = crt_generic(g.host);
+    return launch_crt_batch(ctx, g.dev.as<CrtSlab>(), (int)g.host.size(), g.counter.as<int>(), tile, g.tw_words,
+                            g.launch, generic, generic ? 0 : crt_slab_kernel_class(g.host[0].shapes));
+}
+
+/// Times every launch shape of the candidate set on a scratch copy of a sample of the group's
+/// slabs and keeps the fastest.
+hc_status crt_group_tune(hc_context ctx, CrtGroup& g, int reps) {
+    cudaStream_t st = stream_of(ctx);
+    // a sample of at most 4096 slabs, every k-th, each given its own rows in a scratch buffer
+    // (the operands stay the batch's own, they are only read); a sample of a few slabs per
+    // persistent CTA, so that the last round's imbalance weighs as it will in the batch
+    const size_t k = (g.host.size() + 4095) / 4096;
+    std::vector<CrtSlab> sample;
+    size_t words = 0;
+    for (size_t i = 0; i < g.host.size(); i += k) {
+        sample.push_back(g.host[i]);
+        words += (size_t)g.host[i].dl * g.host[i].dk;
+    }
+    DBuf scratch(ctx, words * 8);
+    CK(cuda_check(cudaMemsetAsync(scratch.p, 0, words * 8, st), "tuning scratch"));
+    size_t off = 0;
+    for (CrtSlab& s : sample) {
+        s.data = scratch.as<int64_t>() + off;
+        s.s2 = s.dk;
+        off += (size_t)s.dl * s.dk;
+    }
+    DBuf sdev(ctx, sample.data(), sample.size() * sizeof(CrtSlab));
+    DBuf cnt(ctx, sizeof(int));
+    cudaEvent_t e0, e1;
+    CK(cuda_check(cudaEventCreate(&e0), "tuning event"));
+    CK(cuda_check(cudaEventCreate(&e1), "tuning event"));
+    CrtLaunch best = g.launch;
+    float best_ms = -1;
+    const bool generic = crt_generic(g.host);
+    const int cls = generic ? 0 : crt_slab_kernel_class(g.host[0].shapes);
+    // 128 or 256 threads at 1..4 CTAs per SM
+    const CrtLaunch shapes[] = {{128, 1, 0}, {128, 2, 0}, {128, 3, 0}, {128, 4, 0},
+                                {256, 1, 0}, {256, 2, 0}, {256, 3, 0}, {256, 4, 0}};
+    const int logvs[] = {4, 5, 6};
+    hc_status rc = HC_OK;
+    for (const CrtLaunch& sh : shapes)
+        for (int lv : logvs) {
+            CrtLaunch L{sh.threads, sh.ctas_per_sm, lv};
+            size_t tile = 0;
+            for (const CrtSlab& s : sample) tile = std::max(tile, crt_tile_words(s, lv));
+            rc = launch_crt_batch(ctx, sdev.as<CrtSlab>(), (int)sample.size(), cnt.as<int>(), tile, g.tw_words, L,
+                                  generic, cls);
+            if (rc == HC_ERR_UNSUPPORTED) {  // shape does not fit an SM
+                rc = HC_OK;
+                continue;
+            }
+            if (rc) break;
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < reps && !rc; r++)
+                rc = launch_crt_batch(ctx, sdev.as<CrtSlab>(), (int)sample.size(), cnt.as<int>(), tile, g.tw_words,
+                                      L, generic, cls);
+            if (rc) break;
+            cudaEventRecord(e1, st);
+            rc = cuda_check(cudaEventSynchronize(e1), "tuning run");
+            if (rc) break;
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (best_ms < 0 || ms < best_ms) best_ms = ms, best = L;
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CK(rc);
+    CK(cuda_check(cudaStreamSynchronize(st), "tuning"));
+    g.launch = best;
+    std::lock_guard<std::mutex> lock(crt_tune_mu);
+    crt_tuned[g.signature] = best;
+    return HC_OK;
 }
 
 }  // namespace
@@ -1942,6 +2032,8 @@ hc_status hc_crt_batch_create(hc_context ctx, const hc_crt_item* items, size_t n
                 "batched transform: ops must combine HC_CRT_FORWARD, HC_CRT_MUL, HC_CRT_INVERSE");
         auto b = std::make_unique<hc_crt_batch_s>();
         b->ctx = ctx;
+        std::vector<CrtSlab> slabs;
+        std::vector<size_t> tws;  // staged twiddle words of each slab's two plans
         for (size_t it = 0; it < n; it++) {
             const hc_crt_item& I = items[it];
             hc_ring R = I.ring;
@@ -1982,22 +2074,41 @@ hc_status hc_crt_batch_create(hc_context ctx, const hc_crt_item* items, size_t n
                         const int32_t s3 = plan_shape(tc.pk[j]), s2 = plan_shape(tc.plp[j]);
                         s.shapes = (s3 & 0xff) | ((s2 & 0xff) << 8) | (((s3 >> 8) & 1) << 16) | (((s2 >> 8) & 1) << 17);
                     }
-                    b->host.push_back(s);
-                    b->tw_words = std::max<size_t>(b->tw_words, 2 * (size_t)(plan_ntw(tc.plp[j]) + plan_ntw(tc.pk[j])));
+                    slabs.push_back(s);
+                    tws.push_back(2 * (size_t)(plan_ntw(tc.plp[j]) + plan_ntw(tc.pk[j])));
                 }
         }
-        REQUIRE(b->host.size() < (size_t)INT32_MAX, HC_ERR_UNSUPPORTED, "batched transform: too many slabs");
-        // largest slabs first: the persistent CTAs finish on the small ones
-        std::stable_sort(b->host.begin(), b->host.end(),
-                         [](const CrtSlab& x, const CrtSlab& y) { return (int64_t)x.dl * x.dk > (int64_t)y.dl * y.dk; });
-        b->signature = crt_signature(b->host);
-        {
-            std::lock_guard<std::mutex> lock(crt_tune_mu);
-            auto it = crt_tuned.find(b->signature);
-            if (it != crt_tuned.end()) b->launch = it->second;
+        REQUIRE(slabs.size() < (size_t)INT32_MAX, HC_ERR_UNSUPPORTED, "batched transform: too many slabs");
+        std::map<int, size_t> index;  // shape class -> group
+        for (size_t i = 0; i < slabs.size(); i++) {
+            const int cls = crt_slab_class(slabs[i]);
+            auto it = index.find(cls);
+            if (it == index.end()) {
+                it = index.emplace(cls, b->groups.size()).first;
+                b->groups.emplace_back();
+            }
+            CrtGroup& g = b->groups[it->second];
+            g.host.push_back(slabs[i]);
+            g.tw_words = std::max(g.tw_words, tws[i]);
+            g.residues += (int64_t)slabs[i].dl * slabs[i].dk;
         }
-        if (!b->host.empty()) b->dev = DBuf(ctx, b->host.data(), b->host.size() * sizeof(CrtSlab));
-        b->counter = DBuf(ctx, sizeof(int));
+        // the group with the most residues first: its launch shape is the batch's reported one
+        std::stable_sort(b->groups.begin(), b->groups.end(),
+                         [](const CrtGroup& x, const CrtGroup& y) { return x.residues > y.residues; });
+        for (CrtGroup& g : b->groups) {
+            // largest slabs first: the persistent CTAs finish on the small ones
+            std::stable_sort(g.host.begin(), g.host.end(), [](const CrtSlab& x, const CrtSlab& y) {
+                return (int64_t)x.dl * x.dk > (int64_t)y.dl * y.dk;
+            });
+            g.signature = "c" + std::to_string(crt_slab_class(g.host[0])) + ":" + crt_signature(g.host);
+            {
+                std::lock_guard<std::mutex> lock(crt_tune_mu);
+                auto it = crt_tuned.find(g.signature);
+                if (it != crt_tuned.end()) g.launch = it->second;
+            }
+            g.dev = DBuf(ctx, g.host.data(), g.host.size() * sizeof(CrtSlab));
+            g.counter = DBuf(ctx, sizeof(int));
+        }
         *out = b.release();
     });
 }
@@ -2005,10 +2116,7 @@ hc_status hc_crt_batch_create(hc_context ctx, const hc_crt_item* items, size_t n
 hc_status hc_crt_batch_run(hc_crt_batch b) {
     return guard([&] {
         REQUIRE(b, HC_ERR_ARG, "null batch");
-        size_t tile = 0;
-        for (const CrtSlab& s : b->host) tile = std::max(tile, crt_tile_words(s, b->launch.logv));
-        CK(launch_crt_batch(b->ctx, b->dev.as<CrtSlab>(), (int)b->host.size(), b->counter.as<int>(), tile, b->tw_words,
-                            b->launch, crt_generic(b->host)));
+        for (CrtGroup& g : b->groups) CK(crt_group_run(b->ctx, g));
     });
 }
 
@@ -2017,83 +2125,31 @@ hc_status hc_crt_batch_set_launch(hc_crt_batch b, const hc_crt_launch* l) {
         REQUIRE(b && l, HC_ERR_ARG, "null argument");
         REQUIRE(l->threads >= 32 && l->threads <= 256 && l->threads % 32 == 0, HC_ERR_ARG, "threads per CTA");
         REQUIRE(l->ctas_per_sm >= 1 && l->logv >= 0 && l->logv <= 6, HC_ERR_ARG, "launch shape");
-        b->launch = CrtLaunch{l->threads, l->ctas_per_sm, l->logv};
+        for (CrtGroup& g : b->groups) g.launch = CrtLaunch{l->threads, l->ctas_per_sm, l->logv};
     });
 }
 
 hc_status hc_crt_batch_get_launch(hc_crt_batch b, hc_crt_launch* out) {
     return guard([&] {
         REQUIRE(b && out, HC_ERR_ARG, "null argument");
-        out->threads = b->launch.threads, out->ctas_per_sm = b->launch.ctas_per_sm, out->logv = b->launch.logv;
+        const CrtLaunch L = b->groups.empty() ? CrtLaunch{256, 3, 6} : b->groups[0].launch;
+        out->threads = L.threads, out->ctas_per_sm = L.ctas_per_sm, out->logv = L.logv;
     });
 }
 
-size_t hc_crt_batch_num_slabs(hc_crt_batch b) { return b ? b->host.size() : 0; }
+size_t hc_crt_batch_num_slabs(hc_crt_batch b) {
+    size_t n = 0;
+    if (b)
+        for (const CrtGroup& g : b->groups) n += g.host.size();
+    return n;
+}
 
 hc_status hc_crt_batch_tune(hc_crt_batch b, int reps, hc_crt_launch* chosen) {
     return guard([&] {
         REQUIRE(b, HC_ERR_ARG, "null batch");
         if (reps < 1) reps = 1;
-        if (!b->host.empty()) {
-            hc_context ctx = b->ctx;
-            cudaStream_t st = stream_of(ctx);
-            // a sample of at most 1024 slabs, every k-th, each given its own rows in a scratch
-            // buffer (the operands stay the batch's own, they are only read)
-            const size_t k = (b->host.size() + 1023) / 1024;
-            std::vector<CrtSlab> sample;
-            size_t words = 0;
-            for (size_t i = 0; i < b->host.size(); i += k) {
-                sample.push_back(b->host[i]);
-                words += (size_t)b->host[i].dl * b->host[i].dk;
-            }
-            DBuf scratch(ctx, words * 8);
-            CK(cuda_check(cudaMemsetAsync(scratch.p, 0, words * 8, st), "tuning scratch"));
-            size_t off = 0;
-            for (CrtSlab& s : sample) {
-                s.data = scratch.as<int64_t>() + off;
-                s.s2 = s.dk;
-                off += (size_t)s.dl * s.dk;
-            }
-            DBuf sdev(ctx, sample.data(), sample.size() * sizeof(CrtSlab));
-            DBuf cnt(ctx, sizeof(int));
-            cudaEvent_t e0, e1;
-            CK(cuda_check(cudaEventCreate(&e0), "tuning event"));
-            CK(cuda_check(cudaEventCreate(&e1), "tuning event"));
-            CrtLaunch best = b->launch;
-            float best_ms = -1;
-            const bool generic = crt_generic(b->host);
-            const int threads[] = {128, 256};
-            const int per_sm[] = {1, 2, 3, 4};
-            const int logvs[] = {4, 5, 6};
-            for (int th : threads)
-                for (int ps : per_sm)
-                    for (int lv : logvs) {
-                        CrtLaunch L{th, ps, lv};
-                        size_t tile = 0;
-                        for (const CrtSlab& s : sample) tile = std::max(tile, crt_tile_words(s, lv));
-                        hc_status rc = launch_crt_batch(ctx, sdev.as<CrtSlab>(), (int)sample.size(), cnt.as<int>(),
-                                                        tile, b->tw_words, L, generic);
-                        if (rc == HC_ERR_UNSUPPORTED) continue;  // shape does not fit an SM
-                        CK(rc);
-                        cudaEventRecord(e0, st);
-                        for (int r = 0; r < reps; r++)
-                            CK(launch_crt_batch(ctx, sdev.as<CrtSlab>(), (int)sample.size(), cnt.as<int>(), tile,
-                                                b->tw_words, L, generic));
-                        cudaEventRecord(e1, st);
-                        CK(cuda_check(cudaEventSynchronize(e1), "tuning run"));
-                        float ms = 0;
-                        cudaEventElapsedTime(&ms, e0, e1);
-                        if (best_ms < 0 || ms < best_ms) best_ms = ms, best = L;
-                    }
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            CK(cuda_check(cudaStreamSynchronize(st), "tuning"));
-            b->launch = best;
-            std::lock_guard<std::mutex> lock(crt_tune_mu);
-            crt_tuned[b->signature] = best;
-        }
-        if (chosen) chosen->threads = b->launch.threads, chosen->ctas_per_sm = b->launch.ctas_per_sm,
-                    chosen->logv = b->launch.logv;
+        for (CrtGroup& g : b->groups) CK(crt_group_tune(b->ctx, g, reps));
+        if (chosen) CK(hc_crt_batch_get_launch(b, chosen));
     });
 }
 

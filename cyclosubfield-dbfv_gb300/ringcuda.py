@@ -276,9 +276,9 @@ class CrtLaunch(ctypes.Structure):
 
 
 class CrtBatch:
-    """hc_crt_batch: batched CRT transforms of (ring, data, op, base) items in one persistent
-    launch; `ops` combines CRT_FORWARD, CRT_MUL and CRT_INVERSE. The tensors and rings must outlive
-    the batch."""
+    """hc_crt_batch: batched CRT transforms of (ring, data, op, base) items, one persistent launch
+    per shape class of their slabs; `ops` combines CRT_FORWARD, CRT_MUL and CRT_INVERSE. The
+    tensors and rings must outlive the batch."""
 
     def __init__(self, items, ops, backend=None):
         if not items:

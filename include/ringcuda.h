@@ -121,7 +121,9 @@ hc_status hc_bfv_hom_gal_batch(hc_ring ring, hc_view ct, const size_t* base, siz
  * Montgomery product with the item's operand (hal_mul_mont64, src/hal/cpu.rs:823-836) and
  * crt_to_pb (:1140-1161), in place and bit-identical to those calls made one by one. The batch
  * keeps device pointers to the items' tensors and to the rings' tables: both must outlive it.
- * Running it issues a counter reset and one kernel on the context's stream (graph-capturable). */
+ * Running it issues, per shape class of its slabs (each field's specialised line and column
+ * shapes; one class for the rest), a counter reset and one persistent kernel on the context's
+ * stream (graph-capturable). */
 #define HC_CRT_FORWARD 1 /* period basis -> CRT basis (input bound 2) */
 #define HC_CRT_MUL 2     /* Montgomery product with `op` (CRT basis) */
 #define HC_CRT_INVERSE 4 /* CRT basis -> period basis */
@@ -134,7 +136,8 @@ typedef struct {
     size_t r;
 } hc_crt_item;
 /* Launch shape of the persistent kernel: threads per CTA (32..256), CTAs per SM, and 2^logv
- * columns per dimension-2 tile (logv 0..6). */
+ * columns per dimension-2 tile (logv 0..6). Each shape class has its own; set_launch sets all
+ * of them, get_launch and tune report that of the class with the most residues. */
 typedef struct {
     int threads;
     int ctas_per_sm;
@@ -142,9 +145,10 @@ typedef struct {
 } hc_crt_launch;
 hc_status hc_crt_batch_create(hc_context ctx, const hc_crt_item* items, size_t n, int ops, hc_crt_batch* out);
 hc_status hc_crt_batch_run(hc_crt_batch b);
-/* Autotuner: times every launch shape of a fixed candidate set on a scratch copy of (a sample of)
- * the batch's slabs - the transforms are data-oblivious - and keeps the fastest; the choice is
- * remembered for batches of the same composition. Synchronises; not during stream capture. */
+/* Autotuner: per shape class, times every launch shape of a fixed candidate set on a scratch copy
+ * of (a sample of) the class's slabs - the transforms are data-oblivious - and keeps the fastest;
+ * the choice is remembered for classes of the same composition. Synchronises; not during stream
+ * capture. */
 hc_status hc_crt_batch_tune(hc_crt_batch b, int reps, hc_crt_launch* chosen);
 hc_status hc_crt_batch_set_launch(hc_crt_batch b, const hc_crt_launch* l);
 hc_status hc_crt_batch_get_launch(hc_crt_batch b, hc_crt_launch* out);
