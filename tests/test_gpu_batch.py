@@ -70,7 +70,7 @@ def build(po, rings, seed, ops, items=ITEMS):
     return ringcuda.CrtBatch(batch_items, ops), checks
 
 
-@pytest.mark.parametrize("ops", [7, 1, 4, 2, 5, 3])
+@pytest.mark.parametrize("ops", [7, 1, 4, 2, 5, 3, 6])
 def test_crt_batch_matches_oracle(po, be, rings, ops):
     batch, checks = build(po, rings, 100 + ops, ops)
     batch.run()
@@ -101,3 +101,22 @@ def test_crt_batch_tuned_and_graph_replay(po, be, rings):
     be.synchronize()
     for i, (dx, exp) in enumerate(checks):
         assert (dx.to_numpy() == exp).all(), "item %d" % i
+
+
+def test_crt_batch_one_launch_per_shape_class(po, be, rings):
+    """The batch runs one persistent kernel per shape class of its slabs: field_36864's and
+    field_49152's specialised shapes and the generic tile programme (field_18) are three."""
+    batch, checks = build(po, rings, 23, 7)
+    l0 = be.launch_count()
+    batch.run()
+    be.synchronize()
+    assert be.launch_count() - l0 == 3
+    for i, (dx, exp) in enumerate(checks):
+        assert (dx.to_numpy() == exp).all(), "item %d" % i
+    single, checks1 = build(po, rings, 24, 7, items=[("field_49152", 2, [0, 1, 2], 1)])
+    l0 = be.launch_count()
+    single.run()
+    be.synchronize()
+    assert be.launch_count() - l0 == 1
+    for dx, exp in checks1:
+        assert (dx.to_numpy() == exp).all()
