@@ -71,12 +71,11 @@ struct KMods {
 __device__ __forceinline__ int64_t wadd(int64_t a, int64_t b) { return (int64_t)((uint64_t)a + (uint64_t)b); }
 __device__ __forceinline__ int64_t wsub(int64_t a, int64_t b) { return (int64_t)((uint64_t)a - (uint64_t)b); }
 
-/// Barrett multiplication by the constant (z, u): q = floor((u x + 2^63) / 2^64), result
-/// z x + q n in wrapping 64-bit arithmetic (|result| <= 3n/4 for |x| <= 2^63).
+/// The Barrett quotient q = floor((u x + 2^63) / 2^64) of signed u, x.
 /// The high word of the unsigned 128-bit product U X is accumulated from 32-bit limbs with one
 /// carry chain; the signed product follows from u x = U X - 2^64 ([u < 0] X + [x < 0] U), and the
 /// rounding bit of "+ 2^63" is bit 63 of the low word (bit 31 of its upper limb).
-__device__ __forceinline__ int64_t bmul(int64_t z, int64_t u, int64_t x, int64_t n) {
+__device__ __forceinline__ uint64_t barrett_q(int64_t u, int64_t x) {
     const uint32_t u0 = (uint32_t)u, u1 = (uint32_t)((uint64_t)u >> 32);
     const uint32_t x0 = (uint32_t)x, x1 = (uint32_t)((uint64_t)x >> 32);
     uint32_t r1, r2, r3;
@@ -93,8 +92,20 @@ __device__ __forceinline__ int64_t bmul(int64_t z, int64_t u, int64_t x, int64_t
         : "=&r"(r1), "=&r"(r2), "=&r"(r3)
         : "r"(u0), "r"(u1), "r"(x0), "r"(x1));
     const uint64_t mx = (uint64_t)(x >> 63), mu = (uint64_t)(u >> 63);
-    const uint64_t q = ((((uint64_t)r3 << 32) | r2) - ((uint64_t)u & mx) - ((uint64_t)x & mu)) + (r1 >> 31);
-    return (int64_t)((uint64_t)z * (uint64_t)x + q * (uint64_t)n);
+    return ((((uint64_t)r3 << 32) | r2) - ((uint64_t)u & mx) - ((uint64_t)x & mu)) + (r1 >> 31);
+}
+
+/// Barrett multiplication by the constant (z, u): result z x + q n in wrapping 64-bit arithmetic
+/// (|result| <= 3n/4 for |x| <= 2^63), q = barrett_q(u, x).
+__device__ __forceinline__ int64_t bmul(int64_t z, int64_t u, int64_t x, int64_t n) {
+    return (int64_t)((uint64_t)z * (uint64_t)x + barrett_q(u, x) * (uint64_t)n);
+}
+
+/// bmul by the Barrett constant of 1, the reduction step of the lazy transforms: that constant's
+/// z is 1 for every odd modulus n >= 3 (1 is its own balanced residue), so z x is x and only the
+/// quotient's product remains - the same result as bmul(1, u, x, n) with one product fewer.
+__device__ __forceinline__ int64_t bmul1(int64_t u, int64_t x, int64_t n) {
+    return (int64_t)((uint64_t)x + barrett_q(u, x) * (uint64_t)n);
 }
 
 /// Montgomery reduction of the 128-bit value hi:lo: ((x + m n) >> 64) with m = lo * (-n^-1).

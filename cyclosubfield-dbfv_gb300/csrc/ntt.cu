@@ -127,14 +127,14 @@ __device__ __forceinline__ void fwd_stage(const Tile& T, const DevStage st, cons
             bool skip = st.skip_ok && z == 1;
             int64_t a = x, yv = y;
             if (st.reduce_before) {  // the reference's reduction pass, applied as the operands are read
-                a = bmul(one_z, one_u, a, n);
-                yv = bmul(one_z, one_u, yv, n);
+                a = bmul1(one_u, a, n);
+                yv = bmul1(one_u, yv, n);
             }
             int64_t t = skip ? yv : bmul(z, u, yv, n);
             int64_t o0 = wadd(a, t), o1 = wsub(a, t);
             if (fuse) {
-                o0 = bmul(one_z, one_u, o0, n);
-                o1 = bmul(one_z, one_u, o1, n);
+                o0 = bmul1(one_u, o0, n);
+                o1 = bmul1(one_u, o1, n);
             }
             x = o0;
             y = o1;
@@ -144,9 +144,9 @@ __device__ __forceinline__ void fwd_stage(const Tile& T, const DevStage st, cons
             bool skip = st.skip_ok && w[0] == 1;
             int64_t a = x, bv = y, c = zr;
             if (st.reduce_before) {
-                a = bmul(one_z, one_u, a, n);
-                bv = bmul(one_z, one_u, bv, n);
-                c = bmul(one_z, one_u, c, n);
+                a = bmul1(one_u, a, n);
+                bv = bmul1(one_u, bv, n);
+                c = bmul1(one_u, c, n);
             }
             int64_t t_b = skip ? bv : bmul(w[0], w[1], bv, n);
             int64_t t_bz = bmul(w[2], w[3], bv, n);
@@ -156,9 +156,9 @@ __device__ __forceinline__ void fwd_stage(const Tile& T, const DevStage st, cons
             int64_t t_czz = bmul(w[10], w[11], c, n);
             int64_t o0 = wadd(wadd(a, t_b), t_c), o1 = wadd(wadd(a, t_bz), t_czz), o2 = wadd(wadd(a, t_bzz), t_cz);
             if (fuse) {
-                o0 = bmul(one_z, one_u, o0, n);
-                o1 = bmul(one_z, one_u, o1, n);
-                o2 = bmul(one_z, one_u, o2, n);
+                o0 = bmul1(one_u, o0, n);
+                o1 = bmul1(one_u, o1, n);
+                o2 = bmul1(one_u, o2, n);
             }
             x = o0;
             y = o1;
@@ -191,8 +191,8 @@ __device__ __forceinline__ void inv_stage(const Tile& T, const DevStage st, cons
             bool skip = !fused && yz == 1;
             int64_t y0 = x, y1 = y;
             if (st.reduce_before) {
-                y0 = bmul(one_z, one_u, y0, n);
-                y1 = bmul(one_z, one_u, y1, n);
+                y0 = bmul1(one_u, y0, n);
+                y1 = bmul1(one_u, y1, n);
             }
             int64_t sum = wadd(y0, y1), dif = wsub(y0, y1);
             x = fused ? bmul(yz, yu, sum, n) : sum;
@@ -211,9 +211,9 @@ __device__ __forceinline__ void inv_stage(const Tile& T, const DevStage st, cons
             const int64_t* zt = tw + 2 * st.zeta_off;
             int64_t y0 = x, y1 = y, y2 = zr;
             if (st.reduce_before) {
-                y0 = bmul(one_z, one_u, y0, n);
-                y1 = bmul(one_z, one_u, y1, n);
-                y2 = bmul(one_z, one_u, y2, n);
+                y0 = bmul1(one_u, y0, n);
+                y1 = bmul1(one_u, y1, n);
+                y2 = bmul1(one_u, y2, n);
             }
             int64_t y1z = bmul(zt[0], zt[1], y1, n), y1zz = bmul(zt[2], zt[3], y1, n);
             int64_t y2z = bmul(zt[0], zt[1], y2, n), y2zz = bmul(zt[2], zt[3], y2, n);
@@ -261,7 +261,7 @@ __device__ __forceinline__ void fwd_pass_r2(const Tile& T, const DevPass ps, con
         for (int q = 0; q < K; q++) {
             if (red[q]) {
 #pragma unroll
-                for (int m = 0; m < M; m++) x[m] = bmul(one_z, one_u, x[m], n);
+                for (int m = 0; m < M; m++) x[m] = bmul1(one_u, x[m], n);
             }
             const int half = M >> (q + 1);
 #pragma unroll
@@ -274,8 +274,8 @@ __device__ __forceinline__ void fwd_pass_r2(const Tile& T, const DevPass ps, con
                 const int64_t t = skip ? x[m2] : bmul(z, u, x[m2], n);
                 int64_t o0 = wadd(a, t), o1 = wsub(a, t);
                 if (fuse[q]) {
-                    o0 = bmul(one_z, one_u, o0, n);
-                    o1 = bmul(one_z, one_u, o1, n);
+                    o0 = bmul1(one_u, o0, n);
+                    o1 = bmul1(one_u, o1, n);
                 }
                 x[m1] = o0;
                 x[m2] = o1;
@@ -319,7 +319,7 @@ __device__ __forceinline__ void inv_pass_r2(const Tile& T, const DevPass ps, con
         for (int q = 0; q < K; q++) {
             if (red[q]) {
 #pragma unroll
-                for (int m = 0; m < M; m++) x[m] = bmul(one_z, one_u, x[m], n);
+                for (int m = 0; m < M; m++) x[m] = bmul1(one_u, x[m], n);
             }
             const int dist = 1 << q;
 #pragma unroll

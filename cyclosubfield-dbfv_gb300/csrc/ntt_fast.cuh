@@ -67,7 +67,7 @@ __device__ __forceinline__ SF sflags(const SCH& sch, int s) {
     return f;
 }
 
-__device__ __forceinline__ int64_t red1(const Ctx& c, int64_t x) { return bmul(c.one_z, c.one_u, x, c.n); }
+__device__ __forceinline__ int64_t red1(const Ctx& c, int64_t x) { return bmul1(c.one_u, x, c.n); }
 
 // ---------------------------------------------------------------- butterflies
 
