@@ -425,7 +425,7 @@ def crt_batch_bench(be, steps, warmup, bpeak=None, peaks=None, elements=512):
             "autotuned": True, "l2": "inputs 2 x %.1f GB, larger than L2" % (w.residues * 8 / 1e9)}
 
 
-def homcrt_bench(be, reps=3):
+def homcrt_bench(be, reps=5):
     """Homomorphic CRT transform step (hom_cyclic_transform_dbfv) on field_49152, r = 23 factors
     (log2 q in 1280..1310), dBFV modulus t = 2^24 in 3 digits of 8 bits: sum_{i < 64} c_i sigma^i(ct)
     for the descriptor's order-64 generator, 13 baby steps and 5 giant steps, 13 Galois keys with
@@ -461,7 +461,6 @@ def homcrt_bench(be, reps=3):
                        "(%d baby x %d giant steps), %d Galois keys of %d gadget digits"
                        % (r, log2_t, log2_b, length, baby, giant, len(gs), len(digits)),
            "key_MB": round(key_bytes / 1e6, 1), "keys": len(gs)}
-    ev0, ev1 = halcuda.Event(), halcuda.Event()
     for label, budget in (("resident", len(gs)), ("streamed", 8)):
         ks = ringcuda.Keyset(R, digits, r, budget * key_bytes)
         for gg in gs:
@@ -469,13 +468,18 @@ def homcrt_bench(be, reps=3):
         ringcuda.dbfv_hom_cyclic_transform(R, log2_b, log2_t, g, coeffs, ct, base, ks)  # warm-up (tables)
         be.synchronize()
         s0 = ks.stats()
-        ev0.record(be)
-        for _ in range(reps):
+        # back-to-back transforms with an event between each two; the median of the per-transform
+        # times is reported, so that one step delayed by the shared host does not set the figure
+        evs = [halcuda.Event() for _ in range(reps + 1)]
+        evs[0].record(be)
+        for q in range(reps):
             ringcuda.dbfv_hom_cyclic_transform(R, log2_b, log2_t, g, coeffs, ct, base, ks)
-        ev1.record(be)
-        ms = ev0.elapsed_ms(ev1) / reps
+            evs[q + 1].record(be)
+        times = [evs[q].elapsed_ms(evs[q + 1]) for q in range(reps)]
         s1 = ks.stats()
-        out[label] = {"ms_per_transform": round(ms, 3), "resident_keys": s1["resident"], "streamed_keys": s1["streamed"],
+        out[label] = {"ms_per_transform": round(statistics.median(times), 3),
+                      "ms_min_max": [round(min(times), 3), round(max(times), 3)], "transforms": reps,
+                      "resident_keys": s1["resident"], "streamed_keys": s1["streamed"],
                       "streamed_GB_per_transform": round((s1["streamed_bytes"] - s0["streamed_bytes"]) / reps / 1e9, 3)}
         ks.close()
     out["key_switches_per_transform"] = 3 * (baby - 1) + 3 * (giant - 1)
