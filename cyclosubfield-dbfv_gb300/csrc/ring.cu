@@ -566,9 +566,38 @@ struct hc_ring_s {
     std::map<std::pair<Base, i128>, std::unique_ptr<Tensor>> scalar_cache;
     std::map<std::pair<Base, Base>, std::unique_ptr<Tensor>> qinv_cache;
     std::map<std::pair<Base, Base>, std::unique_ptr<DBuf>> qinv_pair_cache;
+    // pinned staging of per-call host uploads (upload_async) and the event of its last copy
+    void* stage = nullptr;
+    size_t stage_bytes = 0;
+    cudaEvent_t stage_ev = nullptr;
+
+    /// Copies n host words into the contiguous device buffer dst on the ring's stream without
+    /// waiting for the stream: the words go through the pinned staging buffer, whose previous
+    /// copy (recorded by stage_ev, enqueued by an earlier call) must have been consumed first.
+    /// A host-blocking import here would stall the host until all earlier work is done, and the
+    /// GPU would then idle while the call's remaining launches are issued.
+    void upload_async(void* dst, const int64_t* src, size_t n) {
+        const size_t bytes = n * 8;
+        if (bytes == 0) return;
+        cudaStream_t st = stream_of(ctx);
+        if (stage_ev) CK(cuda_check(cudaEventSynchronize(stage_ev), "staging buffer reuse"));
+        else CK(cuda_check(cudaEventCreateWithFlags(&stage_ev, cudaEventDisableTiming), "staging event"));
+        if (bytes > stage_bytes) {
+            if (stage) cudaFreeHost(stage);
+            stage = nullptr, stage_bytes = 0;
+            count_alloc();
+            CK(cuda_check(cudaMallocHost(&stage, bytes), "pinned staging allocation"));
+            stage_bytes = bytes;
+        }
+        std::memcpy(stage, src, bytes);
+        CK(cuda_check(cudaMemcpyAsync(dst, stage, bytes, cudaMemcpyHostToDevice, st), "staged upload"));
+        CK(cuda_check(cudaEventRecord(stage_ev, st), "staging event"));
+    }
 
     ~hc_ring_s() {
         cudaStreamSynchronize(stream_of(ctx));
+        if (stage_ev) cudaEventDestroy(stage_ev);
+        if (stage) cudaFreeHost(stage);
         if (side) {
             cudaStreamSynchronize(side);
             cudaStreamDestroy(side);
@@ -2454,7 +2483,7 @@ hc_status hc_dbfv_hom_cyclic_transform(hc_ring R, size_t log2_b, size_t log2_t, 
                         const int64_t p = R->prime(idx);
                         for (i128 cf : cv) vals.push_back(mont_repr((int64_t)(cf % (i128)p), p));
                     }
-            CK(hc_import(R->ctx, L.view(), vals.data(), vals.size()));
+            R->upload_async(L.view().ptr, vals.data(), vals.size());
             TransformCache& tc = R->transform_cache(b);
             CK(hc_ntt_mul_mont64_dim(R->ctx, L.view(), tc.plp.data(), r, HC_DIM2, tc.kl.view(), tc.mods.data(), r));
             CK(hc_intt_mont64_dim(R->ctx, L.view(), tc.plp.data(), r, HC_DIM2));
