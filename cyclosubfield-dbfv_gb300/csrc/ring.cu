@@ -566,6 +566,9 @@ struct hc_ring_s {
     std::map<std::pair<Base, i128>, std::unique_ptr<Tensor>> scalar_cache;
     std::map<std::pair<Base, Base>, std::unique_ptr<Tensor>> qinv_cache;
     std::map<std::pair<Base, Base>, std::unique_ptr<DBuf>> qinv_pair_cache;
+    // dBFV reduction tables (dbfv_tables) by (log2 b, log2 t, base), type-erased: their type is
+    // defined with the dBFV code below
+    std::map<std::tuple<size_t, size_t, Base>, std::shared_ptr<void>> dbfv_cache;
     // pinned staging of per-call host uploads (upload_async) and the event of its last copy
     void* stage = nullptr;
     size_t stage_bytes = 0;
@@ -1695,7 +1698,7 @@ hc_status hc_bfv_mod_switch_down(hc_ring R, hc_view x, const size_t* base, size_
         R->bconv(tmp.view(), kept, vbase(x, (int64_t)new_len, (int64_t)r), dropped);
         CK(hc_assign(R->ctx, out, vbase(x, 0, (int64_t)new_len)));
         CK(hc_sub_i64(R->ctx, out, tmp.view()));
-        Tensor inv = R->scalar_tensor_big(kept, [&](int64_t p) { return invm(R->q_mod(dropped, p), p); });
+        const Tensor& inv = R->inv_modulus_tensor(kept, dropped);  // cached: no upload per call
         std::vector<hc_modulus> m = R->mods(kept);
         CK(hc_mul_mont64(R->ctx, out, inv.view(), m.data(), m.size()));
     });
@@ -2711,6 +2714,27 @@ Tensor split_overflow(hc_ring R, const SplitData& D, const hc_view& x, u128 x_bo
     return overflow;
 }
 
+/// The reduction's tables of one (log2 b, log2 t, base): SplitOverflowData and the carries'
+/// delta factors, built once per ring (their uploads would otherwise block the host every call).
+struct DbfvTables {
+    SplitData D;
+    std::vector<Tensor> delta_mont2;
+    DbfvTables(hc_ring R, size_t log2_b, size_t log2_t, const Base& b) : D(R, log2_b, log2_t, b) {
+        auto delta = delta_pow2(R, b, log2_t);
+        for (size_t k = 0; k < D.limbs(); k++)
+            delta_mont2.push_back(
+                scalar_tensor_big_mont2(R, b, [&](int64_t p) { return mulm(delta(p), pow2_mod(64 * k, p), p); }));
+    }
+};
+
+const DbfvTables& dbfv_tables(hc_ring R, size_t log2_b, size_t log2_t, const Base& b) {
+    const auto key = std::make_tuple(log2_b, log2_t, b);
+    auto it = R->dbfv_cache.find(key);
+    if (it == R->dbfv_cache.end())
+        it = R->dbfv_cache.emplace(key, std::make_shared<DbfvTables>(R, log2_b, log2_t, b)).first;
+    return *static_cast<const DbfvTables*>(it->second.get());
+}
+
 /// src/dbfv.rs:968-1032, period basis in and out; returns the [2 digits, r] result
 Tensor dbfv_reduce(hc_ring R, size_t log2_b, size_t log2_t, const hc_view& ct, u128 bound, const Base& b,
                    size_t* rows_out) {
@@ -2723,11 +2747,9 @@ Tensor dbfv_reduce(hc_ring R, size_t log2_b, size_t log2_t, const hc_view& ct, u
         *rows_out = 2 * d;
         return out;
     }
-    SplitData D(R, log2_b, log2_t, b);
-    auto delta = delta_pow2(R, b, log2_t);
-    std::vector<Tensor> delta_mont2;
-    for (size_t k = 0; k < D.limbs(); k++)
-        delta_mont2.push_back(scalar_tensor_big_mont2(R, b, [&](int64_t p) { return mulm(delta(p), pow2_mod(64 * k, p), p); }));
+    const DbfvTables& T = dbfv_tables(R, log2_b, log2_t, b);
+    const SplitData& D = T.D;
+    const std::vector<Tensor>& delta_mont2 = T.delta_mont2;
     Tensor result(R->ctx, 2 * (int64_t)digits, rr, R->dl(), R->dk());
     CK(hc_assign(R->ctx, vrows(result.view(), 0, 2 * (int64_t)d), ct));
     Tensor carry;
