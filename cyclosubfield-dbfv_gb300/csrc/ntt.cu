@@ -811,6 +811,7 @@ namespace hc {
 /// LazyFactorNTT::new :216-281) and simulates the bound tracking of `apply` (:581-657) and of
 /// the factor transforms (:301-537).
 hc_status build_plan(hc_context ctx, const hc_modulus* m, const size_t* shape, size_t k, hc_ntt_plan* out) {
+    (void)ctx;  // plans live in device memory of the current device, shared by its contexts
     const int64_t n = m->n;
     if (n <= 1 || n % 2 == 0 || n >= ((int64_t)1 << 62)) return fail(HC_ERR_ARG, "NTT modulus must be odd and < 2^62");
     HostPlan hp;

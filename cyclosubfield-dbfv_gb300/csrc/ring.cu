@@ -1536,6 +1536,7 @@ hc_status hc_ring_apply_galois(hc_ring ring, hc_view dst, hc_view src, const siz
     return guard([&] {
         REQUIRE(ring, HC_ERR_ARG, "null ring");
         REQUIRE((int64_t)r == src.shape[1], HC_ERR_SHAPE, "base length does not match the tensor");
+        (void)base;  // the automorphism permutes positions; which factors the rows hold does not matter
         ring->apply_galois(dst, src, g);
     });
 }
