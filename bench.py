@@ -307,7 +307,9 @@ class CrtWorkload:
     {field_36864, field_49152} and the RNS length uniformly from 4..24 (seeded); each element goes
     period basis -> CRT basis, Montgomery product with a seeded operand, CRT basis -> period
     basis. Residues are uniform in [-2^56, 2^56), below every 57-bit factor. Elements of the same
-    field and length share one tensor; the batch runs them all in one persistent launch."""
+    field and length share one tensor; the batch runs them in one persistent launch per field (each
+    field's slabs with their own kernel build and tuned shape), and a second batch over the same
+    items runs all of them in one persistent launch with one shape."""
 
     FIELDS = (("field_36864", 900, 930, 8), ("field_49152", 1280, 1310, 2))
 
@@ -335,14 +337,19 @@ class CrtWorkload:
             op = be.tensor(np.tile(block[::-1], reps)[:size].reshape(shape))
             self.items.append((R, x, op, list(range(r))))
             self.residues += size
-        self.batch = ringcuda.CrtBatch(self.items, ringcuda.CRT_FORWARD | ringcuda.CRT_MUL | ringcuda.CRT_INVERSE,
-                                       backend=be)
+        ops = ringcuda.CRT_FORWARD | ringcuda.CRT_MUL | ringcuda.CRT_INVERSE
+        self.batch = ringcuda.CrtBatch(self.items, ops, backend=be)
         self.launch = self.batch.tune(reps=2)
         self.batch.run()
+        # the same items as one persistent launch over both fields, one launch shape
+        self.batch1 = ringcuda.CrtBatch(self.items, ops | ringcuda.CRT_ONE_LAUNCH, backend=be)
+        self.launch1 = self.batch1.tune(reps=2)
+        self.batch1.run()
         be.synchronize()
         import halcuda
 
         self.graph = halcuda.Graph(be, self.batch.run)
+        self.graph1 = halcuda.Graph(be, self.batch1.run)
 
     def plain_element(self, R, x, op, base, mods, i):
         """One element with the HAL/ring calls of the reference, one launch per pass."""
@@ -373,6 +380,15 @@ def crt_batch_bench(be, steps, warmup, bpeak=None, peaks=None, elements=512):
     ev1.record(be)
     ms = ev0.elapsed_ms(ev1) / steps
     launches = (be.launch_count() - l0) // steps
+    # the one-launch form of the same batch
+    for _ in range(warmup):
+        w.graph1.launch()
+    be.synchronize()
+    ev0.record(be)
+    for _ in range(steps):
+        w.graph1.launch()
+    ev1.record(be)
+    ms1 = ev0.elapsed_ms(ev1) / steps
     # host-side modulus lists are built outside the timed region
     plain_items = [(R, x, op, base, R.mods_for(base)) for R, x, op, base in w.items]
     w.plain_element(*plain_items[0], 0)
@@ -388,17 +404,18 @@ def crt_batch_bench(be, steps, warmup, bpeak=None, peaks=None, elements=512):
     rng = np.random.default_rng(17)
     picks = [(int(k), int(rng.integers(0, w.items[int(k)][1].shape[0])))
              for k in rng.integers(0, len(w.items), size=8)]
-    before = [w.items[k][1].rows(i, i + 1).to_numpy() for k, i in picks]
-    w.graph.launch()
-    be.synchronize()
-    for (k, i), x0 in zip(picks, before):
-        R, x, op, base = w.items[k]
-        y = be.tensor(x0)
-        R.pb_to_crt(y, base)
-        be.hal_mul_mont64(y, op.rows(i, i + 1), R.mods_for(base))
-        R.crt_to_pb(y, base)
-        if not np.array_equal(y.to_numpy(), x.rows(i, i + 1).to_numpy()):
-            raise RuntimeError("crt_batch: element %d of item %d differs from the plain form" % (i, k))
+    for graph, form in ((w.graph, "per-class"), (w.graph1, "one-launch")):
+        before = [w.items[k][1].rows(i, i + 1).to_numpy() for k, i in picks]
+        graph.launch()
+        be.synchronize()
+        for (k, i), x0 in zip(picks, before):
+            R, x, op, base = w.items[k]
+            y = be.tensor(x0)
+            R.pb_to_crt(y, base)
+            be.hal_mul_mont64(y, op.rows(i, i + 1), R.mods_for(base))
+            R.crt_to_pb(y, base)
+            if not np.array_equal(y.to_numpy(), x.rows(i, i + 1).to_numpy()):
+                raise RuntimeError("crt_batch (%s): element %d of item %d differs from the plain form" % (form, i, k))
     # roofline: exact 64-bit products (two transforms and the operand product per residue) and
     # algorithmic bytes (read x and the operand, write x: 24 B per residue)
     products = sum(x.shape[0] * len(base) * R.n * (2 * TRANSFORM_PRODUCTS["field_%d" % R.n] + 1)
@@ -416,12 +433,20 @@ def crt_batch_bench(be, steps, warmup, bpeak=None, peaks=None, elements=512):
     return {"workload": "%d elements, field uniform in {field_36864, field_49152}, RNS length uniform in 4..24; "
                         "each pb->crt, mul_mont64 by an operand, crt->pb" % n,
             "elements": n, "slabs": w.batch.num_slabs, "residues": w.residues, "roofline": roof,
-            "checked": "8 seeded elements re-run after the timing: equal to the plain form",
+            "checked": "8 seeded elements re-run after the timing, in both forms: equal to the plain form",
             "crt_transforms_per_s": round(2 * n / (ms * 1e-3), 1),
             "plain_crt_transforms_per_s": round(2 * n / (plain_ms * 1e-3), 1),
             "ms_per_batch": round(ms, 4), "plain_ms_per_batch": round(plain_ms, 4),
             "launches_per_batch": launches, "plain_launches_per_batch": 9 * n,
-            "launch_shape": {"threads": w.launch[0], "ctas_per_sm": w.launch[1], "dim2_columns": 1 << w.launch[2]},
+            "launch_shape": {"threads": w.launch[0], "ctas_per_sm": w.launch[1], "dim2_columns": 1 << w.launch[2],
+                             "of": "the shape class with the most residues; each class has its own"},
+            "one_launch": {"crt_transforms_per_s": round(2 * n / (ms1 * 1e-3), 1), "ms_per_batch": round(ms1, 4),
+                           "launches_per_batch": 1,
+                           "int_roofline_frac": round(products / (ms1 * 1e-3) / bpeak, 4) if bpeak else None,
+                           "launch_shape": {"threads": w.launch1[0], "ctas_per_sm": w.launch1[1],
+                                            "dim2_columns": 1 << w.launch1[2]},
+                           "note": "every slab of both fields in one persistent launch with one shape "
+                                   "(HC_CRT_ONE_LAUNCH); the main figure runs one launch per field"},
             "autotuned": True, "l2": "inputs 2 x %.1f GB, larger than L2" % (w.residues * 8 / 1e9)}
 
 

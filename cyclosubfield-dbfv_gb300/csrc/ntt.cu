@@ -1068,7 +1068,8 @@ auto crt_batch_variant(const CrtLaunch& L) {
                                 : crt_batch_kernel<false, CLS, 256, 2>;
 }
 
-/// Shape class of specialised slab shapes (crt_batch_kernel's CLS): 1 field_36864, 2 field_49152.
+/// Shape class of specialised slab shapes (crt_batch_kernel's CLS): 1 field_36864, 2 field_49152
+/// (CLS 0: a launch over both).
 int crt_slab_kernel_class(int32_t shapes) { return (shapes & 0xff) == HC_SHAPE_L3072 ? 1 : 2; }
 
 hc_status launch_crt_batch(hc_context ctx, const CrtSlab* slabs, int nslabs, int* counter, size_t tile_words,
@@ -1076,7 +1077,8 @@ hc_status launch_crt_batch(hc_context ctx, const CrtSlab* slabs, int nslabs, int
     if (nslabs <= 0) return HC_OK;
     auto kern = generic    ? crt_batch_kernel<true, 0, 256, 2>
                 : cls == 1 ? crt_batch_variant<1>(L)
-                           : crt_batch_variant<2>(L);
+                : cls == 2 ? crt_batch_variant<2>(L)
+                           : crt_batch_variant<0>(L);
     if (L.threads < 32 || L.threads > 256 || L.threads % 32) return fail(HC_ERR_ARG, "batched transform: threads per CTA");
     if (L.logv < 0 || L.logv > 6) return fail(HC_ERR_ARG, "batched transform: dimension-2 tile width");
     const size_t smem = (tile_words + tw_words) * 8;

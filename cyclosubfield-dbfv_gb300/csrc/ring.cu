@@ -1976,12 +1976,22 @@ bool crt_generic(const std::vector<CrtSlab>& slabs) {
     return false;
 }
 
+/// The kernel class of a group's specialised slabs: their shape class when they all share one,
+/// else 0 (the kernel that carries both classes' code).
+int crt_group_kernel_class(const CrtGroup& g) {
+    if (g.host.empty()) return 0;
+    const int c = crt_slab_kernel_class(g.host[0].shapes);
+    for (const CrtSlab& s : g.host)
+        if (crt_slab_kernel_class(s.shapes) != c) return 0;
+    return c;
+}
+
 hc_status crt_group_run(hc_context ctx, CrtGroup& g) {
     size_t tile = 0;
     for (const CrtSlab& s : g.host) tile = std::max(tile, crt_tile_words(s, g.launch.logv));
     const bool generic = crt_generic(g.host);
     return launch_crt_batch(ctx, g.dev.as<CrtSlab>(), (int)g.host.size(), g.counter.as<int>(), tile, g.tw_words,
-                            g.launch, generic, generic ? 0 : crt_slab_kernel_class(g.host[0].shapes));
+                            g.launch, generic, generic ? 0 : crt_group_kernel_class(g));
 }
 
 /// Times every launch shape of the candidate set on a scratch copy of a sample of the group's
@@ -2014,7 +2024,7 @@ hc_status crt_group_tune(hc_context ctx, CrtGroup& g, int reps) {
     CrtLaunch best = g.launch;
     float best_ms = -1;
     const bool generic = crt_generic(g.host);
-    const int cls = generic ? 0 : crt_slab_kernel_class(g.host[0].shapes);
+    const int cls = generic ? 0 : crt_group_kernel_class(g);
     // 128 or 256 threads at 1..4 CTAs per SM
     const CrtLaunch shapes[] = {{128, 1, 0}, {128, 2, 0}, {128, 3, 0}, {128, 4, 0},
                                 {256, 1, 0}, {256, 2, 0}, {256, 3, 0}, {256, 4, 0}};
@@ -2061,6 +2071,8 @@ extern "C" {
 hc_status hc_crt_batch_create(hc_context ctx, const hc_crt_item* items, size_t n, int ops, hc_crt_batch* out) {
     return guard([&] {
         REQUIRE(ctx && out && (items || n == 0), HC_ERR_ARG, "null argument");
+        const bool one_launch = ops & HC_CRT_ONE_LAUNCH;
+        ops &= ~HC_CRT_ONE_LAUNCH;
         REQUIRE(ops > 0 && ops <= (HC_CRT_FORWARD | HC_CRT_MUL | HC_CRT_INVERSE), HC_ERR_ARG,
                 "batched transform: ops must combine HC_CRT_FORWARD, HC_CRT_MUL, HC_CRT_INVERSE");
         auto b = std::make_unique<hc_crt_batch_s>();
@@ -2114,7 +2126,7 @@ hc_status hc_crt_batch_create(hc_context ctx, const hc_crt_item* items, size_t n
         REQUIRE(slabs.size() < (size_t)INT32_MAX, HC_ERR_UNSUPPORTED, "batched transform: too many slabs");
         std::map<int, size_t> index;  // shape class -> group
         for (size_t i = 0; i < slabs.size(); i++) {
-            const int cls = crt_slab_class(slabs[i]);
+            const int cls = one_launch ? 0 : crt_slab_class(slabs[i]);
             auto it = index.find(cls);
             if (it == index.end()) {
                 it = index.emplace(cls, b->groups.size()).first;

@@ -261,6 +261,7 @@ class RingContext:
 
 
 CRT_FORWARD, CRT_MUL, CRT_INVERSE = 1, 2, 4
+CRT_ONE_LAUNCH = 8  # with the above: all slabs in one persistent launch (default: one per shape class)
 
 
 class _CrtItem(ctypes.Structure):

@@ -127,6 +127,8 @@ hc_status hc_bfv_hom_gal_batch(hc_ring ring, hc_view ct, const size_t* base, siz
 #define HC_CRT_FORWARD 1 /* period basis -> CRT basis (input bound 2) */
 #define HC_CRT_MUL 2     /* Montgomery product with `op` (CRT basis) */
 #define HC_CRT_INVERSE 4 /* CRT basis -> period basis */
+#define HC_CRT_ONE_LAUNCH 8 /* with the above: every slab in one persistent launch, one launch shape
+                             * (default: one launch per shape class, each with its own shape) */
 typedef struct hc_crt_batch_s* hc_crt_batch;
 typedef struct {
     hc_ring ring;

@@ -120,3 +120,21 @@ def test_crt_batch_one_launch_per_shape_class(po, be, rings):
     assert be.launch_count() - l0 == 1
     for dx, exp in checks1:
         assert (dx.to_numpy() == exp).all()
+
+
+@pytest.mark.parametrize("items", [ITEMS, [("field_36864", 2, [0, 1, 2], 1), ("field_49152", 2, [0, 1], 2)]],
+                         ids=["with-generic", "both-specialised"])
+def test_crt_batch_one_launch_option(po, be, rings, items):
+    """HC_CRT_ONE_LAUNCH: every slab in one persistent launch (the kernel carrying both specialised
+    classes, or the generic programme), bit-exact like the per-class form."""
+    import ringcuda
+
+    batch, checks = build(po, rings, 29, 7 | ringcuda.CRT_ONE_LAUNCH, items=items)
+    shape = batch.tune(reps=1)
+    assert batch.launch == shape
+    l0 = be.launch_count()
+    batch.run()
+    be.synchronize()
+    assert be.launch_count() - l0 == 1
+    for i, (dx, exp) in enumerate(checks):
+        assert (dx.to_numpy() == exp).all(), "item %d" % i
