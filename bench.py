@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--no-homcrt", action="store_true", help="skip the homomorphic CRT transform workload")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     ap.add_argument("--no-trait-path", action="store_true", help="skip the trait-level ct-mult")
+    ap.add_argument("--no-rns-lengths", action="store_true", help="skip the ct-mult at r = 12 and r = 20")
     ap.add_argument("--crt-elements", type=int, default=512,
                     help="elements of the batched CRT workload with --only crt_batch (512: the configuration's)")
     ap.add_argument("--only", choices=["crt_batch", "homcrt", "serving", "trait_path"],
@@ -241,12 +242,12 @@ class ClockSampler:
 
 # ------------------------------------------------------------------------------ workload
 class Workload:
-    def __init__(self, be, batch, seed=2026):
+    def __init__(self, be, batch, seed=2026, log2_q=LOG2_Q):
         import halcuda
         import ringcuda
 
         self.be = be
-        self.ring = ringcuda.RingContext(FIELD, LOG2_Q[0], LOG2_Q[1], T_BITS, backend=be)
+        self.ring = ringcuda.RingContext(FIELD, log2_q[0], log2_q[1], T_BITS, backend=be)
         R = self.ring
         self.base = R.initial_base()
         self.r = len(self.base)
@@ -683,6 +684,30 @@ def single_steps(be, work, steps, streams, start=0):
         e.wait(be)
     ev1.record(be)
     return ev0.elapsed_ms(ev1)
+
+
+def rns_length_bench(be, streams, scratch, steps=100):
+    """The ct-mult at the other ends of the configuration's RNS range, r = 12 and r = 20 (log2 q in
+    660..690 and 1120..1150): one per launch (graph replays on the streams, as the headline) and
+    8 per call; the same seeded workload construction as r = 16."""
+    out = {}
+    for lo, hi in ((660, 690), (1120, 1150)):
+        w = Workload(be, 8, log2_q=(lo, hi))
+        for g in w.single:
+            g.launch()
+        single_steps(be, w, 8, streams)
+        be.synchronize()
+        ms = single_steps(be, w, steps, streams)
+        timed_steps(be, w, 2, scratch)
+        nb = 20
+        bms = timed_steps(be, w, nb, scratch)
+        be.synchronize()
+        out["r%d" % w.r] = {"log2_q": [lo, hi], "rns_len": w.r, "gadget_digits": len(w.digits),
+                            "ct_mults_per_s": round(steps / (ms * 1e-3), 1),
+                            "batched_ct_mults_per_s": round(w.batch * nb / (bms * 1e-3), 1)}
+        w.single, w.graph = [], None
+        w.ring.close()
+    return out
 
 
 def plain_calls(be, work, rounds, scratch):
@@ -1247,6 +1272,7 @@ def main():
     e2e_val = dist.world * e2e_n / (e2e_ms * 1e-3)
     roof = kernel_roofline(be, work.ring, work.base, 20, peaks)
     trait = None if args.no_trait_path else trait_path_bench(be, work)
+    rns = None if args.no_rns_lengths else rns_length_bench(be, streams, scratch)
     bpeak = halcuda.barrett_peak(be)
     int8 = halcuda.int8_mma_peak(be)
     transforms = transform_rooflines(be, 10, peaks)
@@ -1309,6 +1335,8 @@ def main():
     }
     if trait:
         line["trait_path"] = trait
+    if rns:
+        line["rns_lengths"] = rns
     if crt:
         line["crt_batch"] = crt
     if hcrt:
