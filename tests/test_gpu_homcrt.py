@@ -119,3 +119,31 @@ def test_hom_cyclic_transform(setups, name, length, log2_b, log2_t, dct, budget)
     got = ringcuda.dbfv_hom_cyclic_transform(d, log2_b, log2_t, S["g"], coeffs, d.tensor(ct), base, ks).to_numpy()
     assert got.shape == exp.shape
     assert (got == exp).all()
+
+
+@pytest.mark.parametrize("budget", [100, 1])
+def test_hom_cyclic_transform_back_to_back(setups, be, budget):
+    """Several transforms issued back to back with different coefficients and no synchronisation
+    between them: each call's coefficient digits travel through the ring's pinned staging buffer
+    without blocking the host, so a later call must not overwrite an upload still in flight; every
+    result equals the oracle's."""
+    import ringcuda
+
+    S = setups("field_49152")
+    o, d, base = S["o"], S["d"], S["base"]
+    m = o.info["m"]
+    length, log2_b, log2_t, dct = 12, 6, 18, 3
+    baby, giant = bsgs_split(length)
+    gs = sorted(set([pow_mod(S["g"], j, m) for j in range(1, baby)] + [pow_mod(S["g"], baby, m)]))
+    gks = keys_for(S, gs)
+    ks = make_keyset(S, gks, budget)
+    rng = np.random.default_rng(91)
+    ct = residues(rng, o.shape(2 * dct, len(base)), [o.primes[i] for i in base])
+    dct_t = d.tensor(ct)
+    t = 1 << log2_t
+    sets = [[[int(v) for v in rng.integers(-t, t, size=o.dl)] for _ in range(length)] for _ in range(4)]
+    outs = [ringcuda.dbfv_hom_cyclic_transform(d, log2_b, log2_t, S["g"], c, dct_t, base, ks) for c in sets]
+    be.synchronize()
+    for c, got in zip(sets, outs):
+        exp = o.dbfv_hom_cyclic_transform(log2_b, log2_t, S["g"], c, ct, base, gks, S["digits"])
+        assert (got.to_numpy() == exp).all()
