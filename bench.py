@@ -777,7 +777,7 @@ def e2e_steps(be, work, steps, nslots=4):
 
 # DRAM bytes (read + written) of one launch of that kernel on the [24, 34, 12, 3072] tensor, and
 # the busy fraction of the integer multiply (fmaheavy, IMAD family) pipe over its elapsed cycles,
-# from one ncu capture of `python bench.py --roofline-only` (None: not captured for this build).
+# from one ncu capture of `python bench.py --roofline-only` (None: not captured for the current kernels).
 NCU_TRAFFIC_BYTES = 240779264 + 183514624
 NCU_IMAD_PIPE_FRAC = 0.782
 ROOF_ROWS = 24  # ciphertext rows of the roofline tensor: 240 MB, larger than L2
