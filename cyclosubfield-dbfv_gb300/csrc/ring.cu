@@ -29,7 +29,7 @@ hc_status launch_bconv_fused(hc_context ctx, const KView& src, const KView& dst,
 hc_status launch_galois(hc_context ctx, const KView& d, const KView& s, const uint32_t* p2, const uint32_t* p3);
 hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys, int nterms, const KView* add0,
                            const KView* add1, int full0, int full1, const KView& dst, const KMods& m,
-                           const int64_t* one_dev, const uint32_t* p2, const uint32_t* p3);
+                           const int64_t* one_dev, const uint32_t* p2, const uint32_t* p3, bool reverse = false);
 hc_status launch_tensor(hc_context ctx, const KView& d, const KView& lhs_lo, const KView& lhs_hi, const KView& rhs_lo,
                         const KView& rhs_hi, int rsplit, const KMods& m, int f0,
                         int f1, int f2);
@@ -1298,7 +1298,7 @@ void check_keys(hc_ring R, const hc_view& keys, int64_t r, size_t nd) {
 /// out [2B, r] (rows 2i, 2i + 1).
 void keyswitch(hc_ring R, const hc_view& parts, const hc_view& keys, const Base& base, size_t nd,
                const hc_view* add0, const hc_view* add1, const hc_view& out, const uint32_t* p2 = nullptr,
-               const uint32_t* p3 = nullptr) {
+               const uint32_t* p3 = nullptr, bool reverse = false) {
     const int64_t r = (int64_t)base.size(), B = out.shape[0] / 2;
     check_keys(R, keys, r, nd);
     REQUIRE(parts.shape[0] == B * (int64_t)nd, HC_ERR_SHAPE, "gadget digits per ciphertext");
@@ -1316,7 +1316,8 @@ void keyswitch(hc_ring R, const hc_view& parts, const hc_view& keys, const Base&
     KView a0 = add0 ? kv(*add0) : KView(), a1 = add1 ? kv(*add1) : KView();
     int64_t minp = R->min_p(base);
     CK(launch_keyswitch(R->ctx, pv.data(), kvv.data(), (int)nd, add0 ? &a0 : nullptr, add1 ? &a1 : nullptr,
-                        needs_full(b0, minp), needs_full(b1, minp), kv(out), R->kmods(base), R->one_dev(base), p2, p3));
+                        needs_full(b0, minp), needs_full(b1, minp), kv(out), R->kmods(base), R->one_dev(base), p2, p3,
+                        reverse));
 }
 
 /// Independent work of one call on the ring's side stream: begin() orders the branch after the
@@ -2316,9 +2317,12 @@ void hom_gal_keyset(hc_ring R, const hc_view& ct, const Base& b, const std::vect
     R->transform(c1.view(), b, true, nullptr, &c1_crt);
     Tensor parts = gadget_decompose(R, c1.view(), b, dg);
     hc_view c0 = vstep(ct, 0, 2, B);
+    // consecutive key switches over the same digits alternate their tile order (KsArgs::reverse)
+    size_t launched = 0;
     ks->each(gs, [&](size_t gi, const hc_view& key) {
         PermCache& pc = R->perms(gs[gi]);
-        keyswitch(R, parts.view(), key, b, dg.size(), &c0, nullptr, outs[gi], pc.p2.as<uint32_t>(), pc.p3.as<uint32_t>());
+        keyswitch(R, parts.view(), key, b, dg.size(), &c0, nullptr, outs[gi], pc.p2.as<uint32_t>(), pc.p3.as<uint32_t>(),
+                  (launched++ & 1) != 0);
     });
 }
 

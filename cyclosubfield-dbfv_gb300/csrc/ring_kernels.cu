@@ -238,6 +238,9 @@ struct KsArgs {
     // read, src/bfv.rs:819-820); null means identity
     const uint32_t* p2;
     const uint32_t* p3;
+    // tiles in reverse order: a launch that follows one over the same parts and summands starts
+    // on the tiles that launch read last, which are still in L2
+    int reverse;
 };
 
 __device__ __forceinline__ int64_t finish_wide(i128 acc, bool full, const KMods& m, int j) {
@@ -292,7 +295,8 @@ __global__ void __launch_bounds__(256, 4) keyswitch_async_kernel(KsArgs a, KMods
     __shared__ longlong2 skey[KS_STAGES][2][256];
     const int tid = threadIdx.x;
     const int64_t tiles = lines * chunks;
-    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    for (int64_t t0 = blockIdx.x; t0 < tiles; t0 += gridDim.x) {
+        const int64_t tile = a.reverse ? tiles - 1 - t0 : t0;
         const int64_t i = tile % a.batch, u = tile / a.batch;
         const int64_t line = u / chunks;  // (j, k)
         const int64_t l = 2 * ((u - line * chunks) * blockDim.x + tid);
@@ -582,9 +586,10 @@ hc_status launch_galois(hc_context ctx, const KView& d, const KView& s, const ui
 
 hc_status launch_keyswitch(hc_context ctx, const KView* parts, const KView* keys, int nterms, const KView* add0,
                            const KView* add1, int full0, int full1, const KView& dst, const KMods& m,
-                           const int64_t* one_dev, const uint32_t* p2, const uint32_t* p3) {
+                           const int64_t* one_dev, const uint32_t* p2, const uint32_t* p3, bool reverse) {
     if (nterms > HC_MAX_TERMS) return fail(HC_ERR_UNSUPPORTED, "too many gadget digits");
     KsArgs a;
+    a.reverse = reverse;
     for (int t = 0; t < nterms; t++) a.parts[t] = parts[t], a.keys[t] = keys[t];
     a.nterms = nterms;
     a.has_add0 = add0 != nullptr;
