@@ -107,12 +107,14 @@ __device__ __forceinline__ void four_half(const fast::Ctx& c, const fast::SF& f0
 /// Fused pass of a field_49152 slab: CTA 3k + b of the cluster owns block b of row k.
 template <int DIR, bool POST>
 __global__ void __launch_bounds__(THREADS, 6)
-    crt_slab12288_kernel(KView t, KView src, PlanPtrs p2, PlanPtrs p3, KView m2, KView m3, KMods mods) {
+    crt_slab12288_kernel(KView t, KView src, PlanPtrs p2, PlanPtrs p3, KView m2, KView m3, KMods mods, int reverse) {
     extern __shared__ int64_t smem[];
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
     const int row = rank / 3, blk = rank - 3 * (rank / 3);
-    const int64_t slab = blockIdx.x / CLUSTER;
+    // reverse: the last slab first, so that the clusters scheduled first read what the producer
+    // of the input (or the other half of the transform) wrote last, still in L2
+    const int64_t slab = reverse ? gridDim.x / CLUSTER - 1 - blockIdx.x / CLUSTER : blockIdx.x / CLUSTER;
     const int64_t j = slab % t.n1, i = slab / t.n1;
     const DevPlanHeader* P2 = p2.p[j];
     const DevPlanHeader* P3 = p3.p[j];
@@ -191,7 +193,8 @@ __global__ void __launch_bounds__(THREADS, 6)
 
 template <class K>
 hc_status cluster_launch(hc_context ctx, K kern, int64_t slabs, size_t smem, const KView& t, const KView& src,
-                         const PlanPtrs& p2, const PlanPtrs& p3, const KView& m2, const KView& m3, const KMods& mods) {
+                         const PlanPtrs& p2, const PlanPtrs& p3, const KView& m2, const KView& m3, const KMods& mods,
+                         int reverse) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(slabs * CLUSTER), 1, 1);
     cfg.blockDim = dim3(THREADS, 1, 1);
@@ -204,7 +207,7 @@ hc_status cluster_launch(hc_context ctx, K kern, int64_t slabs, size_t smem, con
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    hc_status st = hc::cuda_check(cudaLaunchKernelEx(&cfg, kern, t, src, p2, p3, m2, m3, mods), "fused CRT pass launch");
+    hc_status st = hc::cuda_check(cudaLaunchKernelEx(&cfg, kern, t, src, p2, p3, m2, m3, mods, reverse), "fused CRT pass launch");
     hc::count_launch(ctx);
     return st;
 }
@@ -245,8 +248,8 @@ bool cluster_ready(K kern, size_t smem) {
 
 template <int DIR, bool POST>
 hc_status launch_fused(hc_context ctx, int64_t slabs, const KView& t, const KView& src, const PlanPtrs& p2,
-                       const PlanPtrs& p3, const KView& m2, const KView& m3, const KMods& mods) {
-    return cluster_launch(ctx, crt_slab12288_kernel<DIR, POST>, slabs, SMEM12288, t, src, p2, p3, m2, m3, mods);
+                       const PlanPtrs& p3, const KView& m2, const KView& m3, const KMods& mods, int reverse) {
+    return cluster_launch(ctx, crt_slab12288_kernel<DIR, POST>, slabs, SMEM12288, t, src, p2, p3, m2, m3, mods, reverse);
 }
 
 /// Whether a transform's plans are field_49152's shapes ([4] along dimension 2, [3, 64, 64] along
@@ -293,9 +296,11 @@ hc_status launch_crt_pass(hc_context ctx, int dir, const KView& t, const KView* 
     const int64_t slabs = t.n0 * t.n1;
     if (slabs == 0) return HC_OK;
     const KView& s = src ? *src : t;
-    if (dir == 0) return launch_fused<0, false>(ctx, slabs, t, s, p2, p3, m2, m3, mods);
-    if (post) return launch_fused<1, true>(ctx, slabs, t, s, p2, p3, m2, m3, mods);
-    return launch_fused<1, false>(ctx, slabs, t, s, p2, p3, m2, m3, mods);
+    // the first half runs the slabs last to first (the input's producer wrote them first to last),
+    // the second half first to last (the first half wrote them last to first)
+    if (dir == 0) return launch_fused<0, false>(ctx, slabs, t, s, p2, p3, m2, m3, mods, 1);
+    if (post) return launch_fused<1, true>(ctx, slabs, t, s, p2, p3, m2, m3, mods, 0);
+    return launch_fused<1, false>(ctx, slabs, t, s, p2, p3, m2, m3, mods, 0);
 }
 
 }  // namespace hc
