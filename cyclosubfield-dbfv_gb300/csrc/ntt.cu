@@ -571,7 +571,10 @@ template <int SHAPE, int MODE, bool FIX>
 __global__ void __launch_bounds__(HC_COL_THREADS, SHAPE == HC_SHAPE_C12 ? HC_COL12_MIN_BLOCKS : 4) ntt_col_kernel(KView t, PlanPtrs plans, KView mul, KMods mods,
                                                                     int ncb, KView src) {
     __shared__ __align__(16) int64_t tws[HC_COL_TW];
-    const int64_t tile = blockIdx.x;
+    // tiles last to first: a transform's column pass follows a line pass (or the input's producer)
+    // that wrote the tensor first to last, so the CTAs scheduled first read what is still in L2,
+    // and the next line pass, first to last, starts on what this pass wrote last
+    const int64_t tile = gridDim.x - 1 - blockIdx.x;
     const int64_t cb = tile % ncb, r = tile / ncb;
     const int64_t j = r % t.n1, i = r / t.n1;
     const DevPlanHeader* P = plans.p[j];
