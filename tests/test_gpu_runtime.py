@@ -21,11 +21,13 @@ def test_bounded_event_wait_times_out_and_the_context_stays_usable(be, ring):
 
     base = ring.initial_base()
     plans = [be.hal_create_ntt_plan(ring.modulus(i), [2, 3, 8, 64]) for i in base]
-    t = ring.allocate(8, len(base))
+    t = ring.allocate(32, len(base))
     ev0, ev1 = halcuda.Event(), halcuda.Event()
     be.synchronize()
     ev0.record(be)
-    for _ in range(400):  # about 40 ms of inverse NTT passes over 38 MB
+    # 400 inverse NTT passes over 151 MB: the GPU needs several times longer for them than the host
+    # takes to issue them, so work is still queued when the bounded wait below starts
+    for _ in range(400):
         be.hal_intt_mont64_dim(t, plans, halcuda.DIM3)
     ev1.record(be)
     with pytest.raises(halcuda.HalError, match="error 5: event wait timed out"):
